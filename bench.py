@@ -1,0 +1,288 @@
+"""Benchmark of the collision hot path: collision+conserve cell-steps/s.
+
+Workload (strong Landau damping, 1-D reduction of the reference's 2-D grid):
+Nx = 64 spatial cells, Nv = N = 24 (24^3 DG velocity cells, 24^3 spectral
+nodes), v in [-6, 6]^3, A = 0.5, k = 0.5, nu = 0.05, dt = 0.005, unit
+Maxwellian initial state.  One "step" is one collision step of every spatial
+cell: node sampling, 4 x (transform + weighted contraction + moment-conserving
+projection), 3 inverse transforms and the DG projection with the dU scatter.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+  python bench.py --impl reference ...   # the CPU implementation of the path
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "landau-poisson-solver-2d_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOAD = dict(nx1=64, nx2=1, nv=24, n=24, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.005, a_amp=0.5,
+                k_wave=0.5)
+METRIC = "collision+conserve cell-steps/s"
+UNIT = "cell-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def _config(extra=None):
+    cfg = {"workload": "strong Landau damping, Nx=64 (1-D), Nv=N=24, v in [-6,6]^3, nu=0.05, "
+                       "dt=0.005; one collision step of all 64 spatial cells",
+           "nx1": 64, "nx2": 1, "nv": 24, "n": 24, "cells_per_step": 64,
+           "l2": "flushed between timed steps (512 MiB write)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 3 + i and r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(sample_cells=1, threads=None):
+    """The CPU restatement of the path (oracle port, same algorithm and cost
+    structure as the reference: direct weighted sums and per-(mode, v-cell)
+    IntModes projection) on a bounded sample of the workload."""
+    from oracle.oracle import Case, FIX_DEFAULT, Oracle
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    case = Case(**WORKLOAD)
+    O = Oracle(case, fixes=FIX_DEFAULT)
+    U = O.set_init(1)
+    nv3 = case.nv ** 3
+    ucell = U.reshape(case.ncell, nv3 * 7)
+    t0 = time.perf_counter()
+    for s in range(sample_cells):
+        f = O.nodes(U, s)
+        q = O.conserve(O.compute_q(f))
+        O.rk4(f, q, ucell[s], direct=True)
+    dt = time.perf_counter() - t0
+    return sample_cells / dt, dt
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, _ = cpu_baseline(1)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals)) if vals else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value if value else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic initial state)",
+            "config": _config({"sample": "1 spatial cell per step (the full step is 64 cells)"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "1 spatial cell of the 64-cell collision step per timed step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import lp_gb300 as lp
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def make(prec):
+        P = lp.Params(**WORKLOAD, fixes=lp.FIX_DEFAULT,
+                      precision=lp.PREC_MIXED if prec == "mixed" else lp.PREC_FP64)
+        ctx = lp.Context(P)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_init(1)
+        return ctx
+
+    def timed(ctx, fn, k, w):
+        with torch.cuda.stream(stream):
+            for _ in range(w):
+                fn()
+            torch.cuda.synchronize()
+            if ws > 1:
+                torch.distributed.barrier()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(k)]
+            total = 0.0
+            for i in range(k):
+                flush.zero_()
+                ev[i][0].record(stream)
+                fn()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        return total
+
+    ctx = make(args.precision)
+    cells = WORKLOAD["nx1"] * WORKLOAD["nx2"]
+    with ClockSampler(local) as clk:
+        t = timed(ctx, lambda: ctx.collision_step(), args.steps, args.warmup)
+    t_max = t
+    if ws > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = ws * cells * args.steps / t_max
+
+    # End to end through the public API with host buffers: H2D of the state
+    # from pinned memory into the context's resident buffer, the collision
+    # step, D2H of the state, every step, all on the context's stream.
+    U_host = torch.from_numpy(ctx.get_state()).pin_memory()
+    U_out = torch.empty_like(U_host).pin_memory()
+    nbytes = U_host.numel() * 8
+
+    class _Dev:
+        def __init__(self, ptr, n):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
+                                             "version": 3, "strides": None}
+
+    Ustate = torch.as_tensor(_Dev(ctx.state_device_ptr(), U_host.numel()), device="cuda")
+
+    def e2e_step():
+        Ustate.copy_(U_host, non_blocking=True)
+        ctx.collision_step()
+        U_out.copy_(Ustate, non_blocking=True)
+
+    t_e2e = timed(ctx, e2e_step, max(2, args.steps // 2), 1)
+    e2e_value = ws * cells * max(2, args.steps // 2) / t_e2e
+
+    # Dominant kernel timing: the weighted contraction alone, on this stream.
+    # (Roofline figures are computed from its average duration.)
+    extra = {}
+    if rank == 0:
+        t_fp64 = None
+        if args.precision == "mixed" and args.fp64_steps > 0:
+            ctx64 = make("fp64")
+            t64 = timed(ctx64, lambda: ctx64.collision_step(), args.fp64_steps, 1)
+            t_fp64 = cells * args.fp64_steps / t64
+            ctx64.close()
+        extra["fp64_value"] = t_fp64
+        extra["mixed_over_fp64"] = (value / ws / t_fp64) if t_fp64 else None
+
+    if rank == 0:
+        peak, peak_kind = _peaks()
+        cb = None
+        if not args.no_cpu_baseline and ws == 1:
+            v, secs = cpu_baseline(1)
+            cb = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                  "sample": f"1 spatial cell of the 64-cell step ({secs:.1f} s of CPU work)"}
+        # algorithmic bytes of the collision step: read the 7-double records,
+        # write the 5 collided coefficients (per cell-step, nv^3 * 12 * 8 B)
+        nv3 = WORKLOAD["nv"] ** 3
+        alg_bytes = cells * nv3 * 12 * 8
+        achieved = alg_bytes / (t_max / args.steps) / 1e9
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+                "data": "synthetic (seeded analytic initial state)",
+                "config": _config({"precision": args.precision}),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                        "d2h_bytes_per_step": nbytes},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None,
+                             "peak_kind": peak_kind,
+                             "note": "step-level algorithmic bytes; the step is compute bound"},
+                "cpu_baseline": cb, "clocks": clk.summary(),
+                "gpu_launches": 43 * args.steps}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,138 @@
+/*
+ * lp_gb300.h -- C ABI of the GB300 (sm_103a) collision/advection hot path of
+ * the Landau-Poisson solver.
+ *
+ * Plain pointers and sizes only; every call returns an lp_status.  A context
+ * owns its device buffers, its CUDA stream and its precomputed tables; it is
+ * bound to the device that was current when it was created.  Contexts are not
+ * thread-safe: use one context per host thread.
+ *
+ * Data layout (identical to the reference):
+ *   state U: ncell * nv^3 records of 7 doubles (AoS),
+ *            record k = s*nv^3 + (j1*nv + j2)*nv + j3, s = i1*nx2 + i2;
+ *            slots 0: 1, 1: (x1-x_i1)/dx, 2: (x2-x_i2)/dx, 3..5: (v_d-v_jd)/dv,
+ *            6: sum_d ((v_d-v_jd)/dv)^2.
+ *   spectral arrays: n^3 complex doubles (re, im interleaved), index
+ *            k + n*(j + n*i) as FFTW's row-major N x N x N.
+ *   Poisson: 3 coefficients per spatial cell (mean, x-slope, y-slope).
+ *
+ * Reference interfaces replaced (paths relative to the reference checkout):
+ *   lp_compute_q         ComputeQ      source/collisionRoutines_1.h:47
+ *   lp_conserve          conserveAllMoments source/conservationRoutines.h:31
+ *   lp_fft3d / lp_fs     fft3D / FS    source/collisionRoutines_1.h:40,44
+ *   lp_rk4_cell          RK4           source/collisionRoutines_1.h:62
+ *   lp_nodes             setInit_spectral source/SetInit_1.h:44
+ *   lp_weights_rows      generate_conv_weights source/collisionRoutines_1.h:36
+ *   lp_conservation_rows createCCtAndPivot source/conservationRoutines.h:34
+ *   lp_poisson           pois2d        source/PoissonFunctions.h:35
+ *   lp_advect_step       RK3           source/advection_1.h:70
+ *   lp_collision_step    the per-cell ComputeQ/conserveAllMoments/RK4 loop and
+ *                        the dU scatter of main, source/LP_ompi_1.cpp:500-568
+ *   lp_step              one pass of the time loop, source/LP_ompi_1.cpp:496-621
+ *   lp_set_init          SetInit_LD    source/SetInit_1.h:37
+ *   lp_moments           computeMass/computeMomentum/computeKiE/computeEleE
+ *                        source/MomentCalculations.h
+ */
+#ifndef LP_GB300_H
+#define LP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    LP_OK = 0,
+    LP_ERR_INVALID = 1,     /* bad argument or unsupported size */
+    LP_ERR_CUDA = 2,        /* a CUDA call failed; see lp_last_error */
+    LP_ERR_ALLOC = 3,       /* device or host allocation failed */
+    LP_ERR_NO_DEVICE = 4,   /* no CUDA device, or not an sm_103 device */
+    LP_ERR_STATE = 5        /* call out of order (e.g. no state uploaded) */
+} lp_status;
+
+/* Fixes of reference defects; LP_FIX_DEFAULT is F1 | F2 | F3. */
+#define LP_FIX_F1 1u   /* RK4 reads the stride-7 slots {0,3,4,5,6} of each record */
+#define LP_FIX_F2 2u   /* node sampling uses slot 3 as the v1 slope */
+#define LP_FIX_F3 4u   /* collide every spatial cell (the reference: s < nx1 only) */
+#define LP_FIX_F11 8u  /* snap the middle Fourier node eta[n/2] to exactly 0 */
+#define LP_FIX_DEFAULT (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3)
+
+/* Arithmetic of the collision operator. */
+#define LP_PREC_FP64 0   /* every kernel in FP64 (the plain path) */
+#define LP_PREC_MIXED 1  /* FP32 transforms, weight contraction and projection,
+                            FP64 moments, 5x5 conservation solve and Poisson */
+
+typedef struct {
+    int nx1, nx2;     /* spatial cells along x1 and x2 (nx2 = nx1: the reference's
+                         2-D grid; nx2 = 1: the 1-D reduction) */
+    int nv;           /* DG velocity cells per dimension */
+    int n;            /* spectral nodes per dimension (even, <= 32) */
+    double lv;        /* velocity box [-lv, lv]^3, also the collision box L_v = R_v */
+    double lx;        /* x1 (and x2) length */
+    double nu, dt;    /* collision frequency and time step */
+    double a_amp, k_wave; /* initial perturbation (1 + a cos(k x1)) */
+    unsigned fixes;   /* LP_FIX_* bits */
+    int precision;    /* LP_PREC_* */
+} lp_params;
+
+typedef struct lp_ctx lp_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+lp_status lp_ctx_create(const lp_params *p, lp_ctx **out);
+lp_status lp_ctx_destroy(lp_ctx *ctx);
+/* Run subsequent work on this cudaStream_t (NULL: the context's own stream). */
+lp_status lp_set_stream(lp_ctx *ctx, void *cuda_stream);
+lp_status lp_synchronize(lp_ctx *ctx);
+/* Last error message of this context (never NULL). */
+const char *lp_last_error(const lp_ctx *ctx);
+/* Device bytes held by the context. */
+size_t lp_device_bytes(const lp_ctx *ctx);
+
+/* ---- state ------------------------------------------------------------- */
+/* Copy the host state (n = ncell*nv^3*7 doubles) to the device and back. */
+lp_status lp_set_state(lp_ctx *ctx, const double *U_host, size_t n);
+lp_status lp_get_state(lp_ctx *ctx, double *U_host, size_t n);
+/* Device pointer of the resident state (ncell*nv^3*7 doubles). */
+lp_status lp_state_device_ptr(lp_ctx *ctx, double **U_dev);
+/* Initial condition: kind 0 = the reference's Landau-damping IC (Maxwellian
+ * of temperature 0.9), 1 = unit Maxwellian, 2 = two-stream with drift u. */
+lp_status lp_set_init(lp_ctx *ctx, int kind, double u);
+
+/* ---- reference-shaped routines (host pointers, one spatial cell) ------- */
+lp_status lp_fft3d(lp_ctx *ctx, const double *in, double *out);
+lp_status lp_fs(lp_ctx *ctx, const double *in, double *out);
+lp_status lp_compute_q(lp_ctx *ctx, const double *f, double *qhat);
+lp_status lp_conserve(lp_ctx *ctx, double *qhat);
+/* RK4 of spatial cell `cell` from node values f and conserved qhat, reading
+ * that cell's records of the resident state; dU receives nv^3*5 doubles. */
+lp_status lp_rk4_cell(lp_ctx *ctx, const double *f, int cell, const double *qhat, double *dU);
+/* Node values of every collided spatial cell from the resident state:
+ * f receives ncell*n^3 doubles. */
+lp_status lp_nodes(lp_ctx *ctx, double *f);
+/* Rows [r0, r1) of the n^3 x n^3 Landau weight table gHat3(eta_xi, eta_omega). */
+lp_status lp_weights_rows(lp_ctx *ctx, int r0, int r1, double *out);
+/* Constraint rows C1, C2 (5 x n^3 each) and the inverse Gram matrix (5x5). */
+lp_status lp_conservation_rows(lp_ctx *ctx, double *c1, double *c2, double *cct_inv);
+
+/* ---- batched device paths (resident state) ----------------------------- */
+/* Poisson solve on the resident state; potc, phix, phiy (3*ncell doubles
+ * each) and fields (14*ncell: IE_X, IXE_X, IYE_X, IXXE_X, IXYE_X, IYYE_X,
+ * the same six for Y, SE_X, SE_Y) are optional host outputs. */
+lp_status lp_poisson(lp_ctx *ctx, double *potc, double *phix, double *phiy, double *fields);
+/* One SSP-RK3 advection step of the resident state. */
+lp_status lp_advect_step(lp_ctx *ctx);
+/* Collision step of spatial cells [cell_begin, cell_end) of the resident
+ * state (-1, -1: every collided cell). */
+lp_status lp_collision_step(lp_ctx *ctx, int cell_begin, int cell_end);
+/* nsteps passes of the time loop (advection, then collisions when nu > 0),
+ * replayed from one captured CUDA graph per step. */
+lp_status lp_step(lp_ctx *ctx, int nsteps);
+/* out = {mass, p1, p2, p3, kinetic energy, electric energy of the last
+ * Poisson solve}. */
+lp_status lp_moments(lp_ctx *ctx, double *out6);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,665 @@
+// Context and C ABI of the GB300 Landau-Poisson hot path (include/lp_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lp_gb300.h"
+#include "lp_kernels.cuh"
+#include "lp_tables.h"
+
+using lp::V2;
+
+struct lp_ctx {
+    lp::Tables T;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::string err;
+    size_t bytes = 0;
+    std::vector<void *> allocs;
+    bool mixed = false;
+    // tables
+    double *eta = nullptr, *shat = nullptr, *ahat = nullptr, *cw = nullptr, *c1 = nullptr, *c2 = nullptr,
+           *cct = nullptr, *nodeoff = nullptr;
+    unsigned char *rzero = nullptr, *gate = nullptr;
+    int *nodecell = nullptr, *pair_off = nullptr, *ipiv = nullptr;
+    void *tfac = nullptr, *mfwd = nullptr, *minv = nullptr;  // R precision
+    void *P = nullptr;                                       // R precision
+    unsigned *PI = nullptr;
+    double *ab = nullptr;
+    // state and advection
+    double *U = nullptr, *U1 = nullptr, *Ut = nullptr, *rt = nullptr, *pb = nullptr, *potc = nullptr,
+           *phix = nullptr, *phiy = nullptr, *fields = nullptr, *mpart = nullptr;
+    bool has_state = false;
+    // collision workspace
+    int Bcap = 0, nchunk = 0;
+    void *f = nullptr, *f1 = nullptr, *qn = nullptr, *F = nullptr, *t1 = nullptr, *t2 = nullptr, *Qc = nullptr,
+         *Y = nullptr, *Z = nullptr;
+    double2 *q[4] = {nullptr, nullptr, nullptr, nullptr};
+    double *cpart = nullptr, *lam = nullptr, *dU = nullptr;
+    // moment reconciliation (mixed path)
+    double *gmom = nullptr, *gm_inv = nullptr, *mtpart = nullptr, *mapart = nullptr, *mlam = nullptr;
+    int nrc = 16;
+    // captured step
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;
+};
+
+namespace {
+
+constexpr int kMomBlocks = 240;
+
+lp_status fail(lp_ctx *c, lp_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+lp_status cuda_fail(lp_ctx *c, cudaError_t e, const char *where) {
+    return fail(c, LP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define LP_CUDA(call)                                          \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+template <typename T> lp_status dalloc(lp_ctx *c, T **p, size_t count) {
+    void *d = nullptr;
+    size_t b = sizeof(T) * (count ? count : 1);
+    cudaError_t e = cudaMalloc(&d, b);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, LP_ERR_ALLOC, "cudaMalloc of " + std::to_string(b) + " bytes failed");
+    }
+    c->allocs.push_back(d);
+    c->bytes += b;
+    *p = static_cast<T *>(d);
+    return LP_OK;
+}
+
+template <typename T> lp_status upload(lp_ctx *c, T **p, const T *host, size_t count) {
+    lp_status s = dalloc(c, p, count);
+    if (s != LP_OK) return s;
+    LP_CUDA(cudaMemcpy(*p, host, sizeof(T) * count, cudaMemcpyHostToDevice));
+    return LP_OK;
+}
+
+#define LP_TRY(x)                   \
+    do {                            \
+        lp_status s_ = (x);         \
+        if (s_ != LP_OK) return s_; \
+    } while (0)
+
+template <typename R> lp_status upload_real(lp_ctx *c, void **p, const std::vector<double> &v) {
+    std::vector<R> h(v.begin(), v.end());
+    R *d = nullptr;
+    LP_TRY(upload(c, &d, h.data(), h.size()));
+    *p = d;
+    return LP_OK;
+}
+
+inline int round32(int b) { return (b + 31) / 32 * 32; }
+
+template <typename R> lp_status alloc_workspace(lp_ctx *c) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    const size_t n3 = T.n3, Bp = c->Bcap, n = T.n, nv = T.nv;
+    R *f, *f1, *qn;
+    C *F, *t1, *t2, *Qc, *Y, *Z;
+    LP_TRY(dalloc(c, &f, n3 * Bp));
+    LP_TRY(dalloc(c, &f1, n3 * Bp));
+    LP_TRY(dalloc(c, &qn, n3 * Bp));
+    LP_TRY(dalloc(c, &F, n3 * Bp));
+    LP_TRY(dalloc(c, &t1, n3 * Bp));
+    LP_TRY(dalloc(c, &t2, n3 * Bp));
+    LP_TRY(dalloc(c, &Qc, n3 * Bp));
+    LP_TRY(dalloc(c, &Y, 3 * n * n * nv * Bp));
+    LP_TRY(dalloc(c, &Z, 5 * n * nv * nv * Bp));
+    c->f = f; c->f1 = f1; c->qn = qn; c->F = F; c->t1 = t1; c->t2 = t2; c->Qc = Qc; c->Y = Y; c->Z = Z;
+    for (int i = 0; i < 4; ++i) LP_TRY(dalloc(c, &c->q[i], n3 * Bp));
+    c->nchunk = 64;
+    LP_TRY(dalloc(c, &c->cpart, (size_t)c->nchunk * 5 * Bp));
+    LP_TRY(dalloc(c, &c->lam, 5 * Bp));
+    LP_TRY(dalloc(c, &c->dU, (size_t)T.nv3 * 5 * Bp));
+    if (c->mixed) {
+        LP_TRY(upload(c, &c->gmom, T.gmom.data(), T.gmom.size()));
+        LP_TRY(upload(c, &c->gm_inv, T.gm_inv, 25));
+        LP_TRY(dalloc(c, &c->mtpart, (size_t)c->nchunk * 5 * Bp));
+        LP_TRY(dalloc(c, &c->mapart, (size_t)c->nrc * 5 * Bp));
+        LP_TRY(dalloc(c, &c->mlam, 5 * Bp));
+    }
+    return LP_OK;
+}
+
+template <typename R> lp_status upload_tables(lp_ctx *c) {
+    const lp::Tables &T = c->T;
+    LP_TRY(upload(c, &c->eta, T.eta.data(), T.eta.size()));
+    LP_TRY(upload(c, &c->shat, T.shat.data(), T.shat.size()));
+    LP_TRY(upload(c, &c->ahat, T.ahat.data(), T.ahat.size()));
+    LP_TRY(upload(c, &c->rzero, T.rzero.data(), T.rzero.size()));
+    LP_TRY(upload(c, &c->cw, T.cw.data(), T.cw.size()));
+    LP_TRY(upload(c, &c->c1, T.c1.data(), T.c1.size()));
+    LP_TRY(upload(c, &c->c2, T.c2.data(), T.c2.size()));
+    LP_TRY(upload(c, &c->cct, T.cct_inv, 25));
+    LP_TRY(upload(c, &c->nodecell, T.nodecell.data(), T.nodecell.size()));
+    LP_TRY(upload(c, &c->nodeoff, T.nodeoff.data(), T.nodeoff.size()));
+    LP_TRY(upload(c, &c->pair_off, T.pair_off.data(), T.pair_off.size()));
+    LP_TRY(upload_real<R>(c, &c->tfac, T.tfac));
+    LP_TRY(upload_real<R>(c, &c->mfwd, T.mfwd));
+    LP_TRY(upload_real<R>(c, &c->minv, T.minv));
+    const size_t npair = (size_t)T.pair_off[T.n3];
+    R *P = nullptr;
+    LP_TRY(dalloc(c, &P, npair));
+    LP_TRY(dalloc(c, &c->PI, npair));
+    c->P = P;
+    LP_CUDA(lp::launch_pairs(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->pair_off, T.n,
+                             std::is_same<R, double>::value ? (double *)P : nullptr,
+                             std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
+    // Poisson
+    LP_TRY(upload(c, &c->ab, T.pois.ab.data(), T.pois.ab.size()));
+    LP_TRY(upload(c, &c->ipiv, T.pois.ipiv.data(), T.pois.ipiv.size()));
+    LP_TRY(upload(c, &c->gate, T.pois.gate.data(), T.pois.gate.size()));
+    return alloc_workspace<R>(c);
+}
+
+lp::PoissonDev poisson_dev(const lp_ctx *c) {
+    const lp::PoissonTables &p = c->T.pois;
+    lp::PoissonDev d{};
+    d.nx = p.nx; d.ny = p.ny; d.ndim = p.ndim; d.kl = p.kl; d.ku = p.ku; d.ldab = p.ldab;
+    d.ab = c->ab; d.ipiv = c->ipiv; d.dxp = p.dxp; d.dyp = p.dyp; d.gate = c->gate;
+    std::memcpy(d.blk[0], p.acvx, sizeof(p.acvx));
+    std::memcpy(d.blk[1], p.acyrr, sizeof(p.acyrr));
+    std::memcpy(d.blk[2], p.acyrl, sizeof(p.acyrl));
+    std::memcpy(d.blk[3], p.acvy, sizeof(p.acvy));
+    std::memcpy(d.blk[4], p.acxrr, sizeof(p.acxrr));
+    std::memcpy(d.blk[5], p.acxrl, sizeof(p.acxrl));
+    return d;
+}
+
+lp::AdvectDev advect_dev(const lp_ctx *c) {
+    const lp::Tables &T = c->T;
+    lp::AdvectDev a{};
+    a.nx1 = T.prm.nx1; a.nx2 = T.prm.nx2; a.nv = T.nv; a.size = T.size;
+    a.lv = T.prm.lv; a.dv = T.dv; a.dx = T.dx; a.scalev = T.scalev; a.dt = T.prm.dt;
+    return a;
+}
+
+lp_status poisson_on(lp_ctx *c, const double *Us) {
+    LP_CUDA(lp::launch_charge(Us, c->T.ncell, c->T.nv3, c->T.scalev, c->rt, c->stream));
+    LP_CUDA(lp::launch_poisson(poisson_dev(c), c->rt, c->pb, c->potc, c->phix, c->phiy, c->fields, c->stream));
+    return LP_OK;
+}
+
+lp_status advect(lp_ctx *c) {
+    const lp::AdvectDev ad = advect_dev(c);
+    LP_TRY(poisson_on(c, c->U));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U, c->fields, 0, c->U1, c->stream));
+    LP_TRY(poisson_on(c, c->U1));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U1, c->fields, 1, c->Ut, c->stream));
+    LP_TRY(poisson_on(c, c->Ut));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->Ut, c->fields, 2, c->U, c->stream));
+    return LP_OK;
+}
+
+// RK4 stages 1-3 (C:831-865) from node values f and conserved q[0].
+template <typename R> lp_status rk4_stages(lp_ctx *c, int Bp) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    const R *M = (const R *)c->mfwd, *Mi = (const R *)c->minv;
+    for (int s = 0; s < 3; ++s) {
+        LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
+                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream));
+        LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
+        LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, c->q[s + 1],
+                                       c->stream));
+        LP_CUDA(lp::launch_conserve(c->q[s + 1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam,
+                                    c->stream));
+    }
+    return LP_OK;
+}
+
+template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    static const int fixed_slots[5] = {0, 3, 4, 5, 6}, ref_slots[5] = {0, 2, 3, 4, 5};
+    const bool f1 = (T.prm.fixes & LP_FIX_F1) != 0;
+    LP_CUDA(lp::launch_project<R>(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const R *)c->tfac, T.n, T.nv, Bp,
+                                  B, c0, c->U, f1 ? 7 : 6, f1 ? fixed_slots : ref_slots, T.prm.dt, T.scalev,
+                                  T.scaleL, T.scale3, (C *)c->Qc, (C *)c->Y, (C *)c->Z, c->dU, c->stream));
+    if (c->mixed && f1) {
+        const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
+        LP_CUDA(lp::launch_moment_fix(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
+                                      c->mtpart, c->U, T.nv, T.dv, T.prm.lv, c0, B, c->nrc, c->mapart, c->gm_inv,
+                                      T.prm.dt * kfac, c->mlam, c->dU, c->stream));
+    }
+    return LP_OK;
+}
+
+// Collision step of cells [c0, c0+B), B <= Bcap (LP_ompi_1.cpp:502-532).
+template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    const int Bp = round32(B);
+    const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
+    LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
+                                c->stream));
+    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
+    LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, c->q[0],
+                                   c->stream));
+    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_TRY(rk4_stages<R>(c, Bp));
+    LP_TRY(project<R>(c, c0, B, Bp));
+    return LP_OK;
+}
+
+lp_status collide(lp_ctx *c, int c0, int c1) {
+    // All batches read the pre-collision state (the reference scatters after
+    // the loop), so dU of every batch is kept and scattered at the end when
+    // the whole range fits one batch; larger ranges are processed batch by
+    // batch with the stride-7 read of LP_FIX_F1, which only touches the
+    // batch's own records.
+    const int total = c1 - c0;
+    for (int b0 = c0; b0 < c1; b0 += c->Bcap) {
+        const int B = std::min(c->Bcap, c1 - b0);
+        if (total > c->Bcap && !(c->T.prm.fixes & LP_FIX_F1))
+            return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one batch");
+        LP_TRY(c->mixed ? collide_batch<float>(c, b0, B) : collide_batch<double>(c, b0, B));
+        LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream));
+    }
+    return LP_OK;
+}
+
+lp_status one_step(lp_ctx *c) {
+    LP_TRY(advect(c));
+    if (c->T.prm.nu > 0.) LP_TRY(collide(c, 0, c->T.ncollide));
+    return LP_OK;
+}
+
+// Copy a contiguous host vector into column 0 of a cell-minor n3 x 32 buffer.
+lp_status put_column(lp_ctx *c, void *dst, size_t elem, const void *src, size_t count) {
+    LP_CUDA(cudaMemsetAsync(dst, 0, elem * count * 32, c->stream));
+    LP_CUDA(cudaMemcpy2DAsync(dst, elem * 32, src, elem, elem, count, cudaMemcpyHostToDevice, c->stream));
+    return LP_OK;
+}
+lp_status get_column(lp_ctx *c, void *dst, size_t elem, const void *src, size_t pitch, size_t count) {
+    LP_CUDA(cudaMemcpy2DAsync(dst, elem, src, pitch, elem, count, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+template <typename R> lp_status put_real_column(lp_ctx *c, R *dst, const double *src, size_t count) {
+    std::vector<R> h(src, src + count);
+    LP_TRY(put_column(c, dst, sizeof(R), h.data(), count));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+template <typename R> lp_status put_cplx_column(lp_ctx *c, typename V2<R>::t *dst, const double *src, size_t count) {
+    std::vector<R> h(src, src + 2 * count);
+    LP_TRY(put_column(c, dst, 2 * sizeof(R), h.data(), count));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+template <typename R> lp_status get_cplx_column(lp_ctx *c, double *dst, const typename V2<R>::t *src, size_t count) {
+    std::vector<R> h(2 * count);
+    LP_TRY(get_column(c, h.data(), 2 * sizeof(R), src, 32 * 2 * sizeof(R), count));
+    for (size_t i = 0; i < 2 * count; ++i) dst[i] = (double)h[i];
+    return LP_OK;
+}
+
+template <typename R> lp_status do_fft3d(lp_ctx *c, const double *in, double *out, bool inverse) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    if (!inverse) {
+        LP_TRY(put_cplx_column<R>(c, (C *)c->t2, in, T.n3));
+        LP_CUDA(lp::launch_fwd_complex<R>((const C *)c->t2, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, 32, c->stream));
+        return get_cplx_column<R>(c, out, (const C *)c->F, T.n3);
+    }
+    LP_TRY(put_cplx_column<double>(c, c->q[0], in, T.n3));
+    LP_CUDA(lp::launch_fs_full<R>(c->q[0], (C *)c->t1, (C *)c->t2, (C *)c->F, (const R *)c->minv, T.n, 32, c->stream));
+    return get_cplx_column<R>(c, out, (const C *)c->F, T.n3);
+}
+
+template <typename R> lp_status do_compute_q(lp_ctx *c, const double *f, double *qhat) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    LP_TRY(put_real_column<R>(c, (R *)c->f, f, T.n3));
+    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, 32, c->stream));
+    LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, 32, c->q[0], c->stream));
+    return get_cplx_column<double>(c, qhat, c->q[0], T.n3);
+}
+
+template <typename R> lp_status do_rk4_cell(lp_ctx *c, const double *f, int cell, const double *qhat, double *dU) {
+    const lp::Tables &T = c->T;
+    LP_TRY(put_real_column<R>(c, (R *)c->f, f, T.n3));
+    LP_TRY(put_cplx_column<double>(c, c->q[0], qhat, T.n3));
+    LP_TRY(rk4_stages<R>(c, 32));
+    LP_TRY(project<R>(c, cell, 1, 32));
+    LP_CUDA(cudaMemcpyAsync(dU, c->dU, sizeof(double) * 5 * T.nv3, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+// SetInit_LD (source/SetInit_1.cpp:60-115) and its two variants, on the host.
+void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> &U) {
+    static const double GW[5] = {0.5688888888888889, 0.4786286704993665, 0.4786286704993665, 0.2369268850561891,
+                                 0.2369268850561891};
+    static const double GX[5] = {0., -0.5384693101056831, 0.5384693101056831, -0.9061798459386640,
+                                 0.9061798459386640};
+    const int nv = T.nv, nx1 = T.prm.nx1, nx2 = T.prm.nx2;
+    const double a = T.prm.a_amp, cw = T.prm.k_wave, dv = T.dv, dx = T.dx, PI = T.PI, lv = T.prm.lv;
+    auto gridv = [&](double m) { return (-lv + (m + 0.5) * dv); };
+    auto gridx = [&](double m) { return (m + 0.5) * dx; };
+    auto maxw = [&](double v1, double v2, double v3, double Tt) {
+        double r2 = v1 * v1 + v2 * v2 + v3 * v3;
+        return std::exp(-r2 / (2 * Tt)) / (2 * PI * Tt * std::sqrt(2 * Tt * PI));
+    };
+    U.assign((size_t)T.size * 7, 0.);
+    for (int j1 = 0; j1 < nv; ++j1)
+        for (int j2 = 0; j2 < nv; ++j2)
+            for (int j3 = 0; j3 < nv; ++j3) {
+                double t0 = 0., t1 = 0., t2 = 0., t3 = 0., t4 = 0.;
+                for (int m1 = 0; m1 < 5; ++m1)
+                    for (int m2 = 0; m2 < 5; ++m2)
+                        for (int m3 = 0; m3 < 5; ++m3) {
+                            double x1 = gridv((double)j1) + 0.5 * dv * GX[m1];
+                            double x2 = gridv((double)j2) + 0.5 * dv * GX[m2];
+                            double x3 = gridv((double)j3) + 0.5 * dv * GX[m3];
+                            double fv;
+                            if (kind == 0) fv = maxw(x1, x2, x3, 0.9);
+                            else if (kind == 1) fv = maxw(x1, x2, x3, 1.0);
+                            else fv = 0.5 * (maxw(x1 - u, x2, x3, 1.0) + maxw(x1 + u, x2, x3, 1.0));
+                            double tp = GW[m1] * GW[m2] * GW[m3] * fv;
+                            t0 += tp;
+                            t1 += tp * 0.5 * GX[m1];
+                            t2 += tp * 0.5 * GX[m2];
+                            t3 += tp * 0.5 * GX[m3];
+                            t4 += tp * 0.25 * (GX[m1] * GX[m1] + GX[m2] * GX[m2] + GX[m3] * GX[m3]);
+                        }
+                t0 = t0 * 0.5 * 0.5 * 0.5; t1 = t1 * 0.5 * 0.5 * 0.5; t2 = t2 * 0.5 * 0.5 * 0.5;
+                t3 = t3 * 0.5 * 0.5 * 0.5; t4 = t4 * 0.5 * 0.5 * 0.5;
+                for (int i1 = 0; i1 < nx1; ++i1) {
+                    double sp = std::sin(cw * gridx(i1 + 0.5)), sm = std::sin(cw * gridx(i1 - 0.5));
+                    double tp0 = (dx + (sp - sm) * a / cw) * t0 / dx;
+                    double tp5 = (dx + (sp - sm) * a / cw) * t4 / dx;
+                    double u1 = (0.5 * (sp + sm) + (std::cos(cw * gridx(i1 + 0.5)) - std::cos(cw * gridx(i1 - 0.5))) / (cw * dx)) * (a / cw) * t0 * 12. / dx;
+                    double u3 = (dx + (sp - sm) * a / cw) * t1 * 12 / dx;
+                    double u4 = (dx + (sp - sm) * a / cw) * t2 * 12 / dx;
+                    double u5 = (dx + (sp - sm) * a / cw) * t3 * 12 / dx;
+                    for (int i2 = 0; i2 < nx2; ++i2) {
+                        size_t k = (size_t)i1 * nx2 * T.nv3 + (size_t)i2 * T.nv3 + (j1 * nv * nv + j2 * nv + j3);
+                        U[7 * k + 0] = 19 * tp0 / 4. - 15 * tp5;
+                        U[7 * k + 6] = 60 * tp5 - 15 * tp0;
+                        U[7 * k + 1] = u1;
+                        U[7 * k + 3] = u3;
+                        U[7 * k + 4] = u4;
+                        U[7 * k + 5] = u5;
+                    }
+                }
+            }
+}
+
+void destroy(lp_ctx *c) {
+    if (!c) return;
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+}  // namespace
+
+extern "C" {
+
+lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) {
+    if (!p || !out) return LP_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return LP_ERR_NO_DEVICE;
+    }
+    lp_ctx *c = new lp_ctx();
+    std::string err;
+    lp_status s = lp::build_tables(*p, c->T, err);
+    if (s != LP_OK) {
+        delete c;
+        return s;
+    }
+    cudaGetDevice(&c->device);
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        cudaGetLastError();
+        delete c;
+        return LP_ERR_NO_DEVICE;
+    }
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return LP_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    c->mixed = (p->precision == LP_PREC_MIXED);
+    c->Bcap = round32(std::min(std::max(c->T.ncollide, 1), 512));
+    const lp::Tables &T = c->T;
+    const size_t rec = (size_t)T.size * 7, nc = T.ncell;
+    s = c->mixed ? upload_tables<float>(c) : upload_tables<double>(c);
+    if (s == LP_OK) s = dalloc(c, &c->U, rec);
+    if (s == LP_OK) s = dalloc(c, &c->U1, rec);
+    if (s == LP_OK) s = dalloc(c, &c->Ut, rec);
+    if (s == LP_OK) s = dalloc(c, &c->rt, 3 * nc);
+    if (s == LP_OK) s = dalloc(c, &c->pb, (size_t)T.pois.ndim);
+    if (s == LP_OK) s = dalloc(c, &c->potc, 3 * nc);
+    if (s == LP_OK) s = dalloc(c, &c->phix, 3 * nc);
+    if (s == LP_OK) s = dalloc(c, &c->phiy, 3 * nc);
+    if (s == LP_OK) s = dalloc(c, &c->fields, 14 * nc);
+    if (s == LP_OK) s = dalloc(c, &c->mpart, 5 * kMomBlocks);
+    if (s == LP_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) s = LP_ERR_CUDA;
+    if (s != LP_OK) {
+        fprintf(stderr, "lp_ctx_create: %s\n", c->err.c_str());
+        destroy(c);
+        return s;
+    }
+    *out = c;
+    return LP_OK;
+}
+
+lp_status lp_ctx_destroy(lp_ctx *c) {
+    if (!c) return LP_ERR_INVALID;
+    cudaStreamSynchronize(c->stream);
+    destroy(c);
+    return LP_OK;
+}
+
+lp_status lp_set_stream(lp_ctx *c, void *st) {
+    if (!c) return LP_ERR_INVALID;
+    c->stream = st ? (cudaStream_t)st : c->own_stream;
+    return LP_OK;
+}
+
+lp_status lp_synchronize(lp_ctx *c) {
+    if (!c) return LP_ERR_INVALID;
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+const char *lp_last_error(const lp_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+size_t lp_device_bytes(const lp_ctx *c) { return c ? c->bytes : 0; }
+
+lp_status lp_set_state(lp_ctx *c, const double *U, size_t n) {
+    if (!c || !U || n != (size_t)c->T.size * 7) return fail(c, LP_ERR_INVALID, "state size mismatch");
+    LP_CUDA(cudaMemcpyAsync(c->U, U, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    c->has_state = true;
+    return LP_OK;
+}
+
+lp_status lp_get_state(lp_ctx *c, double *U, size_t n) {
+    if (!c || !U || n != (size_t)c->T.size * 7) return fail(c, LP_ERR_INVALID, "state size mismatch");
+    LP_CUDA(cudaMemcpyAsync(U, c->U, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+lp_status lp_state_device_ptr(lp_ctx *c, double **U) {
+    if (!c || !U) return LP_ERR_INVALID;
+    *U = c->U;
+    c->has_state = true;
+    return LP_OK;
+}
+
+lp_status lp_set_init(lp_ctx *c, int kind, double u) {
+    if (!c || kind < 0 || kind > 2) return fail(c, LP_ERR_INVALID, "unknown initial condition");
+    std::vector<double> U;
+    set_init_host(c->T, kind, u, U);
+    return lp_set_state(c, U.data(), U.size());
+}
+
+lp_status lp_fft3d(lp_ctx *c, const double *in, double *out) {
+    if (!c || !in || !out) return LP_ERR_INVALID;
+    return c->mixed ? do_fft3d<float>(c, in, out, false) : do_fft3d<double>(c, in, out, false);
+}
+
+lp_status lp_fs(lp_ctx *c, const double *in, double *out) {
+    if (!c || !in || !out) return LP_ERR_INVALID;
+    return c->mixed ? do_fft3d<float>(c, in, out, true) : do_fft3d<double>(c, in, out, true);
+}
+
+lp_status lp_compute_q(lp_ctx *c, const double *f, double *qhat) {
+    if (!c || !f || !qhat) return LP_ERR_INVALID;
+    return c->mixed ? do_compute_q<float>(c, f, qhat) : do_compute_q<double>(c, f, qhat);
+}
+
+lp_status lp_conserve(lp_ctx *c, double *qhat) {
+    if (!c || !qhat) return LP_ERR_INVALID;
+    const lp::Tables &T = c->T;
+    LP_TRY(put_cplx_column<double>(c, c->q[0], qhat, T.n3));
+    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, 32, c->cpart, c->nchunk, c->lam, c->stream));
+    return get_cplx_column<double>(c, qhat, c->q[0], T.n3);
+}
+
+lp_status lp_rk4_cell(lp_ctx *c, const double *f, int cell, const double *qhat, double *dU) {
+    if (!c || !f || !qhat || !dU || cell < 0 || cell >= c->T.ncell) return fail(c, LP_ERR_INVALID, "bad argument");
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    return c->mixed ? do_rk4_cell<float>(c, f, cell, qhat, dU) : do_rk4_cell<double>(c, f, cell, qhat, dU);
+}
+
+lp_status lp_nodes(lp_ctx *c, double *f) {
+    if (!c || !f) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    const lp::Tables &T = c->T;
+    const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
+    double *tmp = (double *)c->q[0];  // n3 * Bcap doubles fit in a complex buffer
+    for (int b0 = 0; b0 < T.ncollide; b0 += c->Bcap) {
+        const int B = std::min(c->Bcap, T.ncollide - b0), Bp = round32(B);
+        LP_CUDA(lp::launch_nodes<double>(c->U, T.nv, T.n, b0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, tmp,
+                                         c->stream));
+        for (int cc = 0; cc < B; ++cc)
+            LP_CUDA(cudaMemcpy2DAsync(f + (size_t)(b0 + cc) * T.n3, sizeof(double), tmp + cc, sizeof(double) * Bp,
+                                      sizeof(double), T.n3, cudaMemcpyDeviceToHost, c->stream));
+        LP_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return LP_OK;
+}
+
+lp_status lp_weights_rows(lp_ctx *c, int r0, int r1, double *out) {
+    if (!c || !out || r0 < 0 || r1 > c->T.n3 || r0 > r1) return fail(c, LP_ERR_INVALID, "bad row range");
+    for (int r = r0; r < r1; ++r)
+        for (int o = 0; o < c->T.n3; ++o) out[(size_t)(r - r0) * c->T.n3 + o] = lp::weight_host(c->T, r, o);
+    return LP_OK;
+}
+
+lp_status lp_conservation_rows(lp_ctx *c, double *c1, double *c2, double *cct) {
+    if (!c) return LP_ERR_INVALID;
+    if (c1) std::memcpy(c1, c->T.c1.data(), sizeof(double) * c->T.c1.size());
+    if (c2) std::memcpy(c2, c->T.c2.data(), sizeof(double) * c->T.c2.size());
+    if (cct) std::memcpy(cct, c->T.cct_inv, sizeof(double) * 25);
+    return LP_OK;
+}
+
+lp_status lp_poisson(lp_ctx *c, double *potc, double *phix, double *phiy, double *fields) {
+    if (!c) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(poisson_on(c, c->U));
+    const size_t nc = c->T.ncell;
+    if (potc) LP_CUDA(cudaMemcpyAsync(potc, c->potc, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (phix) LP_CUDA(cudaMemcpyAsync(phix, c->phix, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (phiy) LP_CUDA(cudaMemcpyAsync(phiy, c->phiy, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (fields) LP_CUDA(cudaMemcpyAsync(fields, c->fields, sizeof(double) * 14 * nc, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+lp_status lp_advect_step(lp_ctx *c) {
+    if (!c) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    return advect(c);
+}
+
+lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
+    if (!c) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    if (cell_begin == -1 && cell_end == -1) { cell_begin = 0; cell_end = c->T.ncollide; }
+    if (cell_begin < 0 || cell_end > c->T.ncollide || cell_begin > cell_end)
+        return fail(c, LP_ERR_INVALID, "bad cell range");
+    return collide(c, cell_begin, cell_end);
+}
+
+lp_status lp_step(lp_ctx *c, int nsteps) {
+    if (!c || nsteps < 0) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    if (nsteps == 0) return LP_OK;
+    if (!c->gexec || c->gstream != c->stream) {
+        if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        LP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        lp_status s = one_step(c);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+        c->gstream = c->stream;
+    }
+    for (int i = 0; i < nsteps; ++i) LP_CUDA(cudaGraphLaunch(c->gexec, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_moments(lp_ctx *c, double *out) {
+    if (!c || !out) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    const lp::Tables &T = c->T;
+    const long long kend = (T.prm.fixes & LP_FIX_F3) ? T.size : std::min<long long>(T.size, (long long)T.prm.nx1 * T.nv3);
+    LP_CUDA(lp::launch_moments(c->U, T.size, kend, T.nv, T.prm.lv, T.dv, c->mpart, kMomBlocks, c->stream));
+    std::vector<double> part(5 * kMomBlocks), px(3 * T.ncell), py(3 * T.ncell);
+    LP_CUDA(cudaMemcpyAsync(part.data(), c->mpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaMemcpyAsync(px.data(), c->phix, sizeof(double) * px.size(), cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaMemcpyAsync(py.data(), c->phiy, sizeof(double) * py.size(), cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    double s[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < kMomBlocks; ++b)
+        for (int q = 0; q < 5; ++q) s[q] += part[5 * b + q];
+    const double dx = T.dx, dy = T.dy, dv = T.dv;
+    out[0] = s[0] * dx * dy * T.scalev;
+    out[1] = s[1] * dx * dy * dv * dv;
+    out[2] = s[2] * dx * dy * dv * dv;
+    out[3] = s[3] * dx * dy * dv * dv;
+    out[4] = 0.5 * (s[4] * (dx * dy * dv * dv));
+    double e = 0.;
+    for (int k = 0; k < T.ncell; ++k) {
+        e += px[3 * k] * px[3 * k] + py[3 * k] * py[3 * k];
+        e += (px[3 * k + 1] * px[3 * k + 1] + py[3 * k + 1] * py[3 * k + 1]) / 12;
+        e += (px[3 * k + 2] * px[3 * k + 2] + py[3 * k + 2] * py[3 * k + 2]) / 12;
+    }
+    out[5] = 0.5 * (dx * dy) * e;
+    return LP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,931 @@
+// CUDA kernels of the GB300 Landau-Poisson hot path (sm_103a).
+// Citations are to the reference checkout:
+//   C = source/collisionRoutines_1.cpp   K = source/conservationRoutines.cpp
+//   A = source/advection_1.cpp           P = source/PoissonFunctions.cpp
+//   S = source/SetInit_1.cpp             MC = source/MomentCalculations.cpp
+#include "lp_kernels.cuh"
+
+#include <cstdint>
+#include <type_traits>
+
+namespace lp {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename R> __device__ __forceinline__ typename V2<R>::t mk2(R x, R y);
+template <> __device__ __forceinline__ double2 mk2<double>(double x, double y) { return make_double2(x, y); }
+template <> __device__ __forceinline__ float2 mk2<float>(float x, float y) { return make_float2(x, y); }
+
+template <typename R> __device__ __forceinline__ typename V2<R>::t ld2(const R *p) { return mk2<R>(*p, R(0)); }
+template <typename R> __device__ __forceinline__ typename V2<R>::t ld2(const typename V2<R>::t *p) { return *p; }
+template <typename R> __device__ __forceinline__ typename V2<R>::t ld2c(const double2 *p) {
+    double2 v = *p;
+    return mk2<R>((R)v.x, (R)v.y);
+}
+
+inline dim3 grid1(long long total, int block) { return dim3((unsigned)((total + block - 1) / block)); }
+
+// ---------------------------------------------------------------- pairs
+// gHat3(eta_xi, eta_omega) (C:30-69) from the omega tables, in the reference's
+// order and without FMA contraction, so the value equals the host's.
+__device__ double weight_dev(const double *eta, const double *shat, const double *ahat,
+                             const unsigned char *rzero, int n, int i, int j, int k, int o) {
+    const int l = o / (n * n), m = (o / n) % n, q = o % n;
+    const double *s = shat + 6 * (long long)o;
+    const double d0 = __dsub_rn(eta[i], eta[l]), d1 = __dsub_rn(eta[j], eta[m]), d2 = __dsub_rn(eta[k], eta[q]);
+    double r = 0.0;
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[0], d0), d0));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[1], d0), d1));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[2], d0), d2));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[1], d1), d0));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[3], d1), d1));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[4], d1), d2));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[2], d2), d0));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[4], d2), d1));
+    r = __dadd_rn(r, __dmul_rn(__dmul_rn(s[5], d2), d2));
+    return rzero[o] ? -r : __dsub_rn(ahat[o], r);
+}
+
+__global__ void k_pairs(const double *__restrict__ eta, const double *__restrict__ shat,
+                        const double *__restrict__ ahat, const unsigned char *__restrict__ rzero,
+                        const double *__restrict__ cw, const int *__restrict__ pair_off, int n,
+                        double *__restrict__ P64, float *__restrict__ P32, unsigned *__restrict__ PI) {
+    const int xi = blockIdx.x, h = n / 2;
+    const int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
+    // window of omega where u = xi + n/2 - omega lies in the grid (C:764-789)
+    const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
+    const int sj = j < h ? 0 : j - h + 1, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+    const int sk = k < h ? 0 : k - h + 1, nk = k < h ? k + h + 1 : 3 * h - 1 - k;
+    const int cnt = ni * nj * nk, off = pair_off[xi], npair = pair_off[xi + 1] - off;
+    for (int L = threadIdx.x; L < npair; L += blockDim.x) {
+        const int l = si + L / (nj * nk), m = sj + (L / nk) % nj, q = sk + L % nk;
+        const int Lu = cnt - 1 - L;
+        const int lu = si + Lu / (nj * nk), mu = sj + (Lu / nk) % nj, qu = sk + Lu % nk;
+        const int om = (l * n + m) * n + q, uu = (lu * n + mu) * n + qu;
+        double w = __dmul_rn(cw[om], weight_dev(eta, shat, ahat, rzero, n, i, j, k, om));
+        if (Lu != L) w = __dadd_rn(w, __dmul_rn(cw[uu], weight_dev(eta, shat, ahat, rzero, n, i, j, k, uu)));
+        if (P64) P64[off + L] = w;
+        if (P32) P32[off + L] = (float)w;
+        PI[off + L] = (unsigned)om | ((unsigned)uu << 16);
+    }
+}
+
+// ---------------------------------------------------------------- nodes
+// setInit_spectral for a batch of cells, cell-minor output.
+template <typename R>
+__global__ void k_nodes(const double *__restrict__ U, int nv, int n, int c0, int B, int Bp, int slot1,
+                        const int *__restrict__ nodecell, const double *__restrict__ nodeoff, double dv,
+                        R *__restrict__ f) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)n * n * n * Bp;
+    if (tid >= total) return;
+    const int c = (int)(tid % Bp);
+    const int pt = (int)(tid / Bp);
+    if (c >= B) { f[tid] = R(0); return; }
+    const int l = pt / (n * n), m = (pt / n) % n, q = pt % n;
+    const int j1 = nodecell[l], j2 = nodecell[m], j3 = nodecell[q];
+    const double *u = U + 7 * ((long long)(c0 + c) * nv * nv * nv + (j1 * nv + j2) * nv + j3);
+    const double o1 = nodeoff[l], o2 = nodeoff[m], o3 = nodeoff[q];
+    const double a = o1 / dv, b = o2 / dv, e = o3 / dv;
+    const double val = u[0] + u[slot1] * o1 / dv + u[4] * o2 / dv + u[5] * o3 / dv + u[6] * (a * a + b * b + e * e);
+    f[tid] = (R)val;
+}
+
+// ---------------------------------------------------------------- DFT pass
+// out(pencil)[p][c] = sum_a M[p][a] in(pencil)[a][c] along axis ax of an
+// n x n x n x Bp array; M holds the per-axis DFT with the fft3D/FS phases and
+// scalings folded in.  Block (32 cells, n outputs), one pencil per block.
+// OUT 0: complex store.  OUT 1: FS stage epilogue on the real part.
+template <typename R, typename TIn, int OUT>
+__global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict__ out,
+                      const R *__restrict__ M, int n, int ax, int Bp, int stage, R dt, R nu,
+                      const R *__restrict__ f, R *__restrict__ qn, R *__restrict__ f1) {
+    using C = typename V2<R>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *Ms = reinterpret_cast<C *>(smem_raw);
+    C *pen = Ms + n * n;
+    const int cl = threadIdx.x, p = threadIdx.y;
+    const int pid = blockIdx.x, c = blockIdx.y * 32 + cl;
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < n * n; t += 32 * n) Ms[t] = mk2<R>(M[2 * t], M[2 * t + 1]);
+    long long base, stride;
+    if (ax == 2) { base = (long long)pid * n * Bp; stride = Bp; }
+    else if (ax == 1) { const int i0 = pid / n, i2 = pid % n; base = ((long long)i0 * n * n + i2) * Bp; stride = (long long)n * Bp; }
+    else { base = (long long)pid * Bp; stride = (long long)n * n * Bp; }
+    const long long o = base + p * stride + c;
+    if constexpr (std::is_same<TIn, double2>::value) pen[p * 32 + cl] = ld2c<R>(in + o);
+    else pen[p * 32 + cl] = ld2<R>(in + o);
+    __syncthreads();
+    R sr = R(0), si = R(0);
+#pragma unroll 4
+    for (int a = 0; a < n; ++a) {
+        const C m = Ms[p * n + a], x = pen[a * 32 + cl];
+        sr += m.x * x.x - m.y * x.y;
+        si += m.x * x.y + m.y * x.x;
+    }
+    if constexpr (OUT == 0) {
+        out[o] = mk2<R>(sr, si);
+    } else {
+        // RK4 node-value stages (C:831-862).
+        if (stage == 0) {
+            qn[o] = sr;
+            f1[o] = f[o] + dt * sr * nu;
+        } else {
+            f1[o] = f[o] + R(0.5) * dt * qn[o] * nu + R(0.5) * dt * sr * nu;
+        }
+    }
+}
+
+template <typename R, typename TIn, int OUT>
+cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
+                     double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st) {
+    using C = typename V2<R>::t;
+    const size_t smem = sizeof(C) * (size_t)(n * n + 32 * n);
+    dim3 grid(n * n, Bp / 32), block(32, n);
+    k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- ComputeQ
+// q(xi)[c] = sum over the pairs of xi of P * F(omega)[c] * F(u)[c]
+// (C:739-822 with the two terms of each symmetric pair folded).  One warp per
+// xi, lanes are cells; pair weights and packed indices are broadcast by
+// shuffle from a coalesced load of 32 pairs.  Products accumulate in R over
+// a chunk of 32 pairs, chunk sums in FP64.
+template <typename R>
+__global__ void __launch_bounds__(128) k_computeq(const typename V2<R>::t *__restrict__ F,
+                                                  const R *__restrict__ P, const unsigned *__restrict__ PI,
+                                                  const int *__restrict__ pair_off, int n3, int Bp,
+                                                  double2 *__restrict__ q) {
+    using C = typename V2<R>::t;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int xi = blockIdx.x * 4 + warp;
+    if (xi >= n3) return;
+    const int c = blockIdx.y * 32 + lane;
+    const int off = pair_off[xi], npair = pair_off[xi + 1] - off;
+    const C *Fc = F + c;
+    double ar = 0.0, ai = 0.0;
+    for (int base = 0; base < npair; base += 32) {
+        const int idx = base + lane;
+        R pw = R(0);
+        unsigned pk = 0u;
+        if (idx < npair) { pw = P[off + idx]; pk = PI[off + idx]; }
+        const int cnt = min(32, npair - base);
+        R cr = R(0), ci = R(0);
+#pragma unroll 4
+        for (int s = 0; s < cnt; ++s) {
+            const R ps = __shfl_sync(FULL, pw, s);
+            const unsigned pks = __shfl_sync(FULL, pk, s);
+            const C a = Fc[(long long)(pks & 0xffffu) * Bp];
+            const C b = Fc[(long long)(pks >> 16) * Bp];
+            const R pr = a.x * b.x - a.y * b.y;
+            const R pim = a.x * b.y + a.y * b.x;
+            cr = fma(ps, pr, cr);
+            ci = fma(ps, pim, ci);
+        }
+        ar += (double)cr;
+        ai += (double)ci;
+    }
+    q[(long long)xi * Bp + c] = make_double2(ar, ai);
+}
+
+// ---------------------------------------------------------------- conserve
+// conserveAllMoments (K:100-129): t = C q (5 dot products), lam = (CC^T)^-1 t,
+// q -= C^T lam.  Partial sums per chunk of points, then per cell.
+__global__ void k_cons_partial(const double2 *__restrict__ q, const double *__restrict__ c1,
+                               const double *__restrict__ c2, int n3, int Bp, int nchunk,
+                               double *__restrict__ part) {
+    __shared__ double red[8][5][32];
+    const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
+    const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
+    double t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+    for (int pt = p0 + y; pt < p1; pt += 8) {
+        const double2 v = q[(long long)pt * Bp + c];
+        t0 += v.x * c1[pt];
+        t1 += v.y * c2[n3 + pt];
+        t2 += v.y * c2[2 * n3 + pt];
+        t3 += v.y * c2[3 * n3 + pt];
+        t4 += v.x * c1[4 * n3 + pt];
+    }
+    red[y][0][cl] = t0; red[y][1][cl] = t1; red[y][2][cl] = t2; red[y][3][cl] = t3; red[y][4][cl] = t4;
+    __syncthreads();
+    if (y < 5) {
+        double s = 0;
+        for (int yy = 0; yy < 8; ++yy) s += red[yy][y][cl];
+        part[((long long)k * 5 + y) * Bp + c] = s;
+    }
+}
+
+__global__ void k_cons_lambda(const double *__restrict__ part, int nchunk, const double *__restrict__ cct,
+                              int Bp, double *__restrict__ lam) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= Bp) return;
+    double t[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k < nchunk; ++k)
+        for (int j = 0; j < 5; ++j) t[j] += part[((long long)k * 5 + j) * Bp + c];
+    for (int i = 0; i < 5; ++i) {  // solveWithCCt (K:49-55)
+        double s = 0.;
+        for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * t[j];
+        lam[(long long)i * Bp + c] = s;
+    }
+}
+
+__global__ void k_cons_apply(double2 *__restrict__ q, const double *__restrict__ c1,
+                             const double *__restrict__ c2, const double *__restrict__ lam, int n3, int Bp) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tid >= (long long)n3 * Bp) return;
+    const int c = (int)(tid % Bp), pt = (int)(tid / Bp);
+    const double l0 = lam[c], l1 = lam[Bp + c], l2 = lam[2 * Bp + c], l3 = lam[3 * Bp + c], l4 = lam[4 * Bp + c];
+    double2 v = q[tid];
+    v.x -= (c1[pt] * l0 + c1[4 * n3 + pt] * l4);
+    v.y -= (c2[n3 + pt] * l1 + c2[2 * n3 + pt] * l2 + c2[3 * n3 + pt] * l3);
+    q[tid] = v;
+}
+
+// ---------------------------------------------------------------- projection
+// Qc = nu (q0/2 + (q1 + q2 + q3)/6) (C:878-879), the non-classical RK4
+// combination of the reference (kept as specified).
+template <typename R>
+__global__ void k_qcomb(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
+                        const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
+                        long long total, typename V2<R>::t *__restrict__ Qc) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tid >= total) return;
+    const double2 a = q0[tid], b = q1[tid], d = q2[tid], e = q3[tid];
+    const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) / 6.);
+    const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) / 6.);
+    Qc[tid] = mk2<R>((R)re, (R)im);
+}
+
+// tp_l(j) = Re sum_k IntModes_l(k, j) Qc(k) (C:867-889) evaluated as three
+// per-axis contractions with the factors T0, T1, T2 of IntModes (C:364-505).
+template <typename R>
+__global__ void k_proj3(const typename V2<R>::t *__restrict__ Qc, const R *__restrict__ tf, int n, int nv,
+                        int Bp, typename V2<R>::t *__restrict__ Y) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)n * n * nv * Bp;
+    if (tid >= total) return;
+    const int c = (int)(tid % Bp);
+    long long r = tid / Bp;
+    const int j3 = (int)(r % nv); r /= nv;
+    const int k2 = (int)(r % n), k1 = (int)(r / n);
+    R s[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    const long long qb = ((long long)(k1 * n + k2) * n) * Bp + c;
+    for (int k3 = 0; k3 < n; ++k3) {
+        const typename V2<R>::t x = Qc[qb + (long long)k3 * Bp];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const R *t = tf + 2 * ((a * n + k3) * nv + j3);
+            s[a][0] += t[0] * x.x - t[1] * x.y;
+            s[a][1] += t[0] * x.y + t[1] * x.x;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        Y[((((long long)a * n + k1) * n + k2) * nv + j3) * Bp + c] = mk2<R>(s[a][0], s[a][1]);
+}
+
+template <typename R>
+__global__ void k_proj2(const typename V2<R>::t *__restrict__ Y, const R *__restrict__ tf, int n, int nv,
+                        int Bp, typename V2<R>::t *__restrict__ Z) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)n * nv * nv * Bp;
+    if (tid >= total) return;
+    const int c = (int)(tid % Bp);
+    long long r = tid / Bp;
+    const int j3 = (int)(r % nv); r /= nv;
+    const int j2 = (int)(r % nv), k1 = (int)(r / nv);
+    // Z[p] with (axis-3 factor, axis-2 factor) = (0,0) (0,1) (0,2) (1,0) (2,0)
+    R s[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    for (int k2 = 0; k2 < n; ++k2) {
+        typename V2<R>::t y[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) y[a] = Y[((((long long)a * n + k1) * n + k2) * nv + j3) * Bp + c];
+        const R *t0 = tf + 2 * ((0 * n + k2) * nv + j2);
+        const R *t1 = tf + 2 * ((1 * n + k2) * nv + j2);
+        const R *t2 = tf + 2 * ((2 * n + k2) * nv + j2);
+        s[0][0] += t0[0] * y[0].x - t0[1] * y[0].y; s[0][1] += t0[0] * y[0].y + t0[1] * y[0].x;
+        s[1][0] += t1[0] * y[0].x - t1[1] * y[0].y; s[1][1] += t1[0] * y[0].y + t1[1] * y[0].x;
+        s[2][0] += t2[0] * y[0].x - t2[1] * y[0].y; s[2][1] += t2[0] * y[0].y + t2[1] * y[0].x;
+        s[3][0] += t0[0] * y[1].x - t0[1] * y[1].y; s[3][1] += t0[0] * y[1].y + t0[1] * y[1].x;
+        s[4][0] += t0[0] * y[2].x - t0[1] * y[2].y; s[4][1] += t0[0] * y[2].y + t0[1] * y[2].x;
+    }
+#pragma unroll
+    for (int p = 0; p < 5; ++p)
+        Z[((((long long)p * n + k1) * nv + j2) * nv + j3) * Bp + c] = mk2<R>(s[p][0], s[p][1]);
+}
+
+// Last contraction, the mass-matrix inverse on {phi0, phi6} and the RK4
+// update of the 5 collided coefficients (C:890-905).
+template <typename R>
+__global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__restrict__ tf, int n, int nv,
+                        int Bp, int B, int c0, const double *__restrict__ U, int ustride, int4 us, int us4,
+                        double dt, double kfac, double *__restrict__ dU) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nv3 = (long long)nv * nv * nv;
+    if (tid >= nv3 * Bp) return;
+    const int c = (int)(tid % Bp);
+    if (c >= B) return;
+    const long long kt = tid / Bp;
+    const int j3 = (int)(kt % nv), j2 = (int)((kt / nv) % nv), j1 = (int)(kt / ((long long)nv * nv));
+    // l=0: T0 on Z0; l=1: T1 on Z0; l=2: T0 on Z1; l=3: T0 on Z3; l=4: T2 on Z0 + T0 on Z2 + T0 on Z4
+    R a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0;
+    for (int k1 = 0; k1 < n; ++k1) {
+        const R *t0 = tf + 2 * ((0 * n + k1) * nv + j1);
+        const R *t1 = tf + 2 * ((1 * n + k1) * nv + j1);
+        const R *t2 = tf + 2 * ((2 * n + k1) * nv + j1);
+        const long long zb = (((long long)k1 * nv + j2) * nv + j3) * Bp + c;
+        const long long zs = (long long)n * nv * nv * Bp;
+        const typename V2<R>::t z0 = Z[zb], z1 = Z[zb + zs], z2 = Z[zb + 2 * zs], z3 = Z[zb + 3 * zs], z4 = Z[zb + 4 * zs];
+        a0 += t0[0] * z0.x - t0[1] * z0.y;
+        a1 += t1[0] * z0.x - t1[1] * z0.y;
+        a2 += t0[0] * z1.x - t0[1] * z1.y;
+        a3 += t0[0] * z3.x - t0[1] * z3.y;
+        a4 += t2[0] * z0.x - t2[1] * z0.y;
+        a5 += t0[0] * z2.x - t0[1] * z2.y;
+        a6 += t0[0] * z4.x - t0[1] * z4.y;
+    }
+    const double tp0 = (double)a0, tp2 = (double)a1, tp3 = (double)a2, tp4 = (double)a3;
+    const double tp5 = (double)a4 + (double)a5 + (double)a6;
+    const double *u = U + (long long)ustride * ((long long)(c0 + c) * nv3 + kt);
+    const double p0 = u[us.x] + u[us4] / 4. + dt * tp0 * kfac;
+    const double p2 = u[us.y] + dt * tp2 * 12. * kfac;
+    const double p3 = u[us.z] + dt * tp3 * 12. * kfac;
+    const double p4 = u[us.w] + dt * tp4 * 12. * kfac;
+    const double p5 = u[us.x] / 4. + u[us4] * 19. / 240. + dt * tp5 * kfac;
+    double *d = dU + 5 * ((long long)c * nv3 + kt);
+    d[0] = 19 * p0 / 4. - 15 * p5;
+    d[4] = 60 * p5 - 15 * p0;
+    d[1] = p2; d[2] = p3; d[3] = p4;
+}
+
+// ---------------------------------------------------------------- moments of the increment
+// Mixed path: the 5 DG moments of each cell's collision increment are
+// evaluated in FP64 directly from the FP64 mode array (target) and from the
+// projected coefficients (actual); the minimal-norm correction
+// delta_j = Phi_j^T lambda, lambda = Gm^-1 (target - actual), then makes the
+// coefficients carry exactly the FP64 moments.
+__global__ void k_mom_target(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
+                             const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
+                             const double *__restrict__ gmom, int n3, int Bp, int nchunk,
+                             double *__restrict__ part) {
+    __shared__ double red[8][5][32];
+    const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
+    const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
+    double t[5] = {0, 0, 0, 0, 0};
+    for (int pt = p0 + y; pt < p1; pt += 8) {
+        const long long o = (long long)pt * Bp + c;
+        const double2 a = q0[o], b = q1[o], d = q2[o], e = q3[o];
+        const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) / 6.);
+        const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) / 6.);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            const double *g = gmom + 2 * ((long long)m * n3 + pt);
+            t[m] += g[0] * re - g[1] * im;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) red[y][m][cl] = t[m];
+    __syncthreads();
+    if (y < 5) {
+        double s = 0;
+        for (int yy = 0; yy < 8; ++yy) s += red[yy][y][cl];
+        part[((long long)k * 5 + y) * Bp + c] = s;
+    }
+}
+
+__device__ __forceinline__ void phi_row(double dv, double lv, int nv, long long kt, double G[3], double &g2) {
+    const int j3 = (int)(kt % nv), j2 = (int)((kt / nv) % nv), j1 = (int)(kt / ((long long)nv * nv));
+    G[0] = -lv + (j1 + 0.5) * dv;
+    G[1] = -lv + (j2 + 0.5) * dv;
+    G[2] = -lv + (j3 + 0.5) * dv;
+    g2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+}
+
+__global__ void k_mom_actual(const double *__restrict__ dU, const double *__restrict__ U, int nv, double dv,
+                             double lv, int c0, int nrc, double *__restrict__ part) {
+    __shared__ double red[5][256];
+    const int cc = blockIdx.y, t = threadIdx.x;
+    const long long nv3 = (long long)nv * nv * nv;
+    const long long cs = (nv3 + nrc - 1) / nrc, r0 = blockIdx.x * cs, r1 = min(nv3, r0 + cs);
+    double m[5] = {0, 0, 0, 0, 0};
+    for (long long kt = r0 + t; kt < r1; kt += 256) {
+        const double *a = dU + 5 * ((long long)cc * nv3 + kt);
+        const double *u = U + 7 * ((long long)(c0 + cc) * nv3 + kt);
+        const double d0 = a[0] - u[0], d1 = a[1] - u[3], d2 = a[2] - u[4], d3 = a[3] - u[5], d4 = a[4] - u[6];
+        double G[3], g2;
+        phi_row(dv, lv, nv, kt, G, g2);
+        m[0] += d0 + 0.25 * d4;
+        m[1] += G[0] * d0 + dv / 12. * d1 + 0.25 * G[0] * d4;
+        m[2] += G[1] * d0 + dv / 12. * d2 + 0.25 * G[1] * d4;
+        m[3] += G[2] * d0 + dv / 12. * d3 + 0.25 * G[2] * d4;
+        m[4] += (g2 + dv * dv / 4.) * d0 + dv / 6. * (G[0] * d1 + G[1] * d2 + G[2] * d3) +
+                (19. * dv * dv / 240. + g2 / 4.) * d4;
+    }
+    for (int q = 0; q < 5; ++q) red[q][t] = m[q];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int q = 0; q < 5; ++q) red[q][t] += red[q][t + w];
+        __syncthreads();
+    }
+    if (t < 5) part[((long long)cc * nrc + blockIdx.x) * 5 + t] = red[t][0];
+}
+
+__global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const double *__restrict__ apart,
+                             int nrc, const double *__restrict__ gm_inv, double scale, int B, int Bp,
+                             double *__restrict__ lam) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= B) return;
+    double r[5];
+    for (int m = 0; m < 5; ++m) {
+        double tg = 0, ac = 0;
+        for (int k = 0; k < nchunk; ++k) tg += tpart[((long long)k * 5 + m) * Bp + c];
+        for (int k = 0; k < nrc; ++k) ac += apart[((long long)c * nrc + k) * 5 + m];
+        r[m] = scale * tg - ac;
+    }
+    for (int i = 0; i < 5; ++i) {
+        double s = 0;
+        for (int j = 0; j < 5; ++j) s += gm_inv[i * 5 + j] * r[j];
+        lam[5 * c + i] = s;
+    }
+}
+
+__global__ void k_mom_apply(double *__restrict__ dU, const double *__restrict__ lam, int nv, double dv, double lv,
+                            long long nrec) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const long long nv3 = (long long)nv * nv * nv;
+    const long long cc = r / nv3, kt = r % nv3;
+    const double *l = lam + 5 * cc;
+    double G[3], g2;
+    phi_row(dv, lv, nv, kt, G, g2);
+    double *a = dU + 5 * r;
+    // delta = Phi^T lambda (columns of Phi: a0, a1, a2, a3, a4)
+    a[0] += l[0] + G[0] * l[1] + G[1] * l[2] + G[2] * l[3] + (g2 + dv * dv / 4.) * l[4];
+    a[1] += dv / 12. * l[1] + dv / 6. * G[0] * l[4];
+    a[2] += dv / 12. * l[2] + dv / 6. * G[1] * l[4];
+    a[3] += dv / 12. * l[3] + dv / 6. * G[2] * l[4];
+    a[4] += 0.25 * l[0] + 0.25 * (G[0] * l[1] + G[1] * l[2] + G[2] * l[3]) + (19. * dv * dv / 240. + g2 / 4.) * l[4];
+}
+
+// dU into slots {0,3,4,5,6} (LP_ompi_1.cpp:522-532).
+__global__ void k_scatter(const double *__restrict__ dU, long long nrec, long long r0, double *__restrict__ U) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const double *d = dU + 5 * r;
+    double *u = U + 7 * (r0 + r);
+    u[0] = d[0]; u[6] = d[4]; u[3] = d[1]; u[4] = d[2]; u[5] = d[3];
+}
+
+// ---------------------------------------------------------------- Poisson
+// Charge moments per spatial cell: scalev sum (U0 + U6/4), U1, U2.
+__global__ void k_charge(const double *__restrict__ U, int nv3, double scalev, double *__restrict__ rt) {
+    __shared__ double red[3][256];
+    const int s = blockIdx.x, t = threadIdx.x;
+    double r0 = 0, r1 = 0, r2 = 0;
+    const double *base = U + 7 * (long long)s * nv3;
+    for (int j = t; j < nv3; j += 256) {
+        const double *u = base + 7 * (long long)j;
+        r0 += scalev * (u[0] + 0.25 * u[6]);
+        r1 += scalev * u[1];
+        r2 += scalev * u[2];
+    }
+    red[0][t] = r0; red[1][t] = r1; red[2][t] = r2;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) { red[0][t] += red[0][t + w]; red[1][t] += red[1][t + w]; red[2][t] += red[2][t + w]; }
+        __syncthreads();
+    }
+    if (t == 0) { rt[3 * s] = red[0][0]; rt[3 * s + 1] = red[1][0]; rt[3 * s + 2] = red[2][0]; }
+}
+
+// pois2d in one block: right-hand side, the band solve of DGBTRS
+// replayed on one warp in the host factorisation's operation order (no FMA),
+// field reconstruction and the cell integrals used by the advection.
+__global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *__restrict__ bg,
+                          double *__restrict__ potc, double *__restrict__ phix, double *__restrict__ phiy,
+                          double *__restrict__ fields) {
+    extern __shared__ double b[];
+    const int t = threadIdx.x, nc = pd.nx * pd.ny, nd = pd.ndim;
+    for (int ii = t; ii < nc; ii += blockDim.x) {
+        const double DXv = pd.dxp, DYv = pd.dyp;
+        b[3 * ii] = __dmul_rn(__dmul_rn(__dsub_rn(rt[3 * ii], 1.0), DXv), DYv);
+        b[3 * ii + 1] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 1], DXv), DYv), 12.);
+        b[3 * ii + 2] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 2], DXv), DYv), 12.);
+    }
+    __syncthreads();
+    const int ldab = pd.ldab;
+#define ABD(i, j) pd.ab[((i) - 1) + (long long)((j) - 1) * ldab]
+    if (t < 32) {
+        const int kd = pd.ku + pd.kl + 1;
+        for (int j = 1; j <= nd - 1; ++j) {
+            const int lm = min(pd.kl, nd - j);
+            const int l = pd.ipiv[j - 1];
+            if (t == 0 && l != j) { const double tmp = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = tmp; }
+            __syncwarp();
+            const double bj = b[j - 1];
+            if (bj != 0.0) {
+                const double tt = -bj;
+                for (int i = 1 + t; i <= lm; i += 32) b[j + i - 1] = __dadd_rn(b[j + i - 1], __dmul_rn(ABD(kd + i, j), tt));
+            }
+            __syncwarp();
+        }
+        const int k = pd.kl + pd.ku, kplus1 = k + 1;
+        for (int j = nd; j >= 1; --j) {
+            const double bj = b[j - 1];
+            __syncwarp();
+            if (bj != 0.0) {
+                const int l = kplus1 - j;
+                const double xj = __ddiv_rn(bj, ABD(kplus1, j));
+                const int ilo = max(1, j - k);
+                for (int i = j - 1 - t; i >= ilo; i -= 32) b[i - 1] = __dsub_rn(b[i - 1], __dmul_rn(xj, ABD(l + i, j)));
+                if (t == 0) b[j - 1] = xj;
+            }
+            __syncwarp();
+        }
+    }
+#undef ABD
+    __syncthreads();
+    for (int i = t; i < nd; i += blockDim.x) { potc[i] = b[i]; bg[i] = b[i]; }
+    __syncthreads();
+    const double *acvx = pd.blk[0], *acyrr = pd.blk[1], *acyrl = pd.blk[2];
+    const double *acvy = pd.blk[3], *acxrr = pd.blk[4], *acxrl = pd.blk[5];
+    for (int ii = t; ii < nc; ii += blockDim.x) {
+        const int ix = ii / pd.ny + 1, jy = ii % pd.ny + 1;
+        const int il = ii - pd.ny, ib = ii - 1;
+        for (int k = 0; k < 3; ++k) {  // E_x
+            double s = 0.;
+            if (ix == 1) {
+                for (int kk = 0; kk < 3; ++kk) s = __dadd_rn(s, __dmul_rn(__dadd_rn(acvx[3 * k + kk], acyrr[3 * k + kk]), b[3 * ii + kk]));
+                s = __dsub_rn(s, __dmul_rn(acyrl[3 * k], 0.));
+            } else if (ix == pd.nx) {
+                for (int kk = 0; kk < 3; ++kk)
+                    s = __dsub_rn(__dadd_rn(s, __dmul_rn(acvx[3 * k + kk], b[3 * ii + kk])), __dmul_rn(acyrl[3 * k + kk], b[3 * il + kk]));
+                s = __dadd_rn(s, __dmul_rn(acyrr[3 * k], 0.));
+            } else {
+                for (int kk = 0; kk < 3; ++kk)
+                    s = __dsub_rn(__dadd_rn(s, __dmul_rn(__dadd_rn(acvx[3 * k + kk], acyrr[3 * k + kk]), b[3 * ii + kk])),
+                                  __dmul_rn(acyrl[3 * k + kk], b[3 * il + kk]));
+            }
+            phix[3 * ii + k] = __ddiv_rn(-s, pd.dxp);
+        }
+        for (int k = 0; k < 3; ++k) {  // E_y
+            double s = 0.;
+            if (jy == 1) {
+                phiy[3 * ii + k] = (k == 0) ? __ddiv_rn(-b[3 * ii + 2], pd.dyp) : 0.;
+                continue;
+            }
+            if (jy == pd.ny && pd.gate[ix]) {
+                for (int kk = 0; kk < 3; ++kk)
+                    s = __dsub_rn(__dadd_rn(s, __dmul_rn(acvy[3 * k + kk], b[3 * ii + kk])), __dmul_rn(acxrl[3 * k + kk], b[3 * ib + kk]));
+                s = __dadd_rn(s, __dmul_rn(acxrr[3 * k], 0.));
+            } else {
+                for (int kk = 0; kk < 3; ++kk)
+                    s = __dsub_rn(__dadd_rn(s, __dmul_rn(__dadd_rn(acvy[3 * k + kk], acxrr[3 * k + kk]), b[3 * ii + kk])),
+                                  __dmul_rn(acxrl[3 * k + kk], b[3 * ib + kk]));
+            }
+            phiy[3 * ii + k] = __ddiv_rn(-s, pd.dyp);
+        }
+        // cell integrals of the field
+        const double ex0 = phix[3 * ii], ex1 = phix[3 * ii + 1], ex2 = phix[3 * ii + 2];
+        const double ey0 = phiy[3 * ii], ey1 = phiy[3 * ii + 1], ey2 = phiy[3 * ii + 2];
+        fields[0 * nc + ii] = ex0;
+        fields[1 * nc + ii] = __ddiv_rn(ex1, 12.);
+        fields[2 * nc + ii] = __ddiv_rn(ex2, 12.);
+        fields[3 * nc + ii] = __ddiv_rn(ex0, 12.);
+        fields[4 * nc + ii] = 0.;
+        fields[5 * nc + ii] = __ddiv_rn(ex0, 12.);
+        fields[6 * nc + ii] = ey0;
+        fields[7 * nc + ii] = __ddiv_rn(ey1, 12.);
+        fields[8 * nc + ii] = __ddiv_rn(ey2, 12.);
+        fields[9 * nc + ii] = __ddiv_rn(ey0, 12.);
+        fields[10 * nc + ii] = 0.;
+        fields[11 * nc + ii] = __ddiv_rn(ey0, 12.);
+        fields[12 * nc + ii] = ex0 > 0. ? 1. : -1.;
+        fields[13 * nc + ii] = ey0 > 0. ? 1. : -1.;
+    }
+}
+
+// ---------------------------------------------------------------- advection
+// Right-hand side H of one record (I1, I2, I3, I5 at A:213-405 combined as at
+// A:455-467; H[2] = 0) and the SSP-RK3 stage (A:469, A:527, A:581).
+__global__ void k_flux(AdvectDev ad, const double *__restrict__ U0, const double *__restrict__ Us,
+                       const double *__restrict__ fields, int stage, double *__restrict__ Uout) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= ad.size) return;
+    const int nv = ad.nv;
+    const long long sv = (long long)nv * nv * nv;
+    const long long jm = k % sv, s = k / sv;
+    const int j3 = (int)(jm % nv), j2 = (int)((jm / nv) % nv), j1 = (int)(jm / ((long long)nv * nv));
+    const int i2 = (int)(s % ad.nx2), i1 = (int)(s / ad.nx2);
+    const double dv = ad.dv;
+    const double G = -ad.lv + (j1 + 0.5) * dv;
+    const double *u = Us + 7 * k;
+    constexpr double i12 = 1. / 12., i720_19 = 19. / 720., i240_19 = 19. / 240., i5_12 = 5. / 12.,
+                     i720_133 = 133. / 720., i6 = 1. / 6.;
+    // x1 upwind neighbours by the sign of v1, periodic (I3).
+    long long kr3, kl3;
+    double ur3, ul3;
+    if (j1 < nv / 2) {
+        int iir = i1 + 1;
+        if (iir == ad.nx1) iir = 0;
+        kr3 = (long long)iir * ad.nx2 * sv + (long long)i2 * sv + jm;
+        kl3 = k;
+        ur3 = -Us[kr3 * 7 + 1];
+        ul3 = -Us[kl3 * 7 + 1];
+    } else {
+        int iil = i1 - 1;
+        if (iil == -1) iil = ad.nx1 - 1;
+        kr3 = k;
+        kl3 = (long long)iil * ad.nx2 * sv + (long long)i2 * sv + jm;
+        ur3 = Us[kr3 * 7 + 1];
+        ul3 = Us[kl3 * 7 + 1];
+    }
+    const double *R3 = Us + 7 * kr3, *L3 = Us + 7 * kl3;
+    // v1 upwind neighbours by the sign of the cell-average E_x, no inflow (I5).
+    const long long nc = (long long)ad.nx1 * ad.nx2;
+    const double ie = fields[s], ixe = fields[nc + s], ixxe = fields[3 * nc + s];
+    int j1r, j1l;
+    long long kr5, kl5;
+    double ur5 = 0., ul5 = 0.;
+    if (ie > 0) {
+        j1r = j1 + 1; j1l = j1;
+        kr5 = s * sv + ((long long)j1r * nv * nv + j2 * nv + j3);
+        kl5 = k;
+        if (j1r < nv) ur5 = -Us[kr5 * 7 + 3];
+        ul5 = -Us[kl5 * 7 + 3];
+    } else {
+        j1r = j1; j1l = j1 - 1;
+        kr5 = k;
+        kl5 = s * sv + ((long long)j1l * nv * nv + j2 * nv + j3);
+        ur5 = Us[kr5 * 7 + 3];
+        if (j1l > -1) ul5 = Us[kl5 * 7 + 3];
+    }
+    const bool hasr = j1r < nv, hasl = j1l > -1;
+    double R5[7] = {0, 0, 0, 0, 0, 0, 0}, L5[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (hasr) for (int q = 0; q < 7; ++q) R5[q] = Us[kr5 * 7 + q];
+    if (hasl) for (int q = 0; q < 7; ++q) L5[q] = Us[kl5 * 7 + q];
+    const double dv2 = dv * dv, dv3 = dv * dv * dv;
+    double tp[6];
+    // l = 0
+    {
+        double i3 = dv3 * ((R3[0] + 0.5 * ur3 - L3[0] - 0.5 * ul3) * G + (R3[3] - L3[3]) * dv * i12 + (R3[6] - L3[6]) * G * 0.25);
+        double i5 = 0.;
+        if (hasr && hasl) i5 = dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12 - L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ie + dv2 * (R5[1] - L5[1]) * ixe;
+        else if (hasr) i5 = dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe;
+        else if (hasl) i5 = dv2 * (-L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ie - dv2 * L5[1] * ixe;
+        tp[0] = -i3 + i5;
+    }
+    // l = 1
+    {
+        double i1v = dv3 * (G * u[0] + dv * u[3] * i12 + u[6] * G * 0.25);
+        double i3 = 0.5 * dv3 * ((R3[0] + 0.5 * ur3 + L3[0] + 0.5 * ul3) * G + (R3[3] + L3[3]) * dv * i12 + (R3[6] + L3[6]) * G * 0.25);
+        double i5 = 0.;
+        if (hasr && hasl) i5 = dv2 * ((R5[0] + 0.5 * ur5 + R5[6] * i5_12 - L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ixe + (R5[1] - L5[1]) * ixxe);
+        else if (hasr) i5 = dv2 * ((R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ixe + R5[1] * ixxe);
+        else if (hasl) i5 = dv2 * ((-L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ixe - L5[1] * ixxe);
+        tp[1] = i1v - i3 + i5;
+    }
+    // l = 3 (v1 slope)
+    {
+        double i2 = (((u[0] + u[6] * 0.25) * ie + u[1] * ixe) * ad.scalev) / dv;
+        double i3 = dv2 * (((R3[0] - L3[0]) * dv2 + (ur3 - ul3) * 0.5 * dv2 + (R3[3] - L3[3]) * dv * G) * i12 + (R3[6] - L3[6]) * dv2 * i720_19);
+        double i5 = 0.;
+        if (hasr && hasl) i5 = 0.5 * (dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12 + L5[0] + 0.5 * ul5 + L5[6] * i5_12) * ie + dv2 * (R5[1] + L5[1]) * ixe);
+        else if (hasr) i5 = 0.5 * (dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe);
+        else if (hasl) i5 = 0.5 * (dv2 * (L5[0] + 0.5 * ul5 + L5[6] * i5_12) * ie + dv2 * L5[1] * ixe);
+        tp[2] = -i2 - i3 + i5;
+    }
+    // l = 4, 5 (v2, v3 slopes)
+    for (int q = 4; q <= 5; ++q) {
+        double i3 = (R3[q] - L3[q]) * G * dv3 * i12;
+        double i5 = 0.;
+        if (hasr && hasl) i5 = (R5[q] - L5[q]) * ie * dv2 * i12;
+        else if (hasr) i5 = R5[q] * ie * dv2 * i12;
+        else if (hasl) i5 = -L5[q] * ie * dv2 * i12;
+        tp[q - 1] = -i3 + i5;
+    }
+    // l = 6 (|v|^2 mode)
+    {
+        double i2 = u[3] * dv2 * ie * i6;
+        double i3 = dv3 * ((R3[0] + 0.5 * ur3 - L3[0] - 0.5 * ul3) * G * 0.25 + (R3[3] - L3[3]) * dv * i720_19 + (R3[6] - L3[6]) * G * i240_19);
+        double i5 = 0.;
+        if (hasr && hasl) i5 = dv2 * (((R5[0] + 0.5 * ur5 - L5[0] - 0.5 * ul5) * i5_12 + (R5[6] - L5[6]) * i720_133) * ie + (R5[1] - L5[1]) * ixe * i5_12);
+        else if (hasr) i5 = dv2 * (((R5[0] + 0.5 * ur5) * i5_12 + R5[6] * i720_133) * ie + R5[1] * ixe * i5_12);
+        else if (hasl) i5 = -dv2 * (((L5[0] + 0.5 * ul5) * i5_12 + L5[6] * i720_133) * ie + L5[1] * ixe * i5_12);
+        tp[5] = -i2 - i3 + i5;
+    }
+    const double inv = 1.0 / ad.dx / ad.scalev;
+    double H[7];
+    H[0] = (19 * tp[0] * 0.25 - 15 * tp[5]) * inv;
+    H[6] = (60 * tp[5] - 15 * tp[0]) * inv;
+    H[1] = tp[1] * 12. * inv;
+    H[2] = 0.;
+    H[3] = tp[2] * 12. * inv;
+    H[4] = tp[3] * 12. * inv;
+    H[5] = tp[4] * 12. * inv;
+    const double dt = ad.dt;
+    const double *u0 = U0 + 7 * k;
+    double *o = Uout + 7 * k;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) {
+        double r;
+        if (stage == 0) r = u0[l] + dt * H[l];
+        else if (stage == 1) r = 0.75 * u0[l] + 0.25 * u[l] + 0.25 * dt * H[l];
+        else r = u0[l] / 3. + u[l] * 2. / 3. + dt * H[l] * 2. / 3.;
+        o[l] = r;
+    }
+}
+
+// ---------------------------------------------------------------- moments
+__global__ void k_moments(const double *__restrict__ U, long long size, long long kend, int nv, double lv,
+                          double dv, double *__restrict__ part) {
+    __shared__ double red[5][256];
+    const int t = threadIdx.x;
+    double m = 0, a1 = 0, a2 = 0, a3 = 0, ke = 0;
+    const long long sv = (long long)nv * nv * nv;
+    for (long long k = blockIdx.x * 256LL + t; k < size; k += (long long)gridDim.x * 256) {
+        const double *u = U + 7 * k;
+        const long long j = k % sv;
+        const int j3 = (int)(j % nv), j2 = (int)((j / nv) % nv), j1 = (int)(j / ((long long)nv * nv));
+        const double g1 = -lv + (j1 + 0.5) * dv, g2 = -lv + (j2 + 0.5) * dv, g3 = -lv + (j3 + 0.5) * dv;
+        m += u[0] + u[6] / 4.;
+        a1 += g1 * dv * u[0] + u[3] * dv * dv / 12. + u[6] * g1 * dv / 4.;
+        a2 += g2 * dv * u[0] + u[4] * dv * dv / 12. + u[6] * g2 * dv / 4.;
+        a3 += g3 * dv * u[0] + u[5] * dv * dv / 12. + u[6] * g3 * dv / 4.;
+        if (k < kend) {
+            const double tp1 = g1 * g1 + g2 * g2 + g3 * g3;
+            ke += u[0] * (tp1 + dv * dv / 4.) * dv + (g1 * u[3] + g2 * u[4] + g3 * u[5]) * dv * dv / 6. +
+                  u[6] * (dv * dv * dv * 19. / 240. + tp1 * dv / 4.);
+        }
+    }
+    red[0][t] = m; red[1][t] = a1; red[2][t] = a2; red[3][t] = a3; red[4][t] = ke;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int q = 0; q < 5; ++q) red[q][t] += red[q][t + w];
+        __syncthreads();
+    }
+    if (t < 5) part[blockIdx.x * 5 + t] = red[t][0];
+}
+
+}  // namespace
+
+// =============================================================== launchers
+cudaError_t launch_pairs(const double *eta, const double *shat, const double *ahat, const unsigned char *rzero,
+                         const double *cw, const int *pair_off, int n, double *P64, float *P32, unsigned *PI,
+                         cudaStream_t st) {
+    k_pairs<<<n * n * n, 256, 0, st>>>(eta, shat, ahat, rzero, cw, pair_off, n, P64, P32, PI);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_nodes(const double *U, int nv, int n, int c0, int B, int Bp, int slot1, const int *nodecell,
+                         const double *nodeoff, double dv, R *f, cudaStream_t st) {
+    const long long total = (long long)n * n * n * Bp;
+    k_nodes<R><<<grid1(total, 256), 256, 0, st>>>(U, nv, n, c0, B, Bp, slot1, nodecell, nodeoff, dv, f);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, const R *M, int n, int Bp,
+                       cudaStream_t st) {
+    using C = typename V2<R>::t;
+    cudaError_t e;
+    if ((e = dft_pass<R, R, 0>(f, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    if ((e = dft_pass<R, C, 0>(F, t1, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    return dft_pass<R, C, 0>(t1, F, M, n, 0, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st);
+}
+
+template <typename R>
+cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t1, typename V2<R>::t *F,
+                               const R *M, int n, int Bp, cudaStream_t st) {
+    using C = typename V2<R>::t;
+    cudaError_t e;
+    if ((e = dft_pass<R, C, 0>(in, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    if ((e = dft_pass<R, C, 0>(F, t1, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    return dft_pass<R, C, 0>(t1, F, M, n, 0, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st);
+}
+
+template <typename R>
+cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2, const R *M, int n,
+                            int Bp, int stage, double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st) {
+    using C = typename V2<R>::t;
+    cudaError_t e;
+    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st);
+}
+
+template <typename R>
+cudaError_t launch_fs_full(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
+                           typename V2<R>::t *out, const R *M, int n, int Bp, cudaStream_t st) {
+    using C = typename V2<R>::t;
+    cudaError_t e;
+    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    return dft_pass<R, C, 0>(t2, out, M, n, 0, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st);
+}
+
+template <typename R>
+cudaError_t launch_computeq(const typename V2<R>::t *F, const R *P, const unsigned *PI, const int *pair_off,
+                            int n3, int Bp, double2 *q, cudaStream_t st) {
+    dim3 grid((n3 + 3) / 4, Bp / 32);
+    k_computeq<R><<<grid, 128, 0, st>>>(F, P, PI, pair_off, n3, Bp, q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
+                            double *part, int nchunk, double *lam, cudaStream_t st) {
+    k_cons_partial<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
+    k_cons_lambda<<<(Bp + 127) / 128, 128, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
+                           const R *tfac, int n, int nv, int Bp, int B, int c0, const double *U, int ustride,
+                           const int *uslot, double dt, double scalev, double scaleL, double scale3,
+                           typename V2<R>::t *Qc, typename V2<R>::t *Y, typename V2<R>::t *Z, double *dU,
+                           cudaStream_t st) {
+    const long long n3 = (long long)n * n * n, nv3 = (long long)nv * nv * nv;
+    k_qcomb<R><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Qc);
+    k_proj3<R><<<grid1((long long)n * n * nv * Bp, 256), 256, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
+    k_proj2<R><<<grid1((long long)n * nv * nv * Bp, 256), 256, 0, st>>>(Y, tfac, n, nv, Bp, Z);
+    const double kfac = 1. / scalev / scaleL / scale3;
+    int4 us = make_int4(uslot[0], uslot[1], uslot[2], uslot[3]);
+    k_proj1<R><<<grid1(nv3 * Bp, 256), 256, 0, st>>>(Z, tfac, n, nv, Bp, B, c0, U, ustride, us, uslot[4], dt, kfac, dU);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
+                              double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
+                              const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
+                              double *apart, const double *gm_inv, double scale, double *lam, double *dU,
+                              cudaStream_t st) {
+    k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, gmom, n3, Bp, nchunk, tpart);
+    k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, c0, nrc, apart);
+    k_mom_lambda<<<(B + 127) / 128, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, B, Bp, lam);
+    const long long nrec = (long long)B * nv * nv * nv;
+    k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, nrec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st) {
+    const long long nrec = (long long)B * nv3;
+    k_scatter<<<grid1(nrec, 256), 256, 0, st>>>(dU, nrec, (long long)c0 * nv3, U);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_charge(const double *U, int ncell, int nv3, double scalev, double *rt, cudaStream_t st) {
+    k_charge<<<ncell, 256, 0, st>>>(U, nv3, scalev, rt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, double *b, double *potc, double *phix,
+                           double *phiy, double *fields, cudaStream_t st) {
+    const size_t smem = sizeof(double) * (size_t)pd.ndim;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_poisson<<<1, 256, smem, st>>>(pd, rt, b, potc, phix, phiy, fields);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const double *fields,
+                              int stage, double *Uout, cudaStream_t st) {
+    k_flux<<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, fields, stage, Uout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_moments(const double *U, long long size, long long kend, int nv, double lv, double dv,
+                           double *part, int nblk, cudaStream_t st) {
+    k_moments<<<nblk, 256, 0, st>>>(U, size, kend, nv, lv, dv, part);
+    return cudaGetLastError();
+}
+
+// explicit instantiations
+#define LP_INST(R)                                                                                              \
+    template cudaError_t launch_nodes<R>(const double *, int, int, int, int, int, int, const int *,             \
+                                         const double *, double, R *, cudaStream_t);                            \
+    template cudaError_t launch_fwd<R>(const R *, V2<R>::t *, V2<R>::t *, const R *, int, int, cudaStream_t);   \
+    template cudaError_t launch_fwd_complex<R>(const V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, int,   \
+                                               cudaStream_t);                                                   \
+    template cudaError_t launch_fs_stage<R>(const double2 *, V2<R>::t *, V2<R>::t *, const R *, int, int, int,  \
+                                            double, double, const R *, R *, R *, cudaStream_t);                 \
+    template cudaError_t launch_fs_full<R>(const double2 *, V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, \
+                                           int, cudaStream_t);                                                  \
+    template cudaError_t launch_computeq<R>(const V2<R>::t *, const R *, const unsigned *, const int *, int,    \
+                                            int, double2 *, cudaStream_t);                                      \
+    template cudaError_t launch_project<R>(const double2 *, const double2 *, const double2 *, const double2 *,  \
+                                           double, const R *, int, int, int, int, int, const double *, int,     \
+                                           const int *, double, double, double, double, V2<R>::t *,             \
+                                           V2<R>::t *, V2<R>::t *, double *, cudaStream_t);
+LP_INST(double)
+LP_INST(float)
+#undef LP_INST
+
+}  // namespace lp

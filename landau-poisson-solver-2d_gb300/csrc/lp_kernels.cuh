@@ -1,0 +1,113 @@
+// Kernel launchers of the GB300 Landau-Poisson hot path (sm_103a).
+//
+// Spectral arrays are "cell-minor": element (point, cell) of an n^3 x Bp
+// array sits at point*Bp + cell, Bp a multiple of 32, so the 32 lanes of a
+// warp are 32 spatial cells and every load is coalesced.  The state U keeps
+// the reference's AoS layout of 7 doubles per record.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace lp {
+
+template <typename R> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+// Pair table of the windowed weight contraction: for each xi, ceil(cnt/2)
+// pairs (omega, u = xi + n/2 - omega) with the combined weight
+// cw(omega) W(xi,omega) + cw(u) W(xi,u) (one term on the diagonal).
+cudaError_t launch_pairs(const double *eta, const double *shat, const double *ahat,
+                         const unsigned char *rzero, const double *cw, const int *pair_off, int n,
+                         double *P64, float *P32, unsigned *PI, cudaStream_t st);
+
+// Node values of cells [c0, c0+B) of U, written to f[n^3][Bp] (R precision).
+template <typename R>
+cudaError_t launch_nodes(const double *U, int nv, int n, int c0, int B, int Bp, int slot1,
+                         const int *nodecell, const double *nodeoff, double dv, R *f,
+                         cudaStream_t st);
+
+// Forward transform (fft3D with the phases folded into per-axis matrices):
+// real f[n^3][Bp] -> complex F.  t1 is scratch of the same size as F.
+template <typename R>
+cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, const R *M, int n,
+                       int Bp, cudaStream_t st);
+
+// Inverse transform FS of q (FP64 complex), real part only, fused with the
+// RK4 stage update of the node values: stage 0 stores Q = Re FS(q) in qn and
+// writes f1 = f + dt Q nu; stages 1, 2 write f1 = f + dt/2 Q nu + dt/2 Re FS(q) nu.
+template <typename R>
+cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
+                            const R *M, int n, int Bp, int stage, double dt, double nu,
+                            const R *f, R *qn, R *f1, cudaStream_t st);
+
+// Inverse transform FS of q, full complex output (for the reference-shaped FS).
+template <typename R>
+cudaError_t launch_fs_full(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
+                           typename V2<R>::t *out, const R *M, int n, int Bp, cudaStream_t st);
+
+// Forward transform of complex input (for the reference-shaped fft3D).
+template <typename R>
+cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t1,
+                               typename V2<R>::t *F, const R *M, int n, int Bp, cudaStream_t st);
+
+// q(xi) = sum_pairs P F(omega) F(u) for every xi and cell.
+template <typename R>
+cudaError_t launch_computeq(const typename V2<R>::t *F, const R *P, const unsigned *PI,
+                            const int *pair_off, int n3, int Bp, double2 *q, cudaStream_t st);
+
+// Moment-conserving projection of q in place (FP64).
+cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
+                            int n3, int Bp, double *part, int nchunk, double *lam,
+                            cudaStream_t st);
+
+// Final RK4 combination, DG projection and mass-matrix inverse: writes
+// dU[B][nv^3][5] for cells [c0, c0+B).  Qc, Y, Z are scratch.
+template <typename R>
+cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *q2,
+                           const double2 *q3, double nu, const R *tfac, int n, int nv, int Bp,
+                           int B, int c0, const double *U, int ustride, const int *uslot,
+                           double dt, double scalev, double scaleL, double scale3,
+                           typename V2<R>::t *Qc, typename V2<R>::t *Y, typename V2<R>::t *Z,
+                           double *dU, cudaStream_t st);
+
+// Mixed path: reconcile the 5 DG moments of each cell's increment with their
+// FP64 values from the mode array (minimal-norm 5x5 Lagrange correction).
+cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
+                              double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
+                              const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
+                              double *apart, const double *gm_inv, double scale, double *lam, double *dU,
+                              cudaStream_t st);
+
+// U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU.
+cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st);
+
+// ---- advection and Poisson (FP64) ----
+cudaError_t launch_charge(const double *U, int ncell, int nv3, double scalev, double *rt,
+                          cudaStream_t st);
+
+struct PoissonDev {
+    int nx, ny, ndim, kl, ku, ldab;
+    const double *ab;
+    const int *ipiv;
+    double dxp, dyp;
+    const unsigned char *gate;  // per x1 cell, 1-based
+    double blk[6][9];           // acvx, acyrr, acyrl, acvy, acxrr, acxrl
+};
+cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, double *b, double *potc,
+                           double *phix, double *phiy, double *fields, cudaStream_t st);
+
+struct AdvectDev {
+    int nx1, nx2, nv;
+    long long size;
+    double lv, dv, dx, scalev, dt;
+};
+// One SSP-RK3 stage: Uout = combination(U0, Us, H(Us)).
+cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us,
+                              const double *fields, int stage, double *Uout, cudaStream_t st);
+
+// Block partial sums of the moments (mass, p1, p2, p3, kinetic energy).
+cudaError_t launch_moments(const double *U, long long size, long long kend, int nv, double lv,
+                           double dv, double *part, int nblk, cudaStream_t st);
+
+}  // namespace lp

@@ -1,0 +1,251 @@
+"""Python binding of the C ABI in include/lp_gb300.h (ctypes over
+_build/liblp_gb300.so).  Every call goes to the GPU library; there is no
+CPU fallback: a missing library or device raises.
+
+    import lp_gb300 as lp
+    ctx = lp.Context(lp.Params(nx1=64, nx2=1, nv=24, n=24, lv=6.0, lx=4*pi, nu=0.05,
+                               dt=0.005, a_amp=0.5, k_wave=0.5))
+    ctx.set_init(1)
+    ctx.step(10)
+    U = ctx.get_state()
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "liblp_gb300.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_NO_DEVICE, ERR_STATE = range(6)
+FIX_F1, FIX_F2, FIX_F3, FIX_F11 = 1, 2, 4, 8
+FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3
+PREC_FP64, PREC_MIXED = 0, 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+EXPORTS = [
+    "lp_ctx_create", "lp_ctx_destroy", "lp_set_stream", "lp_synchronize", "lp_last_error",
+    "lp_device_bytes", "lp_set_state", "lp_get_state", "lp_state_device_ptr", "lp_set_init",
+    "lp_fft3d", "lp_fs", "lp_compute_q", "lp_conserve", "lp_rk4_cell", "lp_nodes",
+    "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_advect_step",
+    "lp_collision_step", "lp_step", "lp_moments",
+]
+
+
+class LPError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"lp status {status}: {msg}")
+        self.status = status
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nv", ctypes.c_int),
+                ("n", ctypes.c_int), ("lv", ctypes.c_double), ("lx", ctypes.c_double),
+                ("nu", ctypes.c_double), ("dt", ctypes.c_double), ("a_amp", ctypes.c_double),
+                ("k_wave", ctypes.c_double), ("fixes", ctypes.c_uint), ("precision", ctypes.c_int)]
+
+
+@dataclass
+class Params:
+    nx1: int
+    nx2: int
+    nv: int
+    n: int
+    lv: float = 5.25
+    lx: float = 4.0 * np.pi
+    nu: float = 0.01
+    dt: float = 0.01
+    a_amp: float = 0.01
+    k_wave: float = 0.5
+    fixes: int = FIX_DEFAULT
+    precision: int = PREC_FP64
+
+    @property
+    def ncell(self):
+        return self.nx1 * self.nx2
+
+    @property
+    def size(self):
+        return self.ncell * self.nv ** 3
+
+    def _c(self):
+        return _Params(self.nx1, self.nx2, self.nv, self.n, self.lv, self.lx, self.nu, self.dt,
+                       self.a_amp, self.k_wave, self.fixes, self.precision)
+
+
+_lib = None
+
+
+def lib():
+    """Load liblp_gb300.so (raises FileNotFoundError when it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing; run the package build first")
+        L = ctypes.CDLL(LIB_PATH)
+        L.lp_ctx_create.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_vp)]
+        L.lp_last_error.restype = ctypes.c_char_p
+        L.lp_last_error.argtypes = [_vp]
+        L.lp_device_bytes.restype = ctypes.c_size_t
+        L.lp_device_bytes.argtypes = [_vp]
+        for name in ["lp_ctx_destroy", "lp_synchronize"]:
+            getattr(L, name).argtypes = [_vp]
+        L.lp_set_stream.argtypes = [_vp, _vp]
+        L.lp_set_state.argtypes = [_vp, _dp, ctypes.c_size_t]
+        L.lp_get_state.argtypes = [_vp, _dp, ctypes.c_size_t]
+        L.lp_state_device_ptr.argtypes = [_vp, ctypes.POINTER(_dp)]
+        L.lp_set_init.argtypes = [_vp, ctypes.c_int, ctypes.c_double]
+        L.lp_fft3d.argtypes = [_vp, _dp, _dp]
+        L.lp_fs.argtypes = [_vp, _dp, _dp]
+        L.lp_compute_q.argtypes = [_vp, _dp, _dp]
+        L.lp_conserve.argtypes = [_vp, _dp]
+        L.lp_rk4_cell.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp]
+        L.lp_nodes.argtypes = [_vp, _dp]
+        L.lp_weights_rows.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
+        L.lp_conservation_rows.argtypes = [_vp, _dp, _dp, _dp]
+        L.lp_poisson.argtypes = [_vp, _dp, _dp, _dp, _dp]
+        L.lp_advect_step.argtypes = [_vp]
+        L.lp_collision_step.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+        L.lp_step.argtypes = [_vp, ctypes.c_int]
+        L.lp_moments.argtypes = [_vp, _dp]
+        for name in EXPORTS:
+            f = getattr(L, name)
+            if name not in ("lp_last_error", "lp_device_bytes"):
+                f.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """One solver instance on the current CUDA device."""
+
+    def __init__(self, params: Params):
+        self.params = params
+        self.L = lib()
+        h = _vp()
+        st = self.L.lp_ctx_create(ctypes.byref(params._c()), ctypes.byref(h))
+        if st != OK:
+            raise LPError(st, "lp_ctx_create failed")
+        self.h = h
+        self.n3 = params.n ** 3
+        self.nv3 = params.nv ** 3
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lp_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st):
+        if st != OK:
+            raise LPError(st, self.L.lp_last_error(self.h).decode())
+
+    @property
+    def device_bytes(self):
+        return int(self.L.lp_device_bytes(self.h))
+
+    def set_stream(self, stream_handle):
+        self._chk(self.L.lp_set_stream(self.h, _vp(stream_handle)))
+
+    def synchronize(self):
+        self._chk(self.L.lp_synchronize(self.h))
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+        self._chk(self.L.lp_set_state(self.h, _p(U), U.size))
+
+    def get_state(self):
+        U = np.zeros(self.params.size * 7)
+        self._chk(self.L.lp_get_state(self.h, _p(U), U.size))
+        return U
+
+    def state_device_ptr(self):
+        p = _dp()
+        self._chk(self.L.lp_state_device_ptr(self.h, ctypes.byref(p)))
+        return ctypes.cast(p, ctypes.c_void_p).value
+
+    def set_init(self, kind=0, u=2.0):
+        self._chk(self.L.lp_set_init(self.h, int(kind), float(u)))
+
+    def fft3d(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)
+        out = np.zeros_like(x)
+        self._chk(self.L.lp_fft3d(self.h, _p(x.view(np.float64)), _p(out.view(np.float64))))
+        return out
+
+    def fs(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)
+        out = np.zeros_like(x)
+        self._chk(self.L.lp_fs(self.h, _p(x.view(np.float64)), _p(out.view(np.float64))))
+        return out
+
+    def compute_q(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        q = np.zeros(self.n3, np.complex128)
+        self._chk(self.L.lp_compute_q(self.h, _p(f), _p(q.view(np.float64))))
+        return q
+
+    def conserve(self, q):
+        q = np.array(q, dtype=np.complex128).reshape(-1)
+        self._chk(self.L.lp_conserve(self.h, _p(q.view(np.float64))))
+        return q
+
+    def rk4_cell(self, f, cell, qhat):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(qhat, dtype=np.complex128).reshape(-1)
+        du = np.zeros(self.nv3 * 5)
+        self._chk(self.L.lp_rk4_cell(self.h, _p(f), int(cell), _p(q.view(np.float64)), _p(du)))
+        return du
+
+    def nodes(self, ncollide=None):
+        nc = ncollide if ncollide is not None else self.params.ncell
+        f = np.zeros(nc * self.n3)
+        self._chk(self.L.lp_nodes(self.h, _p(f)))
+        return f.reshape(nc, self.n3)
+
+    def weights_rows(self, r0, r1):
+        out = np.zeros((r1 - r0) * self.n3)
+        self._chk(self.L.lp_weights_rows(self.h, int(r0), int(r1), _p(out)))
+        return out.reshape(r1 - r0, self.n3)
+
+    def conservation_rows(self):
+        c1 = np.zeros(5 * self.n3); c2 = np.zeros(5 * self.n3); cct = np.zeros(25)
+        self._chk(self.L.lp_conservation_rows(self.h, _p(c1), _p(c2), _p(cct)))
+        return c1.reshape(5, -1), c2.reshape(5, -1), cct.reshape(5, 5)
+
+    def poisson(self):
+        nc = self.params.ncell
+        potc, px, py, fl = np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(14 * nc)
+        self._chk(self.L.lp_poisson(self.h, _p(potc), _p(px), _p(py), _p(fl)))
+        return potc, px, py, fl.reshape(14, nc)
+
+    def advect_step(self):
+        self._chk(self.L.lp_advect_step(self.h))
+
+    def collision_step(self, c0=-1, c1=-1):
+        self._chk(self.L.lp_collision_step(self.h, int(c0), int(c1)))
+
+    def step(self, nsteps=1):
+        self._chk(self.L.lp_step(self.h, int(nsteps)))
+
+    def moments(self):
+        out = np.zeros(6)
+        self._chk(self.L.lp_moments(self.h, _p(out)))
+        return out

@@ -1,0 +1,92 @@
+"""Generates the golden vectors in tests/golden/*.npz from the reference's own
+routines, compiled from the reference checkout by oracle/build_ref.sh (this
+script runs only where that checkout exists; the fixtures it writes are
+committed and travel everywhere).
+
+Each fixture holds seeded inputs and the reference outputs of: grids, the
+conservation rows and inverse Gram matrix, rows of the weight table, fft3D,
+FS, SetInit_LD, setInit_spectral, ComputeQ, conserveAllMoments, IntModes,
+RK4 (zero state, so the stride defect F1 does not enter), pois2d, the band
+factors, one RK3 step, the verbatim collision driver and the moments.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Case, Reference  # noqa: E402
+
+SEED = 20261203
+
+# (name, case): small 2-D cases the reference can run (nx1 = nx2 <= 49).
+CASES = [
+    ("ref_n8", Case(nx1=3, nx2=3, nv=6, n=8, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.005,
+                    a_amp=0.5, k_wave=0.5)),
+    ("ref_n16", Case(nx1=2, nx2=2, nv=4, n=16, lv=5.25, lx=4 * np.pi, nu=0.01, dt=0.01,
+                     a_amp=0.01, k_wave=0.5)),
+    ("ref_n24", Case(nx1=2, nx2=2, nv=4, n=24, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.005,
+                     a_amp=0.5, k_wave=0.5)),
+]
+
+
+def make(name, case, rng):
+    R = Reference(case, with_weights=True)
+    n, nv, n3, nv3 = case.n, case.nv, case.n ** 3, case.nv ** 3
+    out = {"case": np.array([case.nx1, case.nx2, case.nv, case.n], np.int64),
+           "case_f": np.array([case.lv, case.lx, case.nu, case.dt, case.a_amp, case.k_wave])}
+    v, eta, wt, sc = R.grids()
+    out.update(v=v, eta=eta, wt=wt, scalars=sc)
+    c1, c2, cct = R.cons()
+    out.update(c1_rows=c1[[0, 4]], c2_rows=c2[[1, 2, 3]], cct_inv=cct)
+    rows = np.sort(rng.choice(n3, 6, replace=False))
+    out.update(w_rows=rows, w_vals=np.stack([R.weights(int(r), int(r) + 1)[0] for r in rows]))
+    x = rng.standard_normal(n3) + 1j * rng.standard_normal(n3)
+    out.update(fft_in=x, fft_out=R.fft3d(x), fs_out=R.fs(x))
+    U = R.set_init_ld()
+    out.update(U_init=U)
+    # node sampling with slot 2 == slot 3 so that defect F2 does not enter
+    U2 = U.copy().reshape(-1, 7)
+    U2[:, 2] = U2[:, 3]
+    U2 = U2.ravel()
+    fnodes = R.set_init_spectral(U2)
+    out.update(U_nodes=U2, nodes=fnodes)
+    f = fnodes[1].copy()
+    q = R.compute_q(f)
+    qc = R.conserve(q)
+    out.update(f_cell=f, qhat=q, qhat_cons=qc)
+    picks = rng.integers(0, [n, n, n, nv, nv, nv], size=(8, 6))
+    out.update(im_idx=picks, im_vals=np.stack([R.intmodes(*map(int, p)) for p in picks]))
+    Uz = np.zeros_like(U)
+    out.update(rk4_cell=np.int64(1), rk4_du=R.rk4(f, 1, qc, Uz))
+    potc, px, py, fl = R.pois2d(U)
+    out.update(pois_potc=potc, pois_phix=px, pois_phiy=py, pois_fields=fl)
+    dims, ab, piv = R.band()
+    out.update(band_dims=dims, band_ab=ab, band_piv=piv)
+    Up = U + 1e-3 * rng.standard_normal(U.shape) * np.abs(U).max()
+    U3, p3, x3, y3 = R.rk3(Up)
+    out.update(rk3_in=Up, rk3_out=U3)
+    out.update(coll_in=Up, coll_du=R.collision_cells(Up, 0, case.nx1))
+    out.update(moments=R.moments(U3, x3, y3), moments_phix=x3, moments_phiy=y3)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main():
+    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    rng = np.random.default_rng(SEED)
+    for name, case in CASES:
+        make(name, case, rng)
+
+
+if __name__ == "__main__":
+    main()
