@@ -132,6 +132,30 @@ lp_status lp_step(lp_ctx *ctx, int nsteps);
  * Poisson solve}. */
 lp_status lp_moments(lp_ctx *ctx, double *out6);
 
+/* ---- allocation-free projection ---------------------------------------- */
+/* No counterpart in the reference.  The moment-conserving projection of
+ * lp_conserve for `ncell` mode arrays at once, for callers that may not
+ * allocate device memory when they call it: code whose device memory belongs
+ * to another framework's pool, or a time-critical loop in which cudaMalloc
+ * and cudaFree (which can synchronise the whole device) are not allowed.
+ * Nothing is allocated: the caller passes, in device memory it owns,
+ *   qhat_dev     ncell x n3 complex doubles (re, im interleaved), the
+ *                reference's layout, projected in place (16-byte aligned);
+ *   c1_dev, c2_dev  the 5 x n3 constraint rows and cct_inv_dev the inverse
+ *                Gram matrix (25 doubles), e.g. copied from
+ *                lp_conservation_rows;
+ * and the work runs on cuda_stream (NULL: the legacy default stream).
+ * Scratch lives in one fixed device array inside the library sized for
+ * LP_NOALLOC_MAX_CELLS cells (about 2.8 MB, held by every GPU that loads the
+ * library until the process exits); larger ncell is rejected with
+ * LP_ERR_INVALID.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first
+ * call before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU race and must be serialised. */
+#define LP_NOALLOC_MAX_CELLS 4096
+lp_status lp_conserve_noalloc(double *qhat_dev, int ncell, int n3, const double *c1_dev,
+                              const double *c2_dev, const double *cct_inv_dev, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

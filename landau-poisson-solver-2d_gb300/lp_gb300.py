@@ -33,8 +33,9 @@ EXPORTS = [
     "lp_device_bytes", "lp_set_state", "lp_get_state", "lp_state_device_ptr", "lp_set_init",
     "lp_fft3d", "lp_fs", "lp_compute_q", "lp_conserve", "lp_rk4_cell", "lp_nodes",
     "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_advect_step",
-    "lp_collision_step", "lp_step", "lp_moments",
+    "lp_collision_step", "lp_step", "lp_moments", "lp_conserve_noalloc",
 ]
+NOALLOC_MAX_CELLS = 4096
 
 
 class LPError(RuntimeError):
@@ -113,6 +114,7 @@ def lib():
         L.lp_collision_step.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
         L.lp_step.argtypes = [_vp, ctypes.c_int]
         L.lp_moments.argtypes = [_vp, _dp]
+        L.lp_conserve_noalloc.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes"):
