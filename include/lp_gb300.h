@@ -120,6 +120,10 @@ lp_status lp_conservation_rows(lp_ctx *ctx, double *c1, double *c2, double *cct_
  * each) and fields (14*ncell: IE_X, IXE_X, IYE_X, IXXE_X, IXYE_X, IYYE_X,
  * the same six for Y, SE_X, SE_Y) are optional host outputs. */
 lp_status lp_poisson(lp_ctx *ctx, double *potc, double *phix, double *phiy, double *fields);
+/* Results of the last Poisson solve on the device (after lp_advect_step:
+ * the solve on the third stage's input, as the reference's RK3 leaves them);
+ * same outputs as lp_poisson, all optional. */
+lp_status lp_last_fields(lp_ctx *ctx, double *potc, double *phix, double *phiy, double *fields);
 /* One SSP-RK3 advection step of the resident state. */
 lp_status lp_advect_step(lp_ctx *ctx);
 /* Collision step of spatial cells [cell_begin, cell_end) of the resident
@@ -131,6 +135,17 @@ lp_status lp_step(lp_ctx *ctx, int nsteps);
 /* out = {mass, p1, p2, p3, kinetic energy, electric energy of the last
  * Poisson solve}. */
 lp_status lp_moments(lp_ctx *ctx, double *out6);
+
+/* ---- measurement helpers (no reference counterpart) --------------------- */
+/* Average device time in ms of one launch of a hot-path stage on the
+ * context's stream, over `reps` launches after one warm-up, timed with CUDA
+ * events: which = 0 the weighted contraction of ComputeQ for every collided
+ * cell, 1 the forward transform, 2 the moment-conserving projection, 3 the
+ * DG projection of the RK4 combination.  Needs the resident state. */
+lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
+/* Dense FMA throughput of the current device measured with dependent-chain
+ * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */
+lp_status lp_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
 
 /* ---- allocation-free projection ---------------------------------------- */
 /* No counterpart in the reference.  The moment-conserving projection of

@@ -32,6 +32,8 @@ struct lp_ctx {
     void *tfac = nullptr, *mfwd = nullptr, *minv = nullptr;  // R precision
     void *P = nullptr;                                       // R precision
     unsigned *PI = nullptr;
+    float *LW = nullptr;            // line-tiled weight table (mixed path)
+    long long *line_off = nullptr;
     double *ab = nullptr;
     // state and advection
     double *U = nullptr, *U1 = nullptr, *Ut = nullptr, *rt = nullptr, *pb = nullptr, *potc = nullptr,
@@ -154,14 +156,23 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
     LP_TRY(upload_real<R>(c, &c->tfac, T.tfac));
     LP_TRY(upload_real<R>(c, &c->mfwd, T.mfwd));
     LP_TRY(upload_real<R>(c, &c->minv, T.minv));
-    const size_t npair = (size_t)T.pair_off[T.n3];
-    R *P = nullptr;
-    LP_TRY(dalloc(c, &P, npair));
-    LP_TRY(dalloc(c, &c->PI, npair));
-    c->P = P;
-    LP_CUDA(lp::launch_pairs(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->pair_off, T.n,
-                             std::is_same<R, double>::value ? (double *)P : nullptr,
-                             std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
+    if (c->mixed && lp::lines_supported(T.n)) {
+        std::vector<long long> off;
+        const long long nw = lp::lines_table_floats(T.n, off);
+        LP_TRY(upload(c, &c->line_off, off.data(), off.size()));
+        LP_TRY(dalloc(c, &c->LW, (size_t)nw));
+        LP_CUDA(lp::launch_lines_table(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->line_off, T.n, c->LW,
+                                       c->stream));
+    } else {
+        const size_t npair = (size_t)T.pair_off[T.n3];
+        R *P = nullptr;
+        LP_TRY(dalloc(c, &P, npair));
+        LP_TRY(dalloc(c, &c->PI, npair));
+        c->P = P;
+        LP_CUDA(lp::launch_pairs(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->pair_off, T.n,
+                                 std::is_same<R, double>::value ? (double *)P : nullptr,
+                                 std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
+    }
     // Poisson
     LP_TRY(upload(c, &c->ab, T.pois.ab.data(), T.pois.ab.size()));
     LP_TRY(upload(c, &c->ipiv, T.pois.ipiv.data(), T.pois.ipiv.size()));
@@ -208,6 +219,18 @@ lp_status advect(lp_ctx *c) {
     return LP_OK;
 }
 
+// The weighted contraction of ComputeQ on the transformed node values F.
+template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    if (c->LW) {
+        LP_CUDA(lp::launch_computeq_lines((const float2 *)c->F, c->LW, c->line_off, T.n, Bp, q, c->stream));
+        return LP_OK;
+    }
+    LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, q, c->stream));
+    return LP_OK;
+}
+
 // RK4 stages 1-3 (C:831-865) from node values f and conserved q[0].
 template <typename R> lp_status rk4_stages(lp_ctx *c, int Bp) {
     using C = typename V2<R>::t;
@@ -217,8 +240,7 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int Bp) {
         LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
                                        (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream));
         LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
-        LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, c->q[s + 1],
-                                       c->stream));
+        LP_TRY(contract<R>(c, Bp, c->q[s + 1]));
         LP_CUDA(lp::launch_conserve(c->q[s + 1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam,
                                     c->stream));
     }
@@ -251,11 +273,26 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
-    LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, c->q[0],
-                                   c->stream));
+    LP_TRY(contract<R>(c, Bp, c->q[0]));
     LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
     LP_TRY(rk4_stages<R>(c, Bp));
     LP_TRY(project<R>(c, c0, B, Bp));
+    return LP_OK;
+}
+
+// Nodes, forward transform and conserved q[0..3] of cells [c0, c0+B): the
+// inputs of every stage, for lp_time_kernel.
+template <typename R> lp_status collide_batch_prefix(lp_ctx *c, int c0, int B) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    const int Bp = round32(B);
+    const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
+    LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
+                                c->stream));
+    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
+    LP_TRY(contract<R>(c, Bp, c->q[0]));
+    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_TRY(rk4_stages<R>(c, Bp));
     return LP_OK;
 }
 
@@ -331,7 +368,7 @@ template <typename R> lp_status do_compute_q(lp_ctx *c, const double *f, double 
     const lp::Tables &T = c->T;
     LP_TRY(put_real_column<R>(c, (R *)c->f, f, T.n3));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, 32, c->stream));
-    LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, 32, c->q[0], c->stream));
+    LP_TRY(contract<R>(c, 32, c->q[0]));
     return get_cplx_column<double>(c, qhat, c->q[0], T.n3);
 }
 
@@ -596,6 +633,17 @@ lp_status lp_poisson(lp_ctx *c, double *potc, double *phix, double *phiy, double
     return LP_OK;
 }
 
+lp_status lp_last_fields(lp_ctx *c, double *potc, double *phix, double *phiy, double *fields) {
+    if (!c) return LP_ERR_INVALID;
+    const size_t nc = c->T.ncell;
+    if (potc) LP_CUDA(cudaMemcpyAsync(potc, c->potc, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (phix) LP_CUDA(cudaMemcpyAsync(phix, c->phix, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (phiy) LP_CUDA(cudaMemcpyAsync(phiy, c->phiy, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    if (fields) LP_CUDA(cudaMemcpyAsync(fields, c->fields, sizeof(double) * 14 * nc, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
 lp_status lp_advect_step(lp_ctx *c) {
     if (!c) return LP_ERR_INVALID;
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
@@ -629,6 +677,78 @@ lp_status lp_step(lp_ctx *c, int nsteps) {
         c->gstream = c->stream;
     }
     for (int i = 0; i < nsteps; ++i) LP_CUDA(cudaGraphLaunch(c->gexec, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
+    if (!c || !ms || reps < 1 || which < 0 || which > 3) return fail(c, LP_ERR_INVALID, "bad argument");
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    const lp::Tables &T = c->T;
+    const int B = std::min(c->Bcap, T.ncollide), Bp = round32(B);
+    // inputs of every stage: node values, transform, one conserved mode array
+    lp_status s = c->mixed ? collide_batch_prefix<float>(c, 0, B) : collide_batch_prefix<double>(c, 0, B);
+    if (s != LP_OK) return s;
+    auto run = [&]() -> lp_status {
+        switch (which) {
+        case 0: return c->mixed ? contract<float>(c, Bp, c->q[1]) : contract<double>(c, Bp, c->q[1]);
+        case 1:
+            if (c->mixed) LP_CUDA(lp::launch_fwd<float>((const float *)c->f, (float2 *)c->t1, (float2 *)c->F, (const float *)c->mfwd, T.n, Bp, c->stream));
+            else LP_CUDA(lp::launch_fwd<double>((const double *)c->f, (double2 *)c->t1, (double2 *)c->F, (const double *)c->mfwd, T.n, Bp, c->stream));
+            return LP_OK;
+        case 2:
+            LP_CUDA(lp::launch_conserve(c->q[1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+            return LP_OK;
+        default: return c->mixed ? project<float>(c, 0, B, Bp) : project<double>(c, 0, B, Bp);
+        }
+    };
+    LP_TRY(run());
+    cudaEvent_t e0, e1;
+    LP_CUDA(cudaEventCreate(&e0));
+    LP_CUDA(cudaEventCreate(&e1));
+    LP_CUDA(cudaEventRecord(e0, c->stream));
+    for (int r = 0; r < reps; ++r) LP_TRY(run());
+    LP_CUDA(cudaEventRecord(e1, c->stream));
+    LP_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    LP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / reps;
+    return LP_OK;
+}
+
+lp_status lp_measure_fp_peaks(double *fp32, double *fp64) {
+    lp_ctx *c = nullptr;  // LP_CUDA reports through c; no context here
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return LP_ERR_NO_DEVICE;
+    double *sink = nullptr;
+    if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess) return LP_ERR_ALLOC;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8;
+    double out[2] = {0, 0};
+    for (int which = 0; which < 2; ++which) {
+        const int iters = which ? 2000 : 20000;
+        lp::launch_fma_peak(which == 1, blocks, iters / 10, sink, 0);
+        cudaEventRecord(e0, 0);
+        lp::launch_fma_peak(which == 1, blocks, iters, sink, 0);
+        cudaEventRecord(e1, 0);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        // flops: threads * iters * 8 chains * (2 per FMA) * (2 lanes for f32x2)
+        const double flops = (double)blocks * 256 * iters * 8 * 2 * (which ? 1 : 2);
+        out[which] = t > 0 ? flops / (t * 1e-3) / 1e12 : 0.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    (void)c;
+    if (cudaGetLastError() != cudaSuccess) return LP_ERR_CUDA;
+    if (fp32) *fp32 = out[0];
+    if (fp64) *fp64 = out[1];
     return LP_OK;
 }
 

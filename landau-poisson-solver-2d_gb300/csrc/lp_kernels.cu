@@ -86,9 +86,9 @@ __global__ void k_nodes(const double *__restrict__ U, int nv, int n, int c0, int
     const int l = pt / (n * n), m = (pt / n) % n, q = pt % n;
     const int j1 = nodecell[l], j2 = nodecell[m], j3 = nodecell[q];
     const double *u = U + 7 * ((long long)(c0 + c) * nv * nv * nv + (j1 * nv + j2) * nv + j3);
-    const double o1 = nodeoff[l], o2 = nodeoff[m], o3 = nodeoff[q];
-    const double a = o1 / dv, b = o2 / dv, e = o3 / dv;
-    const double val = u[0] + u[slot1] * o1 / dv + u[4] * o2 / dv + u[5] * o3 / dv + u[6] * (a * a + b * b + e * e);
+    // nodeoff holds (v[l] - Gridv(j)) / dv, so no division per node
+    const double a = nodeoff[l], b = nodeoff[m], e = nodeoff[q];
+    const double val = u[0] + u[slot1] * a + u[4] * b + u[5] * e + u[6] * (a * a + b * b + e * e);
     f[tid] = (R)val;
 }
 
@@ -189,6 +189,249 @@ __global__ void __launch_bounds__(128) k_computeq(const typename V2<R>::t *__res
     q[(long long)xi * Bp + c] = make_double2(ar, ai);
 }
 
+// ---------------------------------------------------------------- line-tiled contraction
+// For output xi = (i, j, k) the window of omega = (l, m, k') is a box; the
+// planes (l, m) pair up under (l, m) -> (i+h-l, j+h-m) and, inside a pair,
+// term (l, m, k') of one plane and term (i+h-l, j+h-m, k+h-k') of the other
+// multiply the same product A(k') B(k+h-k') with A = F(l, m, .),
+// B = F(i+h-l, j+h-m, .).  The weight table holds, per (line, plane pair,
+// k-tile), the combined weights in (k, k') order, padded to 4 floats.
+template <int N> __host__ __device__ constexpr int wlo(int k) { return k < N / 2 ? 0 : k - N / 2 + 1; }
+template <int N> __host__ __device__ constexpr int whi(int k) { return k < N / 2 ? k + N / 2 + 1 : N; }
+template <int N> __host__ __device__ constexpr int span_terms(int k0, int k1) {
+    int s = 0;
+    for (int k = k0; k < k1; ++k) s += whi<N>(k) - wlo<N>(k);
+    return s;
+}
+__host__ __device__ constexpr int pad4(int x) { return (x + 3) & ~3; }
+// floats of one tile's weights per plane pair, padded to 16 bytes
+template <int N> __host__ __device__ constexpr int tile_floats(int k0, int k1) { return pad4(span_terms<N>(k0, k1)); }
+template <int N, int KT> __host__ __device__ constexpr int tile_off(int t) {
+    int s = 0;
+    for (int u = 0; u < t; ++u) s += tile_floats<N>(u * KT, (u + 1) * KT);
+    return s;
+}
+template <int N, int KT> __host__ __device__ constexpr int pp_floats() { return tile_off<N, KT>(N / KT); }
+// Inside a tile the terms are stored k'-major (then k), so consecutive terms
+// feed different accumulators: k' = n pairs with k in [n - N/2, n + N/2 - 1].
+template <int N> __host__ __device__ constexpr int klo_of(int n, int K0) { return n - N / 2 > K0 ? n - N / 2 : K0; }
+template <int N> __host__ __device__ constexpr int khi_of(int n, int K1) { return n + N / 2 - 1 < K1 - 1 ? n + N / 2 - 1 : K1 - 1; }
+template <int N> __host__ __device__ constexpr int nmaj_before(int n, int K0, int K1) {
+    int s = 0;
+    for (int nn = 0; nn < n; ++nn) {
+        const int c = khi_of<N>(nn, K1) - klo_of<N>(nn, K0) + 1;
+        s += c > 0 ? c : 0;
+    }
+    return s;
+}
+
+template <int N> struct LinesCfg;
+template <> struct LinesCfg<8> { static constexpr int KT = 8; };
+template <> struct LinesCfg<16> { static constexpr int KT = 8; };
+template <> struct LinesCfg<24> { static constexpr int KT = 12; };
+template <> struct LinesCfg<32> { static constexpr int KT = 8; };
+constexpr int kLineWarps = 2;  // warps of a block share one output line tile
+
+__device__ __forceinline__ float pick4(const float4 &v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w)); }
+
+// Packed FP32x2 helpers (Blackwell f32x2 arithmetic on 64-bit register pairs).
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 up2(unsigned long long v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return make_float2(lo, hi);
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// One k-tile of output lines.  The kLineWarps warps of a block take the
+// plane pairs of the same (line, tile, 32 cells) in turn; each warp stages
+// the next plane pair's two F lines in shared memory with cp.async (double
+// buffered, every lane copying its own cell) together with the plane pair's
+// weights, while it computes the current one from registers.  Per plane pair, with a = A(k'), b = B(k+h-k') and
+// weight w: U += (w a) (bx, by) and V += (w a) (by, bx) in packed FP32x2, so
+// Re = U.x - U.y, Im = V.x + V.y; each plane's partials enter a
+// Kahan-compensated FP32 accumulator, and the warps' results are summed in
+// FP64 in a fixed order.
+template <int N, int TILE>
+__global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
+                                                            const long long *__restrict__ line_off, int Bp,
+                                                            double2 *__restrict__ q) {
+    constexpr int KT = LinesCfg<N>::KT, h = N / 2, K0 = TILE * KT;
+    constexpr int TP = pp_floats<N, KT>(), TOFF = tile_off<N, KT>(TILE);
+    constexpr int TT = tile_floats<N>(K0, K0 + KT);  // weight floats of this tile per plane pair
+    extern __shared__ __align__(16) unsigned char lines_smem[];
+    // per warp: [2 buffers][2 lines][N][32 lanes] float2; then per warp
+    // [2 buffers][TT] weights; then the reduction area
+    float2 *stage = reinterpret_cast<float2 *>(lines_smem);
+    float *wstage = reinterpret_cast<float *>(lines_smem + sizeof(float2) * 4 * N * 32 * kLineWarps);
+    double2 *red = reinterpret_cast<double2 *>(lines_smem);  // reuses the staging area after the loop
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *mybuf = stage + (long long)warp * 4 * N * 32;
+    float *mywbuf = wstage + warp * 2 * TT;
+    const int G = Bp / 32;
+    const int g = (int)(blockIdx.x % G), ij = (int)(blockIdx.x / G);
+    const int i = ij / N, j = ij % N;
+    const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
+    const int sj = j < h ? 0 : j - h + 1, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+    const int npp = (ni * nj + 1) / 2;
+    const int c = g * 32 + lane;
+    const float *wbase = W + line_off[ij] + TOFF;
+    auto stage_pp = [&](int pp, int buf) {
+        const int l = si + pp / nj, m = sj + pp % nj;
+        const int x = i + h - l, y = j + h - m;
+        const float2 *Al = F + (long long)((l * N + m) * N) * Bp + c;
+        const float2 *Bl = F + (long long)((x * N + y) * N) * Bp + c;
+        float2 *dA = mybuf + (buf * 2 + 0) * N * 32 + lane;
+        float2 *dB = mybuf + (buf * 2 + 1) * N * 32 + lane;
+#pragma unroll
+        for (int n = 0; n < N; ++n) {
+            cp_async8(dA + n * 32, Al + (long long)n * Bp);
+            cp_async8(dB + n * 32, Bl + (long long)n * Bp);
+        }
+        const float *ws = wbase + (long long)pp * TP;
+        float *wd = mywbuf + buf * TT;
+        for (int q4 = lane; q4 < TT / 4; q4 += 32) cp_async16(wd + 4 * q4, ws + 4 * q4);
+    };
+    float sr[KT], sim[KT], cr[KT], ci[KT];
+    unsigned long long U[KT], V[KT];
+#pragma unroll
+    for (int kk = 0; kk < KT; ++kk) { sr[kk] = 0.f; sim[kk] = 0.f; cr[kk] = 0.f; ci[kk] = 0.f; U[kk] = 0ull; V[kk] = 0ull; }
+    if (warp < npp) stage_pp(warp, 0);
+    cp_async_commit();
+    int it = 0;
+    for (int pp = warp; pp < npp; pp += kLineWarps, ++it) {
+        const int nxt = pp + kLineWarps;
+        if (nxt < npp) stage_pp(nxt, (it + 1) & 1);
+        cp_async_commit();
+        cp_async_wait1();
+        __syncwarp();
+        const float2 *sA = mybuf + ((it & 1) * 2 + 0) * N * 32 + lane;
+        const float2 *sB = mybuf + ((it & 1) * 2 + 1) * N * 32 + lane;
+        const float *wp = mywbuf + (it & 1) * TT;
+        unsigned long long A[N], B[N], Bs[N];
+#pragma unroll
+        for (int n = 0; n < N; ++n) {
+            const float2 a = sA[n * 32], b = sB[n * 32];
+            A[n] = pk2(a.x, a.y);
+            B[n] = pk2(b.x, b.y);
+            Bs[n] = pk2(b.y, b.x);
+        }
+        float4 w4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int kk = 0; kk < KT; ++kk) { U[kk] = 0ull; V[kk] = 0ull; }
+#pragma unroll
+        for (int n = 0; n < N; ++n) {
+#pragma unroll
+            for (int k = klo_of<N>(n, K0); k <= khi_of<N>(n, K0 + KT); ++k) {
+                const int t = nmaj_before<N>(n, K0, K0 + KT) + k - klo_of<N>(n, K0);
+                if ((t & 3) == 0) w4 = *reinterpret_cast<const float4 *>(wp + t);
+                const float wt = pick4(w4, t & 3);
+                const unsigned long long wa = mul2(pk2(wt, wt), A[n]);
+                U[k - K0] = fma2(wa, B[k + h - n], U[k - K0]);
+                V[k - K0] = fma2(wa, Bs[k + h - n], V[k - K0]);
+            }
+        }
+        {
+#pragma unroll
+        for (int kk = 0; kk < KT; ++kk) {
+            const float2 u2 = up2(U[kk]), v2 = up2(V[kk]);
+            const float pr = u2.x - u2.y, pm = v2.x + v2.y;
+            float yr = pr - cr[kk], tr = sr[kk] + yr;  // Kahan: s + (p - c)
+            cr[kk] = (tr - sr[kk]) - yr; sr[kk] = tr;
+            float yi = pm - ci[kk], ti = sim[kk] + yi;
+            ci[kk] = (ti - sim[kk]) - yi; sim[kk] = ti;
+        }
+        }
+        __syncwarp();
+    }
+    cp_async_wait0();
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < KT; ++kk)
+        red[(warp * KT + kk) * 32 + lane] = make_double2((double)sr[kk] - (double)cr[kk], (double)sim[kk] - (double)ci[kk]);
+    __syncthreads();
+    for (int kk = warp; kk < KT; kk += kLineWarps) {
+        double2 acc = red[kk * 32 + lane];
+#pragma unroll
+        for (int w = 1; w < kLineWarps; ++w) {
+            const double2 v = red[(w * KT + kk) * 32 + lane];
+            acc.x += v.x; acc.y += v.y;
+        }
+        q[(long long)((i * N + j) * N + K0 + kk) * Bp + c] = acc;
+    }
+}
+
+template <int N, int T> constexpr size_t lines_smem_bytes() {
+    constexpr int KT = LinesCfg<N>::KT;
+    constexpr size_t staging = sizeof(float2) * 4 * N * 32 * kLineWarps +
+                               sizeof(float) * 2 * tile_floats<N>(T * KT, T * KT + KT) * kLineWarps;
+    constexpr size_t reduction = sizeof(double2) * kLineWarps * KT * 32;
+    return staging > reduction ? staging : reduction;
+}
+
+template <int N>
+__global__ void k_lines_table(const double *__restrict__ eta, const double *__restrict__ shat,
+                              const double *__restrict__ ahat, const unsigned char *__restrict__ rzero,
+                              const double *__restrict__ cw, const long long *__restrict__ line_off,
+                              float *__restrict__ W) {
+    constexpr int KT = LinesCfg<N>::KT, NT = N / KT, h = N / 2, TP = pp_floats<N, KT>();
+    const int ij = blockIdx.x, i = ij / N, j = ij % N;
+    const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
+    const int sj = j < h ? 0 : j - h + 1, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+    const int cntp = ni * nj, npp = (cntp + 1) / 2;
+    float *out = W + line_off[ij];
+    for (int idx = threadIdx.x; idx < npp * TP; idx += blockDim.x) {
+        const int pp = idx / TP;
+        int t = idx % TP;  // float offset inside the plane pair's block
+        // locate (tile, k, k') of slot t
+        int tile = 0;
+        while (tile + 1 < NT && t >= tile_off<N, KT>(tile + 1)) ++tile;
+        t -= tile_off<N, KT>(tile);  // term index inside the tile
+        const int K0 = tile * KT, K1 = K0 + KT;
+        int k = -1, kp = -1;
+        for (int nn = 0; nn < N; ++nn) {
+            const int lo = klo_of<N>(nn, K0), hi = khi_of<N>(nn, K1);
+            const int cnt = hi - lo + 1 > 0 ? hi - lo + 1 : 0;
+            if (t < cnt) { kp = nn; k = lo + t; break; }
+            t -= cnt;
+        }
+        if (kp < 0) { out[idx] = 0.f; continue; }  // padding
+        const int l = si + pp / nj, m = sj + pp % nj;
+        const int x = i + h - l, y = j + h - m;
+        const int xi_ = (i * N + j) * N + k;
+        const int om = (l * N + m) * N + kp, uu = (x * N + y) * N + (k + h - kp);
+        double wv = __dmul_rn(cw[om], weight_dev(eta, shat, ahat, rzero, N, i, j, k, om));
+        if (2 * pp != cntp - 1) wv = __dadd_rn(wv, __dmul_rn(cw[uu], weight_dev(eta, shat, ahat, rzero, N, i, j, k, uu)));
+        (void)xi_;
+        out[idx] = (float)wv;
+    }
+}
+
 // ---------------------------------------------------------------- conserve
 // conserveAllMoments (K:100-129): t = C q (5 dot products), lam = (CC^T)^-1 t,
 // q -= C^T lam.  Partial sums per chunk of points, then per cell.
@@ -216,18 +459,23 @@ __global__ void k_cons_partial(const double2 *__restrict__ q, const double *__re
     }
 }
 
+// One warp per cell: lanes sum the chunk partials (fixed order, then a fixed
+// shuffle tree), lane 0 solves (C C^T)^-1 t (solveWithCCt, K:49-55).
 __global__ void k_cons_lambda(const double *__restrict__ part, int nchunk, const double *__restrict__ cct,
                               int Bp, double *__restrict__ lam) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= Bp) return;
     double t[5] = {0, 0, 0, 0, 0};
-    for (int k = 0; k < nchunk; ++k)
+    for (int k = lane; k < nchunk; k += 32)
         for (int j = 0; j < 5; ++j) t[j] += part[((long long)k * 5 + j) * Bp + c];
-    for (int i = 0; i < 5; ++i) {  // solveWithCCt (K:49-55)
-        double s = 0.;
-        for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * t[j];
-        lam[(long long)i * Bp + c] = s;
-    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int j = 0; j < 5; ++j) t[j] += __shfl_down_sync(FULL, t[j], off);
+    if (lane == 0)
+        for (int i = 0; i < 5; ++i) {
+            double s = 0.;
+            for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * t[j];
+            lam[(long long)i * Bp + c] = s;
+        }
 }
 
 __global__ void k_cons_apply(double2 *__restrict__ q, const double *__restrict__ c1,
@@ -252,67 +500,100 @@ __global__ void k_qcomb(const double2 *__restrict__ q0, const double2 *__restric
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= total) return;
     const double2 a = q0[tid], b = q1[tid], d = q2[tid], e = q3[tid];
-    const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) / 6.);
-    const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) / 6.);
+    constexpr double sixth = 1. / 6.;
+    const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) * sixth);
+    const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) * sixth);
     Qc[tid] = mk2<R>((R)re, (R)im);
 }
 
 // tp_l(j) = Re sum_k IntModes_l(k, j) Qc(k) (C:867-889) evaluated as three
 // per-axis contractions with the factors T0, T1, T2 of IntModes (C:364-505).
+// Each thread owns a chunk of JB output indices along the contracted axis,
+// so every input element is read once per chunk.
+constexpr int JB = 8;
+
 template <typename R>
 __global__ void k_proj3(const typename V2<R>::t *__restrict__ Qc, const R *__restrict__ tf, int n, int nv,
                         int Bp, typename V2<R>::t *__restrict__ Y) {
+    const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long total = (long long)n * n * nv * Bp;
+    const long long total = (long long)n * n * nch * Bp;
     if (tid >= total) return;
     const int c = (int)(tid % Bp);
     long long r = tid / Bp;
-    const int j3 = (int)(r % nv); r /= nv;
+    const int ch = (int)(r % nch); r /= nch;
     const int k2 = (int)(r % n), k1 = (int)(r / n);
-    R s[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    const int j0 = ch * JB;
+    R s[3][JB][2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) { s[a][jj][0] = 0; s[a][jj][1] = 0; }
     const long long qb = ((long long)(k1 * n + k2) * n) * Bp + c;
     for (int k3 = 0; k3 < n; ++k3) {
         const typename V2<R>::t x = Qc[qb + (long long)k3 * Bp];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const R *t = tf + 2 * ((a * n + k3) * nv + j3);
-            s[a][0] += t[0] * x.x - t[1] * x.y;
-            s[a][1] += t[0] * x.y + t[1] * x.x;
-        }
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int jj = 0; jj < JB; ++jj) {
+                if (j0 + jj < nv) {
+                    const R *t = tf + 2 * ((a * n + k3) * nv + j0 + jj);
+                    s[a][jj][0] += t[0] * x.x - t[1] * x.y;
+                    s[a][jj][1] += t[0] * x.y + t[1] * x.x;
+                }
+            }
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        Y[((((long long)a * n + k1) * n + k2) * nv + j3) * Bp + c] = mk2<R>(s[a][0], s[a][1]);
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj)
+            if (j0 + jj < nv)
+                Y[((((long long)a * n + k1) * n + k2) * nv + j0 + jj) * Bp + c] = mk2<R>(s[a][jj][0], s[a][jj][1]);
 }
 
 template <typename R>
 __global__ void k_proj2(const typename V2<R>::t *__restrict__ Y, const R *__restrict__ tf, int n, int nv,
                         int Bp, typename V2<R>::t *__restrict__ Z) {
+    const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long total = (long long)n * nv * nv * Bp;
+    const long long total = (long long)n * nv * nch * Bp;
     if (tid >= total) return;
     const int c = (int)(tid % Bp);
     long long r = tid / Bp;
     const int j3 = (int)(r % nv); r /= nv;
-    const int j2 = (int)(r % nv), k1 = (int)(r / nv);
+    const int ch = (int)(r % nch), k1 = (int)(r / nch);
+    const int j0 = ch * JB;
     // Z[p] with (axis-3 factor, axis-2 factor) = (0,0) (0,1) (0,2) (1,0) (2,0)
-    R s[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    R s[5][JB][2];
+#pragma unroll
+    for (int p = 0; p < 5; ++p)
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) { s[p][jj][0] = 0; s[p][jj][1] = 0; }
     for (int k2 = 0; k2 < n; ++k2) {
         typename V2<R>::t y[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) y[a] = Y[((((long long)a * n + k1) * n + k2) * nv + j3) * Bp + c];
-        const R *t0 = tf + 2 * ((0 * n + k2) * nv + j2);
-        const R *t1 = tf + 2 * ((1 * n + k2) * nv + j2);
-        const R *t2 = tf + 2 * ((2 * n + k2) * nv + j2);
-        s[0][0] += t0[0] * y[0].x - t0[1] * y[0].y; s[0][1] += t0[0] * y[0].y + t0[1] * y[0].x;
-        s[1][0] += t1[0] * y[0].x - t1[1] * y[0].y; s[1][1] += t1[0] * y[0].y + t1[1] * y[0].x;
-        s[2][0] += t2[0] * y[0].x - t2[1] * y[0].y; s[2][1] += t2[0] * y[0].y + t2[1] * y[0].x;
-        s[3][0] += t0[0] * y[1].x - t0[1] * y[1].y; s[3][1] += t0[0] * y[1].y + t0[1] * y[1].x;
-        s[4][0] += t0[0] * y[2].x - t0[1] * y[2].y; s[4][1] += t0[0] * y[2].y + t0[1] * y[2].x;
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) {
+            if (j0 + jj < nv) {
+                const int j2 = j0 + jj;
+                const R *t0 = tf + 2 * ((0 * n + k2) * nv + j2);
+                const R *t1 = tf + 2 * ((1 * n + k2) * nv + j2);
+                const R *t2 = tf + 2 * ((2 * n + k2) * nv + j2);
+                s[0][jj][0] += t0[0] * y[0].x - t0[1] * y[0].y; s[0][jj][1] += t0[0] * y[0].y + t0[1] * y[0].x;
+                s[1][jj][0] += t1[0] * y[0].x - t1[1] * y[0].y; s[1][jj][1] += t1[0] * y[0].y + t1[1] * y[0].x;
+                s[2][jj][0] += t2[0] * y[0].x - t2[1] * y[0].y; s[2][jj][1] += t2[0] * y[0].y + t2[1] * y[0].x;
+                s[3][jj][0] += t0[0] * y[1].x - t0[1] * y[1].y; s[3][jj][1] += t0[0] * y[1].y + t0[1] * y[1].x;
+                s[4][jj][0] += t0[0] * y[2].x - t0[1] * y[2].y; s[4][jj][1] += t0[0] * y[2].y + t0[1] * y[2].x;
+            }
+        }
     }
 #pragma unroll
     for (int p = 0; p < 5; ++p)
-        Z[((((long long)p * n + k1) * nv + j2) * nv + j3) * Bp + c] = mk2<R>(s[p][0], s[p][1]);
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj)
+            if (j0 + jj < nv)
+                Z[((((long long)p * n + k1) * nv + j0 + jj) * nv + j3) * Bp + c] = mk2<R>(s[p][jj][0], s[p][jj][1]);
 }
 
 // Last contraction, the mass-matrix inverse on {phi0, phi6} and the RK4
@@ -321,42 +602,60 @@ template <typename R>
 __global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__restrict__ tf, int n, int nv,
                         int Bp, int B, int c0, const double *__restrict__ U, int ustride, int4 us, int us4,
                         double dt, double kfac, double *__restrict__ dU) {
+    const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nv3 = (long long)nv * nv * nv;
-    if (tid >= nv3 * Bp) return;
+    if (tid >= (long long)nv * nv * nch * Bp) return;
     const int c = (int)(tid % Bp);
     if (c >= B) return;
-    const long long kt = tid / Bp;
-    const int j3 = (int)(kt % nv), j2 = (int)((kt / nv) % nv), j1 = (int)(kt / ((long long)nv * nv));
+    long long r = tid / Bp;
+    const int j3 = (int)(r % nv); r /= nv;
+    const int j2 = (int)(r % nv), ch = (int)(r / nv);
+    const int j0 = ch * JB;
     // l=0: T0 on Z0; l=1: T1 on Z0; l=2: T0 on Z1; l=3: T0 on Z3; l=4: T2 on Z0 + T0 on Z2 + T0 on Z4
-    R a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0;
+    R a[7][JB];
+#pragma unroll
+    for (int e = 0; e < 7; ++e)
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) a[e][jj] = 0;
+    const long long zs = (long long)n * nv * nv * Bp;
     for (int k1 = 0; k1 < n; ++k1) {
-        const R *t0 = tf + 2 * ((0 * n + k1) * nv + j1);
-        const R *t1 = tf + 2 * ((1 * n + k1) * nv + j1);
-        const R *t2 = tf + 2 * ((2 * n + k1) * nv + j1);
         const long long zb = (((long long)k1 * nv + j2) * nv + j3) * Bp + c;
-        const long long zs = (long long)n * nv * nv * Bp;
         const typename V2<R>::t z0 = Z[zb], z1 = Z[zb + zs], z2 = Z[zb + 2 * zs], z3 = Z[zb + 3 * zs], z4 = Z[zb + 4 * zs];
-        a0 += t0[0] * z0.x - t0[1] * z0.y;
-        a1 += t1[0] * z0.x - t1[1] * z0.y;
-        a2 += t0[0] * z1.x - t0[1] * z1.y;
-        a3 += t0[0] * z3.x - t0[1] * z3.y;
-        a4 += t2[0] * z0.x - t2[1] * z0.y;
-        a5 += t0[0] * z2.x - t0[1] * z2.y;
-        a6 += t0[0] * z4.x - t0[1] * z4.y;
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) {
+            if (j0 + jj < nv) {
+                const int j1 = j0 + jj;
+                const R *t0 = tf + 2 * ((0 * n + k1) * nv + j1);
+                const R *t1 = tf + 2 * ((1 * n + k1) * nv + j1);
+                const R *t2 = tf + 2 * ((2 * n + k1) * nv + j1);
+                a[0][jj] += t0[0] * z0.x - t0[1] * z0.y;
+                a[1][jj] += t1[0] * z0.x - t1[1] * z0.y;
+                a[2][jj] += t0[0] * z1.x - t0[1] * z1.y;
+                a[3][jj] += t0[0] * z3.x - t0[1] * z3.y;
+                a[4][jj] += t2[0] * z0.x - t2[1] * z0.y;
+                a[5][jj] += t0[0] * z2.x - t0[1] * z2.y;
+                a[6][jj] += t0[0] * z4.x - t0[1] * z4.y;
+            }
+        }
     }
-    const double tp0 = (double)a0, tp2 = (double)a1, tp3 = (double)a2, tp4 = (double)a3;
-    const double tp5 = (double)a4 + (double)a5 + (double)a6;
-    const double *u = U + (long long)ustride * ((long long)(c0 + c) * nv3 + kt);
-    const double p0 = u[us.x] + u[us4] / 4. + dt * tp0 * kfac;
-    const double p2 = u[us.y] + dt * tp2 * 12. * kfac;
-    const double p3 = u[us.z] + dt * tp3 * 12. * kfac;
-    const double p4 = u[us.w] + dt * tp4 * 12. * kfac;
-    const double p5 = u[us.x] / 4. + u[us4] * 19. / 240. + dt * tp5 * kfac;
-    double *d = dU + 5 * ((long long)c * nv3 + kt);
-    d[0] = 19 * p0 / 4. - 15 * p5;
-    d[4] = 60 * p5 - 15 * p0;
-    d[1] = p2; d[2] = p3; d[3] = p4;
+#pragma unroll
+    for (int jj = 0; jj < JB; ++jj) {
+        if (j0 + jj >= nv) continue;
+        const long long kt = ((long long)(j0 + jj) * nv + j2) * nv + j3;
+        const double tp0 = (double)a[0][jj], tp2 = (double)a[1][jj], tp3 = (double)a[2][jj], tp4 = (double)a[3][jj];
+        const double tp5 = (double)a[4][jj] + (double)a[5][jj] + (double)a[6][jj];
+        const double *u = U + (long long)ustride * ((long long)(c0 + c) * nv3 + kt);
+        const double p0 = u[us.x] + u[us4] / 4. + dt * tp0 * kfac;
+        const double p2 = u[us.y] + dt * tp2 * 12. * kfac;
+        const double p3 = u[us.z] + dt * tp3 * 12. * kfac;
+        const double p4 = u[us.w] + dt * tp4 * 12. * kfac;
+        const double p5 = u[us.x] / 4. + u[us4] * 19. / 240. + dt * tp5 * kfac;
+        double *d = dU + 5 * ((long long)c * nv3 + kt);
+        d[0] = 19 * p0 / 4. - 15 * p5;
+        d[4] = 60 * p5 - 15 * p0;
+        d[1] = p2; d[2] = p3; d[3] = p4;
+    }
 }
 
 // ---------------------------------------------------------------- moments of the increment
@@ -376,8 +675,8 @@ __global__ void k_mom_target(const double2 *__restrict__ q0, const double2 *__re
     for (int pt = p0 + y; pt < p1; pt += 8) {
         const long long o = (long long)pt * Bp + c;
         const double2 a = q0[o], b = q1[o], d = q2[o], e = q3[o];
-        const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) / 6.);
-        const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) / 6.);
+        const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) * (1. / 6.));
+        const double im = nu * (0.5 * a.y + (b.y + d.y + e.y) * (1. / 6.));
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
             const double *g = gmom + 2 * ((long long)m * n3 + pt);
@@ -435,19 +734,26 @@ __global__ void k_mom_actual(const double *__restrict__ dU, const double *__rest
 __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const double *__restrict__ apart,
                              int nrc, const double *__restrict__ gm_inv, double scale, int B, int Bp,
                              double *__restrict__ lam) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
-    double r[5];
-    for (int m = 0; m < 5; ++m) {
-        double tg = 0, ac = 0;
-        for (int k = 0; k < nchunk; ++k) tg += tpart[((long long)k * 5 + m) * Bp + c];
-        for (int k = 0; k < nrc; ++k) ac += apart[((long long)c * nrc + k) * 5 + m];
-        r[m] = scale * tg - ac;
-    }
-    for (int i = 0; i < 5; ++i) {
-        double s = 0;
-        for (int j = 0; j < 5; ++j) s += gm_inv[i * 5 + j] * r[j];
-        lam[5 * c + i] = s;
+    double tg[5] = {0, 0, 0, 0, 0}, ac[5] = {0, 0, 0, 0, 0};
+    for (int k = lane; k < nchunk; k += 32)
+        for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
+    for (int k = lane; k < nrc; k += 32)
+        for (int m = 0; m < 5; ++m) ac[m] += apart[((long long)c * nrc + k) * 5 + m];
+    for (int off = 16; off > 0; off >>= 1)
+        for (int m = 0; m < 5; ++m) {
+            tg[m] += __shfl_down_sync(FULL, tg[m], off);
+            ac[m] += __shfl_down_sync(FULL, ac[m], off);
+        }
+    if (lane == 0) {
+        double r[5];
+        for (int m = 0; m < 5; ++m) r[m] = scale * tg[m] - ac[m];
+        for (int i = 0; i < 5; ++i) {
+            double sum = 0;
+            for (int j = 0; j < 5; ++j) sum += gm_inv[i * 5 + j] * r[j];
+            lam[5 * c + i] = sum;
+        }
     }
 }
 
@@ -479,25 +785,35 @@ __global__ void k_scatter(const double *__restrict__ dU, long long nrec, long lo
 }
 
 // ---------------------------------------------------------------- Poisson
-// Charge moments per spatial cell: scalev sum (U0 + U6/4), U1, U2.
+// Charge moments per spatial cell: the sums over the cell's
+// records of scalev (U0 + U6/4), scalev U1 and scalev U2.  The right-hand
+// side of the Poisson problem is the small difference rho - 1, so the
+// summation order matters at the 1e-12 level; the terms are staged in shared
+// memory and each moment is accumulated by one thread in the reference's
+// record order, without FMA, which gives the reference's sums bit for bit.
+constexpr int kChargeChunk = 2048;
 __global__ void k_charge(const double *__restrict__ U, int nv3, double scalev, double *__restrict__ rt) {
-    __shared__ double red[3][256];
+    __shared__ double term[3][kChargeChunk];
     const int s = blockIdx.x, t = threadIdx.x;
-    double r0 = 0, r1 = 0, r2 = 0;
     const double *base = U + 7 * (long long)s * nv3;
-    for (int j = t; j < nv3; j += 256) {
-        const double *u = base + 7 * (long long)j;
-        r0 += scalev * (u[0] + 0.25 * u[6]);
-        r1 += scalev * u[1];
-        r2 += scalev * u[2];
-    }
-    red[0][t] = r0; red[1][t] = r1; red[2][t] = r2;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) { red[0][t] += red[0][t + w]; red[1][t] += red[1][t + w]; red[2][t] += red[2][t + w]; }
+    double acc = 0.0;
+    for (int c0 = 0; c0 < nv3; c0 += kChargeChunk) {
+        const int len = min(kChargeChunk, nv3 - c0);
+        for (int j = t; j < len; j += blockDim.x) {
+            const double *u = base + 7 * (long long)(c0 + j);
+            term[0][j] = __dmul_rn(scalev, __dadd_rn(u[0], __dmul_rn(0.25, u[6])));
+            term[1][j] = __dmul_rn(scalev, u[1]);
+            term[2][j] = __dmul_rn(scalev, u[2]);
+        }
+        __syncthreads();
+        if (t < 3) {
+            const double *tt = term[t];
+#pragma unroll 8
+            for (int j = 0; j < len; ++j) acc = __dadd_rn(acc, tt[j]);
+        }
         __syncthreads();
     }
-    if (t == 0) { rt[3 * s] = red[0][0]; rt[3 * s + 1] = red[1][0]; rt[3 * s + 2] = red[2][0]; }
+    if (t < 3) rt[3 * s + t] = acc;
 }
 
 // pois2d in one block: right-hand side, the band solve of DGBTRS
@@ -738,6 +1054,35 @@ __global__ void k_flux(AdvectDev ad, const double *__restrict__ U0, const double
     }
 }
 
+// ---------------------------------------------------------------- FMA peaks
+// Eight independent dependent chains per thread of packed FP32x2 FMAs (two
+// FMAs each) or of FP64 FMAs; the result is written so nothing is elided.
+__global__ void k_fma_f32(int iters, double *sink) {
+    unsigned long long a[8], b = pk2(1.0000001f, 0.9999999f), c = pk2(1e-7f, -1e-7f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = pk2((float)threadIdx.x + q, (float)blockIdx.x);
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = fma2(a[q], b, c);
+    float sum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { const float2 v = up2(a[q]); sum += v.x + v.y; }
+    if (sum == 1234.5f) sink[0] = sum;
+}
+__global__ void k_fma_f64(int iters, double *sink) {
+    double a[8];
+    const double b = 1.0000000001, c = 1e-12;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = threadIdx.x + q + blockIdx.x;
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = fma(a[q], b, c);
+    double sum = 0.;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sum += a[q];
+    if (sum == 1234.5) sink[0] = sum;
+}
+
 // ---------------------------------------------------------------- moments
 __global__ void k_moments(const double *__restrict__ U, long long size, long long kend, int nv, double lv,
                           double dv, double *__restrict__ part) {
@@ -836,10 +1181,77 @@ cudaError_t launch_computeq(const typename V2<R>::t *F, const R *P, const unsign
     return cudaGetLastError();
 }
 
+bool lines_supported(int n) { return n == 8 || n == 16 || n == 24 || n == 32; }
+
+namespace {
+template <int N> long long lines_offsets(std::vector<long long> &line_off) {
+    constexpr int KT = LinesCfg<N>::KT, h = N / 2, TP = pp_floats<N, KT>();
+    line_off.assign((size_t)N * N + 1, 0);
+    for (int ij = 0; ij < N * N; ++ij) {
+        const int i = ij / N, j = ij % N;
+        const int ni = i < h ? i + h + 1 : 3 * h - 1 - i, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+        line_off[ij + 1] = line_off[ij] + (long long)((ni * nj + 1) / 2) * TP;
+    }
+    return line_off[(size_t)N * N];
+}
+}  // namespace
+
+long long lines_table_floats(int n, std::vector<long long> &line_off) {
+    switch (n) {
+    case 8: return lines_offsets<8>(line_off);
+    case 16: return lines_offsets<16>(line_off);
+    case 24: return lines_offsets<24>(line_off);
+    case 32: return lines_offsets<32>(line_off);
+    default: return 0;
+    }
+}
+
+cudaError_t launch_lines_table(const double *eta, const double *shat, const double *ahat, const unsigned char *rzero,
+                               const double *cw, const long long *line_off, int n, float *W, cudaStream_t st) {
+    switch (n) {
+    case 8: k_lines_table<8><<<64, 256, 0, st>>>(eta, shat, ahat, rzero, cw, line_off, W); break;
+    case 16: k_lines_table<16><<<256, 256, 0, st>>>(eta, shat, ahat, rzero, cw, line_off, W); break;
+    case 24: k_lines_table<24><<<576, 256, 0, st>>>(eta, shat, ahat, rzero, cw, line_off, W); break;
+    case 32: k_lines_table<32><<<1024, 256, 0, st>>>(eta, shat, ahat, rzero, cw, line_off, W); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+namespace {
+template <int N, int T>
+void launch_tiles(const float2 *F, const float *W, const long long *line_off, int Bp, double2 *q, cudaStream_t st) {
+    constexpr int NT = N / LinesCfg<N>::KT;
+    if constexpr (T < NT) {
+        const unsigned blocks = (unsigned)((long long)N * N * (Bp / 32));
+        constexpr size_t smem = lines_smem_bytes<N, T>();
+        static bool attr_set = false;  // one attribute call per instantiation
+        if (!attr_set) {
+            cudaFuncSetAttribute(k_cq_lines<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr_set = true;
+        }
+        k_cq_lines<N, T><<<blocks, 32 * kLineWarps, smem, st>>>(F, W, line_off, Bp, q);
+        launch_tiles<N, T + 1>(F, W, line_off, Bp, q, st);
+    }
+}
+}  // namespace
+
+cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n, int Bp,
+                                  double2 *q, cudaStream_t st) {
+    switch (n) {
+    case 8: launch_tiles<8, 0>(F, W, line_off, Bp, q, st); break;
+    case 16: launch_tiles<16, 0>(F, W, line_off, Bp, q, st); break;
+    case 24: launch_tiles<24, 0>(F, W, line_off, Bp, q, st); break;
+    case 32: launch_tiles<32, 0>(F, W, line_off, Bp, q, st); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
                             double *part, int nchunk, double *lam, cudaStream_t st) {
     k_cons_partial<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
-    k_cons_lambda<<<(Bp + 127) / 128, 128, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    k_cons_lambda<<<(Bp + 3) / 4, 128, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
     return cudaGetLastError();
 }
@@ -852,11 +1264,13 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
                            cudaStream_t st) {
     const long long n3 = (long long)n * n * n, nv3 = (long long)nv * nv * nv;
     k_qcomb<R><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Qc);
-    k_proj3<R><<<grid1((long long)n * n * nv * Bp, 256), 256, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
-    k_proj2<R><<<grid1((long long)n * nv * nv * Bp, 256), 256, 0, st>>>(Y, tfac, n, nv, Bp, Z);
+    const int nch = (nv + JB - 1) / JB;
+    k_proj3<R><<<grid1((long long)n * n * nch * Bp, 128), 128, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
+    k_proj2<R><<<grid1((long long)n * nv * nch * Bp, 128), 128, 0, st>>>(Y, tfac, n, nv, Bp, Z);
     const double kfac = 1. / scalev / scaleL / scale3;
     int4 us = make_int4(uslot[0], uslot[1], uslot[2], uslot[3]);
-    k_proj1<R><<<grid1(nv3 * Bp, 256), 256, 0, st>>>(Z, tfac, n, nv, Bp, B, c0, U, ustride, us, uslot[4], dt, kfac, dU);
+    k_proj1<R><<<grid1((long long)nv * nv * nch * Bp, 128), 128, 0, st>>>(Z, tfac, n, nv, Bp, B, c0, U, ustride, us,
+                                                                             uslot[4], dt, kfac, dU);
     return cudaGetLastError();
 }
 
@@ -867,7 +1281,7 @@ cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double
                               cudaStream_t st) {
     k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, gmom, n3, Bp, nchunk, tpart);
     k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, c0, nrc, apart);
-    k_mom_lambda<<<(B + 127) / 128, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, B, Bp, lam);
+    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, B, Bp, lam);
     const long long nrec = (long long)B * nv * nv * nv;
     k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, nrec);
     return cudaGetLastError();
@@ -898,6 +1312,12 @@ cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, double *b, do
 cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const double *fields,
                               int stage, double *Uout, cudaStream_t st) {
     k_flux<<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, fields, stage, Uout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fma_peak(bool fp64, int blocks, int iters, double *sink, cudaStream_t st) {
+    if (fp64) k_fma_f64<<<blocks, 256, 0, st>>>(iters, sink);
+    else k_fma_f32<<<blocks, 256, 0, st>>>(iters, sink);
     return cudaGetLastError();
 }
 

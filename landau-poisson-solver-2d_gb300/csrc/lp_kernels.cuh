@@ -8,6 +8,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace lp {
 
 template <typename R> struct V2;
@@ -55,6 +57,19 @@ cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t
 template <typename R>
 cudaError_t launch_computeq(const typename V2<R>::t *F, const R *P, const unsigned *PI,
                             const int *pair_off, int n3, int Bp, double2 *q, cudaStream_t st);
+
+// Line-tiled FP32 contraction (mixed path, n in {8, 16, 24, 32}): one warp
+// per (output line (i, j), k-tile, 32 cells); the symmetric plane pairs
+// {(l, m), (i+n/2-l, j+n/2-m)} of the window keep both F lines in registers
+// and every term A(k') B(k+n/2-k') takes one combined weight.  Per-plane
+// partial sums are added to a Kahan-compensated FP32 accumulator.
+bool lines_supported(int n);
+long long lines_table_floats(int n, std::vector<long long> &line_off);
+cudaError_t launch_lines_table(const double *eta, const double *shat, const double *ahat,
+                               const unsigned char *rzero, const double *cw, const long long *line_off,
+                               int n, float *W, cudaStream_t st);
+cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n,
+                                  int Bp, double2 *q, cudaStream_t st);
 
 // Moment-conserving projection of q in place (FP64).
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
@@ -105,6 +120,9 @@ struct AdvectDev {
 // One SSP-RK3 stage: Uout = combination(U0, Us, H(Us)).
 cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us,
                               const double *fields, int stage, double *Uout, cudaStream_t st);
+
+// FMA-throughput microbenchmarks (FP32 packed f32x2 and FP64).
+cudaError_t launch_fma_peak(bool fp64, int blocks, int iters, double *sink, cudaStream_t st);
 
 // Block partial sums of the moments (mass, p1, p2, p3, kinetic energy).
 cudaError_t launch_moments(const double *U, long long size, long long kend, int nv, double lv,

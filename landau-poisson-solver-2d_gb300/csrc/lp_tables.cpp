@@ -449,7 +449,7 @@ lp_status build_tables(const lp_params &p, Tables &t, std::string &err) {
         int j = (int)((l * t.h_v) / t.dv);
         if (j == nv) j = nv - 1;
         t.nodecell[l] = j;
-        t.nodeoff[l] = t.v[l] - (-p.lv + ((double)j + 0.5) * t.dv);
+        t.nodeoff[l] = (t.v[l] - (-p.lv + ((double)j + 0.5) * t.dv)) / t.dv;
     }
 
     // Per-axis factors of IntModes (C:364-505).

@@ -40,7 +40,7 @@ struct Tables {
     std::vector<double> c1, c2;  // 5 x n3
     double cct_inv[25] = {0};
     std::vector<int> nodecell;   // n
-    std::vector<double> nodeoff; // n: v[l] - Gridv(nodecell[l])
+    std::vector<double> nodeoff; // n: (v[l] - Gridv(nodecell[l])) / dv
     std::vector<double> tfac;    // 3 x n x nv complex (T0, T1, T2)
     std::vector<double> mfwd;    // n x n complex, out index major
     std::vector<double> minv;    // n x n complex, out index major

@@ -32,8 +32,9 @@ EXPORTS = [
     "lp_ctx_create", "lp_ctx_destroy", "lp_set_stream", "lp_synchronize", "lp_last_error",
     "lp_device_bytes", "lp_set_state", "lp_get_state", "lp_state_device_ptr", "lp_set_init",
     "lp_fft3d", "lp_fs", "lp_compute_q", "lp_conserve", "lp_rk4_cell", "lp_nodes",
-    "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_advect_step",
-    "lp_collision_step", "lp_step", "lp_moments", "lp_conserve_noalloc",
+    "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_last_fields", "lp_advect_step",
+    "lp_collision_step", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
+    "lp_conserve_noalloc",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -110,10 +111,13 @@ def lib():
         L.lp_weights_rows.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
         L.lp_conservation_rows.argtypes = [_vp, _dp, _dp, _dp]
         L.lp_poisson.argtypes = [_vp, _dp, _dp, _dp, _dp]
+        L.lp_last_fields.argtypes = [_vp, _dp, _dp, _dp, _dp]
         L.lp_advect_step.argtypes = [_vp]
         L.lp_collision_step.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
         L.lp_step.argtypes = [_vp, ctypes.c_int]
         L.lp_moments.argtypes = [_vp, _dp]
+        L.lp_time_kernel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
+        L.lp_measure_fp_peaks.argtypes = [_dp, _dp]
         L.lp_conserve_noalloc.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         for name in EXPORTS:
             f = getattr(L, name)
@@ -128,6 +132,15 @@ def _p(a):
         return None
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(_dp)
+
+
+def measure_fp_peaks():
+    """(FP32, FP64) dense FMA throughput of the current device in TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    st = lib().lp_measure_fp_peaks(ctypes.byref(a), ctypes.byref(b))
+    if st != OK:
+        raise LPError(st, "lp_measure_fp_peaks failed")
+    return a.value, b.value
 
 
 class Context:
@@ -238,6 +251,12 @@ class Context:
         self._chk(self.L.lp_poisson(self.h, _p(potc), _p(px), _p(py), _p(fl)))
         return potc, px, py, fl.reshape(14, nc)
 
+    def last_fields(self):
+        nc = self.params.ncell
+        potc, px, py, fl = np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(14 * nc)
+        self._chk(self.L.lp_last_fields(self.h, _p(potc), _p(px), _p(py), _p(fl)))
+        return potc, px, py, fl.reshape(14, nc)
+
     def advect_step(self):
         self._chk(self.L.lp_advect_step(self.h))
 
@@ -246,6 +265,13 @@ class Context:
 
     def step(self, nsteps=1):
         self._chk(self.L.lp_step(self.h, int(nsteps)))
+
+    def time_kernel(self, which=0, reps=10):
+        """Average ms per launch of a stage (0 contraction, 1 forward transform,
+        2 conservation, 3 DG projection), CUDA events on the context's stream."""
+        ms = ctypes.c_double()
+        self._chk(self.L.lp_time_kernel(self.h, int(which), int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def moments(self):
         out = np.zeros(6)

@@ -359,6 +359,51 @@ void lpo_intmodes(const lpo_ctx *c, int k1, int k2, int k3, int j1, int j2, int 
     r[9] = p1i + p2i + p3i;
 }
 
+/* IntModes evaluated from scratch for every (mode, v-cell) pair, computing
+ * the sines and cosines of each axis factor on every call as the reference
+ * does (C:364-505); same values as lpo_intmodes, at the reference's cost. */
+static void axis_factors(const lpo_ctx *c, int k, int j, double *t0, double *t1, double *t2)
+{
+    const double e = c->eta[k], dv = c->dv;
+    const double gp = gridv(c, j + 0.5), gm = gridv(c, j - 0.5), gj = gridv(c, (double)j);
+    if (e != 0.) {
+        t0[0] = (sin(e * gp) - sin(e * gm)) / e;
+        t0[1] = (cos(e * gm) - cos(e * gp)) / e;
+        t1[0] = ((gp * sin(e * gp) - gm * sin(e * gm)) / e + (cos(e * gp) - cos(e * gm)) / e / e - gj * t0[0]) / dv;
+        t1[1] = ((sin(e * gp) - sin(e * gm)) / e / e + (gm * cos(e * gm) - gp * cos(e * gp)) / e - gj * t0[1]) / dv;
+        double ar = (gp * sin(e * gp) - gm * sin(e * gm)) / e + (cos(e * gp) - cos(e * gm)) / e / e;
+        double ai = (sin(e * gp) - sin(e * gm)) / e / e + (gm * cos(e * gm) - gp * cos(e * gp)) / e;
+        t2[0] = ((gp * gp * sin(e * gp) - gm * gm * sin(e * gm) - 2 * ai) / e - 2 * gj * ar + gj * gj * t0[0]) / dv / dv;
+        t2[1] = ((gm * gm * cos(e * gm) - gp * gp * cos(e * gp) + 2 * ar) / e - 2 * gj * ai + gj * gj * t0[1]) / dv / dv;
+    } else {
+        t0[0] = dv; t0[1] = 0.; t1[0] = 0.; t1[1] = 0.; t2[0] = dv / 12.; t2[1] = 0.;
+    }
+}
+
+static void intmodes_trig(const lpo_ctx *c, int k1, int k2, int k3, int j1, int j2, int j3, double *r)
+{
+    double a1[2], a2[2], a3[2], b1[2], b2[2], b3[2], d1[2], d2[2], d3[2];
+    axis_factors(c, k1, j1, a1, b1, d1);
+    axis_factors(c, k2, j2, a2, b2, d2);
+    axis_factors(c, k3, j3, a3, b3, d3);
+    r[0] = a3[0] * (a1[0] * a2[0] - a1[1] * a2[1]) - a3[1] * (a1[0] * a2[1] + a2[0] * a1[1]);
+    r[1] = a3[0] * (a1[0] * a2[1] + a2[0] * a1[1]) + a3[1] * (a1[0] * a2[0] - a1[1] * a2[1]);
+    r[2] = a3[0] * (b1[0] * a2[0] - b1[1] * a2[1]) - a3[1] * (b1[0] * a2[1] + a2[0] * b1[1]);
+    r[3] = a3[0] * (b1[0] * a2[1] + a2[0] * b1[1]) + a3[1] * (b1[0] * a2[0] - b1[1] * a2[1]);
+    r[4] = a3[0] * (a1[0] * b2[0] - a1[1] * b2[1]) - a3[1] * (a1[0] * b2[1] + b2[0] * a1[1]);
+    r[5] = a3[0] * (a1[0] * b2[1] + b2[0] * a1[1]) + a3[1] * (a1[0] * b2[0] - a1[1] * b2[1]);
+    r[6] = b3[0] * (a1[0] * a2[0] - a1[1] * a2[1]) - b3[1] * (a1[0] * a2[1] + a2[0] * a1[1]);
+    r[7] = b3[0] * (a1[0] * a2[1] + a2[0] * a1[1]) + b3[1] * (a1[0] * a2[0] - a1[1] * a2[1]);
+    double p1r = a3[0] * (d1[0] * a2[0] - d1[1] * a2[1]) - a3[1] * (d1[0] * a2[1] + a2[0] * d1[1]);
+    double p1i = a3[0] * (d1[0] * a2[1] + a2[0] * d1[1]) + a3[1] * (d1[0] * a2[0] - d1[1] * a2[1]);
+    double p2r = a3[0] * (a1[0] * d2[0] - a1[1] * d2[1]) - a3[1] * (a1[0] * d2[1] + d2[0] * a1[1]);
+    double p2i = a3[0] * (a1[0] * d2[1] + d2[0] * a1[1]) + a3[1] * (a1[0] * d2[0] - a1[1] * d2[1]);
+    double p3r = d3[0] * (a1[0] * a2[0] - a1[1] * a2[1]) - d3[1] * (a1[0] * a2[1] + a2[0] * a1[1]);
+    double p3i = d3[0] * (a1[0] * a2[1] + a2[0] * a1[1]) + d3[1] * (a1[0] * a2[0] - a1[1] * a2[1]);
+    r[8] = p1r + p2r + p3r;
+    r[9] = p1i + p2i + p3i;
+}
+
 /* Separable evaluation of tp_l(j) = Re sum_k IntM_l(k, j) Qc(k): three
  * successive per-axis contractions of the complex mode array Qc. */
 static void project_separable(const lpo_ctx *c, const double *qc, double *tp /* nv3 x 5 */)
@@ -467,7 +512,8 @@ static void rk4_impl(const lpo_ctx *c, const double *f, const double *qhat, cons
                 for (int j = 0; j < n; ++j)
                     for (int k = 0; k < n; ++k) {
                         long ke = k + n * (j + (long)n * i);
-                        lpo_intmodes(c, i, j, k, j1, j2, j3, im);
+                        if (direct == 2) intmodes_trig(c, i, j, k, j1, j2, j3, im);
+                        else lpo_intmodes(c, i, j, k, j1, j2, j3, im);
                         double qr = qc[2 * ke], qi = qc[2 * ke + 1];
                         for (int l = 0; l < 5; ++l) a[l] += im[2 * l] * qr - im[2 * l + 1] * qi;
                     }

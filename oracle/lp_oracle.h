@@ -48,7 +48,9 @@ void lpo_conserve(const lpo_ctx *c, double *qhat);
 void lpo_intmodes(const lpo_ctx *c, int k1, int k2, int k3, int j1, int j2, int j3, double *out10);
 /* RK4 of one spatial cell: f (n^3 node values), conserved qhat, the cell's
  * nv^3*7 state and its nv^3*5 output.  direct=1 sums IntModes over every
- * (mode, v-cell) pair as the reference does; direct=0 uses the separable form. */
+ * (mode, v-cell) pair from precomputed axis factors; direct=2 recomputes the
+ * factors' sines and cosines on every call as the reference does (its cost);
+ * direct=0 uses the separable form. */
 void lpo_rk4(const lpo_ctx *c, const double *f, const double *qhat, const double *ucell,
              double *du, int direct);
 void lpo_nodes(const lpo_ctx *c, const double *U, int cell, double *f);
