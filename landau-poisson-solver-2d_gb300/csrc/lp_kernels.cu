@@ -270,28 +270,30 @@ __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_g
 
 // One k-tile of output lines.  The kLineWarps warps of a block take the
 // plane pairs of the same (line, tile, 32 cells) in turn; each warp stages
-// the next plane pair's two F lines in shared memory with cp.async (double
-// buffered, every lane copying its own cell) together with the plane pair's
-// weights, while it computes the current one from registers.  Per plane pair, with a = A(k'), b = B(k+h-k') and
+// the plane pair's two F lines in shared memory with cp.async (one buffer:
+// every lane copies and reads only its own cell's column, and the copy of
+// the next plane pair is issued when the current one has been consumed, its
+// latency hidden by the other resident warps) and its weights (double
+// buffered: the next plane pair's weights are copied during the computation).  Per plane pair, with a = A(k'), b = B(k+h-k') and
 // weight w: U += (w a) (bx, by) and V += (w a) (by, bx) in packed FP32x2, so
 // Re = U.x - U.y, Im = V.x + V.y; each plane's partials enter a
 // Kahan-compensated FP32 accumulator, and the warps' results are summed in
 // FP64 in a fixed order.
 template <int N, int TILE>
-__global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
+__global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
                                                             const long long *__restrict__ line_off, int Bp,
                                                             double2 *__restrict__ q) {
     constexpr int KT = LinesCfg<N>::KT, h = N / 2, K0 = TILE * KT;
     constexpr int TP = pp_floats<N, KT>(), TOFF = tile_off<N, KT>(TILE);
     constexpr int TT = tile_floats<N>(K0, K0 + KT);  // weight floats of this tile per plane pair
     extern __shared__ __align__(16) unsigned char lines_smem[];
-    // per warp: [2 buffers][2 lines][N][32 lanes] float2; then per warp
-    // [2 buffers][TT] weights; then the reduction area
+    // per warp: [2 lines][N][32 lanes] float2; then per warp [2 buffers][TT]
+    // weights; the reduction area reuses the space after the loop
     float2 *stage = reinterpret_cast<float2 *>(lines_smem);
-    float *wstage = reinterpret_cast<float *>(lines_smem + sizeof(float2) * 4 * N * 32 * kLineWarps);
+    float *wstage = reinterpret_cast<float *>(lines_smem + sizeof(float2) * 2 * N * 32 * kLineWarps);
     double2 *red = reinterpret_cast<double2 *>(lines_smem);  // reuses the staging area after the loop
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2 *mybuf = stage + (long long)warp * 4 * N * 32;
+    float2 *mybuf = stage + (long long)warp * 2 * N * 32;
     float *mywbuf = wstage + warp * 2 * TT;
     const int G = Bp / 32;
     const int g = (int)(blockIdx.x % G), ij = (int)(blockIdx.x / G);
@@ -301,18 +303,20 @@ __global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__re
     const int npp = (ni * nj + 1) / 2;
     const int c = g * 32 + lane;
     const float *wbase = W + line_off[ij] + TOFF;
-    auto stage_pp = [&](int pp, int buf) {
+    auto stage_lines = [&](int pp) {
         const int l = si + pp / nj, m = sj + pp % nj;
         const int x = i + h - l, y = j + h - m;
         const float2 *Al = F + (long long)((l * N + m) * N) * Bp + c;
         const float2 *Bl = F + (long long)((x * N + y) * N) * Bp + c;
-        float2 *dA = mybuf + (buf * 2 + 0) * N * 32 + lane;
-        float2 *dB = mybuf + (buf * 2 + 1) * N * 32 + lane;
-#pragma unroll
+        float2 *dA = mybuf + lane;
+        float2 *dB = mybuf + N * 32 + lane;
+#pragma unroll 4
         for (int n = 0; n < N; ++n) {
             cp_async8(dA + n * 32, Al + (long long)n * Bp);
             cp_async8(dB + n * 32, Bl + (long long)n * Bp);
         }
+    };
+    auto stage_w = [&](int pp, int buf) {
         const float *ws = wbase + (long long)pp * TP;
         float *wd = mywbuf + buf * TT;
         for (int q4 = lane; q4 < TT / 4; q4 += 32) cp_async16(wd + 4 * q4, ws + 4 * q4);
@@ -321,17 +325,22 @@ __global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__re
     unsigned long long U[KT], V[KT];
 #pragma unroll
     for (int kk = 0; kk < KT; ++kk) { sr[kk] = 0.f; sim[kk] = 0.f; cr[kk] = 0.f; ci[kk] = 0.f; U[kk] = 0ull; V[kk] = 0ull; }
-    if (warp < npp) stage_pp(warp, 0);
+    if (warp < npp) {
+        stage_lines(warp);
+        stage_w(warp, 0);
+    }
     cp_async_commit();
     int it = 0;
     for (int pp = warp; pp < npp; pp += kLineWarps, ++it) {
         const int nxt = pp + kLineWarps;
-        if (nxt < npp) stage_pp(nxt, (it + 1) & 1);
-        cp_async_commit();
-        cp_async_wait1();
+        cp_async_wait0();
         __syncwarp();
-        const float2 *sA = mybuf + ((it & 1) * 2 + 0) * N * 32 + lane;
-        const float2 *sB = mybuf + ((it & 1) * 2 + 1) * N * 32 + lane;
+        // (issued before the line reads: the copy instructions order the
+        // compiler's memory accesses, and the reads should sink to their uses)
+        if (nxt < npp) stage_w(nxt, (it + 1) & 1);
+        cp_async_commit();
+        const float2 *sA = mybuf + lane;
+        const float2 *sB = mybuf + N * 32 + lane;
         const float *wp = mywbuf + (it & 1) * TT;
         unsigned long long A[N], B[N], Bs[N];
 #pragma unroll
@@ -367,7 +376,9 @@ __global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__re
             ci[kk] = (ti - sim[kk]) - yi; sim[kk] = ti;
         }
         }
-        __syncwarp();
+        __syncwarp();  // every lane is done with this plane pair's lines and weights
+        if (nxt < npp) stage_lines(nxt);
+        cp_async_commit();
     }
     cp_async_wait0();
     __syncthreads();
@@ -388,7 +399,7 @@ __global__ void __launch_bounds__(32 * kLineWarps) k_cq_lines(const float2 *__re
 
 template <int N, int T> constexpr size_t lines_smem_bytes() {
     constexpr int KT = LinesCfg<N>::KT;
-    constexpr size_t staging = sizeof(float2) * 4 * N * 32 * kLineWarps +
+    constexpr size_t staging = sizeof(float2) * 2 * N * 32 * kLineWarps +
                                sizeof(float) * 2 * tile_floats<N>(T * KT, T * KT + KT) * kLineWarps;
     constexpr size_t reduction = sizeof(double2) * kLineWarps * KT * 32;
     return staging > reduction ? staging : reduction;
