@@ -157,6 +157,120 @@ def run_reference(args):
     return 0
 
 
+def batch_runs(seed=20261203, count=64):
+    """64 independent runs drawn from a seed: Nx uniform in {16, 32, 64, 128},
+    N = Nv uniform in {16, 24, 32}, A log-uniform in [1e-3, 0.5], k uniform in
+    [0.3, 0.6], nu log-uniform in [1e-3, 1e-1]; v in [-5.25, 5.25]^3, perturbed
+    unit Maxwellian; dt = min(0.01, 0.25 dx / 5.25), inside the SSP-RK3 / P1
+    upwind stability bound of every run (dt = 0.01 is not, for the finest
+    grids: Nx = 128 at k = 0.6 gives a Courant number of 0.64)."""
+    rng = np.random.default_rng(seed)
+    runs = []
+    for _ in range(count):
+        nx = int(rng.choice([16, 32, 64, 128]))
+        nn = int(rng.choice([16, 24, 32]))
+        a = float(np.exp(rng.uniform(np.log(1e-3), np.log(0.5))))
+        k = float(rng.uniform(0.3, 0.6))
+        nu = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-1))))
+        lx = 2 * np.pi / k
+        dt = min(0.01, 0.25 * (lx / nx) / 5.25)
+        runs.append(dict(nx1=nx, nx2=1, nv=nn, n=nn, lv=5.25, lx=lx, nu=nu, dt=dt, a_amp=a, k_wave=k))
+    return runs
+
+
+TWOSTREAM = dict(nx1=256, nx2=1, nv=32, n=32, lv=8.0, lx=2 * np.pi / 0.3, nu=0.01, dt=0.0025,
+                 a_amp=0.01, k_wave=0.3)
+
+
+def run_workload(args):
+    """Secondary workloads, one JSON line each: `batch` (64 seeded uneven runs
+    in one batch, full time steps from the batch's per-step graph, schedules
+    picked by the autotuner) and `twostream` (the large two-stream instance,
+    Nx = 256, N = Nv = 32, full time steps, plus its error against FP64)."""
+    import torch
+    import lp_gb300 as lp
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    prec = lp.PREC_MIXED if args.precision == "mixed" else lp.PREC_FP64
+
+    def timed(fn, k, w):
+        with torch.cuda.stream(stream):
+            for _ in range(w):
+                fn()
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(k)]
+            for i in range(k):
+                flush.zero_()
+                ev[i][0].record(stream)
+                fn()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+    extra = {}
+    if args.workload == "batch":
+        specs = batch_runs()
+        b = lp.Batch([lp.Params(**r, fixes=lp.FIX_DEFAULT, precision=prec) for r in specs])
+        b.set_stream(stream.cuda_stream)
+        for i in range(len(specs)):
+            b.set_init(i, 1)
+        t0 = time.perf_counter()
+        b.autotune(reps=2)
+        extra["autotune_s"] = time.perf_counter() - t0
+        extra["classes"] = [dict(zip(["n", "nv", "runs", "cells", "cells_per_pass", "line_warps",
+                                      "collision_ms"], c)) for c in b.classes()]
+        cells = sum(r["nx1"] * r["nx2"] for r in specs)
+        with ClockSampler(0) as clk:
+            t = timed(lambda: b.step(1), args.steps, args.warmup)
+        m = [b.moments(i) for i in range(len(specs))]
+        extra["finite"] = bool(all(np.all(np.isfinite(x)) for x in m))
+        cfg = {"workload": "64 seeded uneven runs (Nx in {16,32,64,128}, N=Nv in {16,24,32}, "
+                           "A, k, nu drawn), one full time step of every run per step",
+               "seed": 20261203, "runs": len(specs), "cells_per_step": cells,
+               "l2": "flushed between timed steps (512 MiB write)", "precision": args.precision}
+        metric, unit = "batched full-step cell-steps/s", "cell-steps/s"
+    else:
+        P = lp.Params(**TWOSTREAM, fixes=lp.FIX_DEFAULT, precision=prec)
+        ctx = lp.Context(P)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_init(2, 2.0)
+        cells = TWOSTREAM["nx1"]
+        with ClockSampler(0) as clk:
+            t = timed(lambda: ctx.step(1), args.steps, args.warmup)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            extra["contraction_ms"] = ctx.time_kernel(0, reps=3)
+        if prec == lp.PREC_MIXED and args.fp64_steps > 0:
+            ref = lp.Context(lp.Params(**TWOSTREAM, fixes=lp.FIX_DEFAULT, precision=lp.PREC_FP64))
+            mix = lp.Context(P)
+            ref.set_init(2, 2.0)
+            mix.set_init(2, 2.0)
+            m0 = mix.moments()
+            ref.step(args.fp64_steps)
+            mix.step(args.fp64_steps)
+            Ur, Um = ref.get_state(), mix.get_state()
+            extra["rel_err_vs_fp64"] = float(np.linalg.norm(Um - Ur) / np.linalg.norm(Ur))
+            extra["err_steps"] = args.fp64_steps
+            m1 = mix.moments()
+            extra["mass_drift"] = float(abs(m1[0] - m0[0]) / abs(m0[0]))
+        cfg = {"workload": "two-stream, Nx=256 (1-D), N=Nv=32, v in [-8,8]^3, u=2, A=0.01, k=0.3, "
+                           "nu=0.01, dt=0.0025; one full time step per step",
+               "cells_per_step": cells, "l2": "flushed between timed steps (512 MiB write)",
+               "precision": args.precision}
+        metric, unit = "full-step cell-steps/s", "cell-steps/s"
+    line = {"metric": metric, "value": cells * args.steps / t, "unit": unit, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded analytic initial states)", "config": cfg,
+            "clocks": clk.summary()}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,9 +280,12 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="landau64", choices=["landau64", "batch", "twostream"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "landau64":
+        return run_workload(args)
 
     import torch
     import lp_gb300 as lp

@@ -147,6 +147,47 @@ lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
  * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */
 lp_status lp_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
 
+/* ---- batches of independent runs ---------------------------------------- */
+/* No counterpart in the reference, which runs one instance per job.  A batch
+ * steps `count` independent runs, each with its own lp_params (grid nx1 x nx2,
+ * nv, n, lv, lx, nu, dt, initial-condition parameters); fixes and precision
+ * must agree across runs and include LP_FIX_F1 (collisions run in passes of
+ * cells), and 2-D runs need LP_FIX_F3.  Runs with equal (n, nv, lv) form a
+ * class: their spatial cells go through one set of collision launches with
+ * per-cell nu and dt, over one shared weight table.  Every run is advected on
+ * its own stream and every class collided on its own stream; lp_batch_step
+ * replays one captured CUDA graph per time step.  A run whose nu is 0 still
+ * passes through its class's collision launches (an increment of zero). */
+typedef struct lp_batch lp_batch;
+lp_status lp_batch_create(const lp_params *params, int count, lp_batch **out);
+lp_status lp_batch_destroy(lp_batch *b);
+lp_status lp_batch_set_stream(lp_batch *b, void *cuda_stream);
+lp_status lp_batch_synchronize(lp_batch *b);
+const char *lp_batch_last_error(const lp_batch *b);
+size_t lp_batch_device_bytes(const lp_batch *b);
+/* State of run `run` (its nx1*nx2*nv^3*7 doubles), as lp_set_state etc. */
+lp_status lp_batch_set_state(lp_batch *b, int run, const double *U_host, size_t n);
+lp_status lp_batch_get_state(lp_batch *b, int run, double *U_host, size_t n);
+lp_status lp_batch_set_init(lp_batch *b, int run, int kind, double u);
+lp_status lp_batch_moments(lp_batch *b, int run, double *out6);
+lp_status lp_batch_advect_step(lp_batch *b);
+lp_status lp_batch_collision_step(lp_batch *b);
+lp_status lp_batch_step(lp_batch *b, int nsteps);
+/* Classes and their schedules: info6 = {n, nv, runs, cells, cells per pass,
+ * warps per line block}; tuned_ms (optional) = the class's collision step
+ * time measured by the autotuner (0 if not tuned). */
+int lp_batch_classes(const lp_batch *b);
+lp_status lp_batch_class_info(const lp_batch *b, int cls, int *info6, double *tuned_ms);
+/* Autotuner: for every class, time one collision step (best of `reps` after
+ * a warm-up, CUDA events, the class state restored before each run) for
+ * every candidate schedule -- cells per pass 64, 128, ... up to the
+ * workspace's capacity, and 2 or 4 warps per block of the line-tiled
+ * contraction -- and keep the fastest.  With cache_path, schedules already
+ * recorded there for the same key (n, nv, lv, cells, precision, device) are
+ * reused and new ones appended.  Needs every run's state; leaves it as it
+ * was. */
+lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path);
+
 /* ---- allocation-free projection ---------------------------------------- */
 /* No counterpart in the reference.  The moment-conserving projection of
  * lp_conserve for `ncell` mode arrays at once, for callers that may not

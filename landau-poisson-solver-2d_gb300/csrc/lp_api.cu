@@ -38,9 +38,24 @@ struct lp_ctx {
     // state and advection
     double *U = nullptr, *U1 = nullptr, *Ut = nullptr, *rt = nullptr, *pb = nullptr, *potc = nullptr,
            *phix = nullptr, *phiy = nullptr, *fields = nullptr, *mpart = nullptr;
+    // mixed-path advection: FP32 stage copies, charge partials per block of
+    // 128 records (nullptr when nv^3 is not a multiple of 128), reciprocals
+    // of the band diagonal
+    float *Ufa = nullptr, *Ufb = nullptr;
+    double *apart = nullptr, *rdiag = nullptr;
+    // increment form (nv^3 a multiple of 128, Poisson matrix small enough for
+    // its dense inverse): FP32 copy of U, running FP32 flux sum, FP32 charge
+    // partials of that sum, dense inverse of the Poisson matrix
+    float *Uf0 = nullptr, *Sf = nullptr, *ipart = nullptr;
+    double *Ainv = nullptr;
+    // batched runs (lp_batch): per collided cell nu and dt (nullptr: the
+    // scalars), and which parts this context holds
+    double *cnu = nullptr, *cdt = nullptr;
+    bool owns_state = true, collide_on = true, advect_on = true;
     bool has_state = false;
-    // collision workspace
-    int Bcap = 0, nchunk = 0;
+    // collision workspace (Bcap cells) and schedule: cells per pass (<= Bcap)
+    // and warps per block of the line-tiled contraction
+    int Bcap = 0, nchunk = 0, Bpass = 0, line_warps = 2;
     void *f = nullptr, *f1 = nullptr, *qn = nullptr, *F = nullptr, *t1 = nullptr, *t2 = nullptr, *Qc = nullptr,
          *Y = nullptr, *Z = nullptr;
     double2 *q[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -173,14 +188,47 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
                                  std::is_same<R, double>::value ? (double *)P : nullptr,
                                  std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
     }
-    // Poisson
-    LP_TRY(upload(c, &c->ab, T.pois.ab.data(), T.pois.ab.size()));
-    LP_TRY(upload(c, &c->ipiv, T.pois.ipiv.data(), T.pois.ipiv.size()));
-    LP_TRY(upload(c, &c->gate, T.pois.gate.data(), T.pois.gate.size()));
     return alloc_workspace<R>(c);
 }
 
-lp::PoissonDev poisson_dev(const lp_ctx *c) {
+// Poisson tables and the advection buffers; U, U1, Ut are allocated unless
+// the context works on a batch's state buffers (owns_state false).
+lp_status setup_advection(lp_ctx *c) {
+    const lp::Tables &T = c->T;
+    const size_t rec = (size_t)T.size * 7, nc = T.ncell;
+    LP_TRY(upload(c, &c->ab, T.pois.ab.data(), T.pois.ab.size()));
+    LP_TRY(upload(c, &c->ipiv, T.pois.ipiv.data(), T.pois.ipiv.size()));
+    LP_TRY(upload(c, &c->gate, T.pois.gate.data(), T.pois.gate.size()));
+    LP_TRY(dalloc(c, &c->rt, 3 * nc));
+    LP_TRY(dalloc(c, &c->pb, (size_t)T.pois.ndim));
+    LP_TRY(dalloc(c, &c->potc, 3 * nc));
+    LP_TRY(dalloc(c, &c->phix, 3 * nc));
+    LP_TRY(dalloc(c, &c->phiy, 3 * nc));
+    LP_TRY(dalloc(c, &c->fields, 14 * nc));
+    if (c->mixed) {
+        LP_TRY(dalloc(c, &c->Ufa, rec));
+        LP_TRY(dalloc(c, &c->Ufb, rec));
+        if (T.nv3 % 128 == 0) LP_TRY(dalloc(c, &c->apart, 3 * ((size_t)T.size / 128)));
+        // reciprocals of the diagonal of the band factor U (row ku+kl+1 of AB)
+        const lp::PoissonTables &pt = T.pois;
+        std::vector<double> rd(pt.ndim);
+        for (int j = 0; j < pt.ndim; ++j) rd[j] = 1.0 / pt.ab[(size_t)(pt.kl + pt.ku) + (size_t)j * pt.ldab];
+        LP_TRY(upload(c, &c->rdiag, rd.data(), rd.size()));
+        if (c->apart && pt.ndim <= 4096) {
+            LP_TRY(dalloc(c, &c->Uf0, rec));
+            LP_TRY(dalloc(c, &c->Sf, rec));
+            LP_TRY(dalloc(c, &c->ipart, 3 * ((size_t)T.size / 128)));
+            std::vector<double> inv;
+            lp::poisson_inverse(pt, inv);
+            LP_TRY(upload(c, &c->Ainv, inv.data(), inv.size()));
+        }
+    }
+    return LP_OK;
+}
+
+// fast = false: the host's operations (pois2d bit for bit); fast = true: the
+// mixed path's variant (reciprocals, charge from block partials).
+lp::PoissonDev poisson_dev(const lp_ctx *c, bool fast) {
     const lp::PoissonTables &p = c->T.pois;
     lp::PoissonDev d{};
     d.nx = p.nx; d.ny = p.ny; d.ndim = p.ndim; d.kl = p.kl; d.ku = p.ku; d.ldab = p.ldab;
@@ -191,6 +239,9 @@ lp::PoissonDev poisson_dev(const lp_ctx *c) {
     std::memcpy(d.blk[3], p.acvy, sizeof(p.acvy));
     std::memcpy(d.blk[4], p.acxrr, sizeof(p.acxrr));
     std::memcpy(d.blk[5], p.acxrl, sizeof(p.acxrl));
+    d.rdiag = fast ? c->rdiag : nullptr;
+    d.rdxp = 1.0 / p.dxp; d.rdyp = 1.0 / p.dyp;
+    d.cscale = (fast && c->apart) ? c->T.scalev : 1.0;
     return d;
 }
 
@@ -199,23 +250,70 @@ lp::AdvectDev advect_dev(const lp_ctx *c) {
     lp::AdvectDev a{};
     a.nx1 = T.prm.nx1; a.nx2 = T.prm.nx2; a.nv = T.nv; a.size = T.size;
     a.lv = T.prm.lv; a.dv = T.dv; a.dx = T.dx; a.scalev = T.scalev; a.dt = T.prm.dt;
+    a.rdv = 1.0 / T.dv; a.inv = 1.0 / T.dx / T.scalev;
+    a.dt_f = (float)T.prm.dt; a.dt6 = T.prm.dt / 6.;
     return a;
 }
 
+// pois2d on stage values Us with the host's operations (the FP64 path and
+// the reference-shaped lp_poisson).
 lp_status poisson_on(lp_ctx *c, const double *Us) {
     LP_CUDA(lp::launch_charge(Us, c->T.ncell, c->T.nv3, c->T.scalev, c->rt, c->stream));
-    LP_CUDA(lp::launch_poisson(poisson_dev(c), c->rt, c->pb, c->potc, c->phix, c->phiy, c->fields, c->stream));
+    LP_CUDA(lp::launch_poisson(poisson_dev(c, false), c->rt, 1, c->pb, c->potc, c->phix, c->phiy, c->fields,
+                               c->stream));
     return LP_OK;
 }
 
+// Mixed path: Poisson solve whose charge is in c->apart (block partials of
+// the stage values, written by the previous kernel) or, when the records of
+// a block can straddle cells, summed from Us here.
+lp_status poisson_mixed(lp_ctx *c, const double *Us) {
+    const int npart = c->apart ? c->T.nv3 / 128 : 1;
+    if (!c->apart) LP_CUDA(lp::launch_charge(Us, c->T.ncell, c->T.nv3, c->T.scalev, c->rt, c->stream));
+    LP_CUDA(lp::launch_poisson(poisson_dev(c, true), c->apart ? c->apart : c->rt, npart, c->pb, c->potc, c->phix,
+                               c->phiy, c->fields, c->stream));
+    return LP_OK;
+}
+
+// One SSP-RK3 step of U (RK3, A:428-601): stage buffers U -> U1 -> Ut -> U.
+// FP64 path: every flux in FP64, each Poisson solve as the reference's.
+// Mixed path: fluxes in FP32 from FP32 stage copies, the stage combinations,
+// charge sums and Poisson solves in FP64.
 lp_status advect(lp_ctx *c) {
     const lp::AdvectDev ad = advect_dev(c);
-    LP_TRY(poisson_on(c, c->U));
-    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U, c->fields, 0, c->U1, c->stream));
-    LP_TRY(poisson_on(c, c->U1));
-    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U1, c->fields, 1, c->Ut, c->stream));
-    LP_TRY(poisson_on(c, c->Ut));
-    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->Ut, c->fields, 2, c->U, c->stream));
+    if (!c->mixed) {
+        LP_TRY(poisson_on(c, c->U));
+        LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U, nullptr, c->fields, 0, c->U1, nullptr, nullptr, c->stream));
+        LP_TRY(poisson_on(c, c->U1));
+        LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U1, nullptr, c->fields, 1, c->Ut, nullptr, nullptr, c->stream));
+        LP_TRY(poisson_on(c, c->Ut));
+        LP_CUDA(lp::launch_flux_stage(ad, c->U, c->Ut, nullptr, c->fields, 2, c->U, nullptr, nullptr, c->stream));
+        return LP_OK;
+    }
+    if (c->Ainv) {
+        // increment form: U1 = U + dt H0, U2 = U + dt/4 (H0 + H1), U += dt/6 (H0 + H1 + 4 H2)
+        const lp::PoissonDev pd = poisson_dev(c, true);
+        const int npart = c->T.nv3 / 128;
+        const double dt = c->T.prm.dt;
+        LP_CUDA(lp::launch_state_f32_grp(c->U, c->T.size, c->Uf0, c->apart, c->stream));
+        LP_CUDA(lp::launch_poisson_dense(pd, c->apart, nullptr, 0., npart, c->Ainv, c->pb, c->potc, c->phix,
+                                         c->phiy, c->fields, c->stream));
+        LP_CUDA(lp::launch_flux_inc(ad, 0, c->Uf0, c->Uf0, c->fields, c->Sf, c->Ufa, c->U, c->ipart, c->stream));
+        LP_CUDA(lp::launch_poisson_dense(pd, c->apart, c->ipart, dt, npart, c->Ainv, c->pb, c->potc, c->phix,
+                                         c->phiy, c->fields, c->stream));
+        LP_CUDA(lp::launch_flux_inc(ad, 1, c->Ufa, c->Uf0, c->fields, c->Sf, c->Ufb, c->U, c->ipart, c->stream));
+        LP_CUDA(lp::launch_poisson_dense(pd, c->apart, c->ipart, 0.25 * dt, npart, c->Ainv, c->pb, c->potc,
+                                         c->phix, c->phiy, c->fields, c->stream));
+        LP_CUDA(lp::launch_flux_inc(ad, 2, c->Ufb, c->Uf0, c->fields, c->Sf, nullptr, c->U, nullptr, c->stream));
+        return LP_OK;
+    }
+    LP_CUDA(lp::launch_state_f32(c->U, c->T.size, c->Ufa, c->apart, c->stream));
+    LP_TRY(poisson_mixed(c, c->U));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U, c->Ufa, c->fields, 0, c->U1, c->Ufb, c->apart, c->stream));
+    LP_TRY(poisson_mixed(c, c->U1));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->U1, c->Ufb, c->fields, 1, c->Ut, c->Ufa, c->apart, c->stream));
+    LP_TRY(poisson_mixed(c, c->Ut));
+    LP_CUDA(lp::launch_flux_stage(ad, c->U, c->Ut, c->Ufa, c->fields, 2, c->U, nullptr, nullptr, c->stream));
     return LP_OK;
 }
 
@@ -224,7 +322,8 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     if (c->LW) {
-        LP_CUDA(lp::launch_computeq_lines((const float2 *)c->F, c->LW, c->line_off, T.n, Bp, q, c->stream));
+        LP_CUDA(lp::launch_computeq_lines((const float2 *)c->F, c->LW, c->line_off, T.n, Bp, q, c->stream,
+                                          c->line_warps));
         return LP_OK;
     }
     LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, q, c->stream));
@@ -232,13 +331,19 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
 }
 
 // RK4 stages 1-3 (C:831-865) from node values f and conserved q[0].
-template <typename R> lp_status rk4_stages(lp_ctx *c, int Bp) {
+lp::Rates rates_at(const lp_ctx *c, int c0) {
+    lp::Rates r;
+    if (c->cnu) { r.nu = c->cnu + c0; r.dt = c->cdt + c0; }
+    return r;
+}
+
+template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     const R *M = (const R *)c->mfwd, *Mi = (const R *)c->minv;
     for (int s = 0; s < 3; ++s) {
         LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
-                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream));
+                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0)));
         LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
         LP_TRY(contract<R>(c, Bp, c->q[s + 1]));
         LP_CUDA(lp::launch_conserve(c->q[s + 1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam,
@@ -254,12 +359,13 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp) {
     const bool f1 = (T.prm.fixes & LP_FIX_F1) != 0;
     LP_CUDA(lp::launch_project<R>(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const R *)c->tfac, T.n, T.nv, Bp,
                                   B, c0, c->U, f1 ? 7 : 6, f1 ? fixed_slots : ref_slots, T.prm.dt, T.scalev,
-                                  T.scaleL, T.scale3, (C *)c->Qc, (C *)c->Y, (C *)c->Z, c->dU, c->stream));
+                                  T.scaleL, T.scale3, (C *)c->Qc, (C *)c->Y, (C *)c->Z, c->dU, c->stream,
+                                  rates_at(c, c0)));
     if (c->mixed && f1) {
         const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
         LP_CUDA(lp::launch_moment_fix(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
                                       c->mtpart, c->U, T.nv, T.dv, T.prm.lv, c0, B, c->nrc, c->mapart, c->gm_inv,
-                                      T.prm.dt * kfac, c->mlam, c->dU, c->stream));
+                                      T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream, rates_at(c, c0)));
     }
     return LP_OK;
 }
@@ -275,7 +381,7 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
     LP_TRY(contract<R>(c, Bp, c->q[0]));
     LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
-    LP_TRY(rk4_stages<R>(c, Bp));
+    LP_TRY(rk4_stages<R>(c, c0, Bp));
     LP_TRY(project<R>(c, c0, B, Bp));
     return LP_OK;
 }
@@ -292,7 +398,7 @@ template <typename R> lp_status collide_batch_prefix(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
     LP_TRY(contract<R>(c, Bp, c->q[0]));
     LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
-    LP_TRY(rk4_stages<R>(c, Bp));
+    LP_TRY(rk4_stages<R>(c, c0, Bp));
     return LP_OK;
 }
 
@@ -302,10 +408,10 @@ lp_status collide(lp_ctx *c, int c0, int c1) {
     // the whole range fits one batch; larger ranges are processed batch by
     // batch with the stride-7 read of LP_FIX_F1, which only touches the
     // batch's own records.
-    const int total = c1 - c0;
-    for (int b0 = c0; b0 < c1; b0 += c->Bcap) {
-        const int B = std::min(c->Bcap, c1 - b0);
-        if (total > c->Bcap && !(c->T.prm.fixes & LP_FIX_F1))
+    const int total = c1 - c0, pass = c->Bpass;
+    for (int b0 = c0; b0 < c1; b0 += pass) {
+        const int B = std::min(pass, c1 - b0);
+        if (total > pass && !(c->T.prm.fixes & LP_FIX_F1))
             return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one batch");
         LP_TRY(c->mixed ? collide_batch<float>(c, b0, B) : collide_batch<double>(c, b0, B));
         LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream));
@@ -376,7 +482,7 @@ template <typename R> lp_status do_rk4_cell(lp_ctx *c, const double *f, int cell
     const lp::Tables &T = c->T;
     LP_TRY(put_real_column<R>(c, (R *)c->f, f, T.n3));
     LP_TRY(put_cplx_column<double>(c, c->q[0], qhat, T.n3));
-    LP_TRY(rk4_stages<R>(c, 32));
+    LP_TRY(rk4_stages<R>(c, cell, 32));
     LP_TRY(project<R>(c, cell, 1, 32));
     LP_CUDA(cudaMemcpyAsync(dU, c->dU, sizeof(double) * 5 * T.nv3, cudaMemcpyDeviceToHost, c->stream));
     LP_CUDA(cudaStreamSynchronize(c->stream));
@@ -450,11 +556,15 @@ void destroy(lp_ctx *c) {
     delete c;
 }
 
-}  // namespace
+// Context creation.  A batch builds collision-only contexts (one per class
+// of runs, over the class's concatenated cells) and advection-only contexts
+// (one per run, working on its slice of the class's state buffers).
+struct CtxOpts {
+    bool collide = true, advect = true;
+    double *U = nullptr, *U1 = nullptr, *Ut = nullptr;  // external state buffers
+};
 
-extern "C" {
-
-lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) {
+lp_status ctx_create(const lp_params *p, const CtxOpts &o, lp_ctx **out) {
     if (!p || !out) return LP_ERR_INVALID;
     *out = nullptr;
     int ndev = 0;
@@ -464,7 +574,8 @@ lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) {
     }
     lp_ctx *c = new lp_ctx();
     std::string err;
-    lp_status s = lp::build_tables(*p, c->T, err);
+    const unsigned parts = (o.collide ? lp::kTablesCollision : 0u) | (o.advect ? lp::kTablesPoisson : 0u);
+    lp_status s = lp::build_tables(*p, c->T, err, parts);
     if (s != LP_OK) {
         delete c;
         return s;
@@ -482,19 +593,22 @@ lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) {
     }
     c->stream = c->own_stream;
     c->mixed = (p->precision == LP_PREC_MIXED);
+    c->collide_on = o.collide;
+    c->advect_on = o.advect;
+    c->owns_state = (o.U == nullptr);
     c->Bcap = round32(std::min(std::max(c->T.ncollide, 1), 512));
+    c->Bpass = c->Bcap;
     const lp::Tables &T = c->T;
-    const size_t rec = (size_t)T.size * 7, nc = T.ncell;
-    s = c->mixed ? upload_tables<float>(c) : upload_tables<double>(c);
-    if (s == LP_OK) s = dalloc(c, &c->U, rec);
-    if (s == LP_OK) s = dalloc(c, &c->U1, rec);
-    if (s == LP_OK) s = dalloc(c, &c->Ut, rec);
-    if (s == LP_OK) s = dalloc(c, &c->rt, 3 * nc);
-    if (s == LP_OK) s = dalloc(c, &c->pb, (size_t)T.pois.ndim);
-    if (s == LP_OK) s = dalloc(c, &c->potc, 3 * nc);
-    if (s == LP_OK) s = dalloc(c, &c->phix, 3 * nc);
-    if (s == LP_OK) s = dalloc(c, &c->phiy, 3 * nc);
-    if (s == LP_OK) s = dalloc(c, &c->fields, 14 * nc);
+    const size_t rec = (size_t)T.size * 7;
+    if (o.collide) s = c->mixed ? upload_tables<float>(c) : upload_tables<double>(c);
+    if (s == LP_OK && c->owns_state) {
+        s = dalloc(c, &c->U, rec);
+        if (s == LP_OK) s = dalloc(c, &c->U1, rec);
+        if (s == LP_OK) s = dalloc(c, &c->Ut, rec);
+    } else if (s == LP_OK) {
+        c->U = o.U; c->U1 = o.U1; c->Ut = o.Ut;
+    }
+    if (s == LP_OK && o.advect) s = setup_advection(c);
     if (s == LP_OK) s = dalloc(c, &c->mpart, 5 * kMomBlocks);
     if (s == LP_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) s = LP_ERR_CUDA;
     if (s != LP_OK) {
@@ -505,6 +619,12 @@ lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) {
     *out = c;
     return LP_OK;
 }
+
+}  // namespace
+
+extern "C" {
+
+lp_status lp_ctx_create(const lp_params *p, lp_ctx **out) { return ctx_create(p, CtxOpts{}, out); }
 
 lp_status lp_ctx_destroy(lp_ctx *c) {
     if (!c) return LP_ERR_INVALID;
@@ -718,7 +838,6 @@ lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
 }
 
 lp_status lp_measure_fp_peaks(double *fp32, double *fp64) {
-    lp_ctx *c = nullptr;  // LP_CUDA reports through c; no context here
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return LP_ERR_NO_DEVICE;
@@ -745,7 +864,6 @@ lp_status lp_measure_fp_peaks(double *fp32, double *fp64) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(sink);
-    (void)c;
     if (cudaGetLastError() != cudaSuccess) return LP_ERR_CUDA;
     if (fp32) *fp32 = out[0];
     if (fp64) *fp64 = out[1];
@@ -779,6 +897,410 @@ lp_status lp_moments(lp_ctx *c, double *out) {
         e += (px[3 * k + 2] * px[3 * k + 2] + py[3 * k + 2] * py[3 * k + 2]) / 12;
     }
     out[5] = 0.5 * (dx * dy) * e;
+    return LP_OK;
+}
+
+}  // extern "C"
+
+// ============================================================== batches
+// Many independent runs stepped together.  Runs with equal (n, nv, lv) form
+// a class: one collision-only context over the class's concatenated spatial
+// cells (its weight table and workspace shared by the runs, per-cell nu and
+// dt), whose state buffers hold the runs' states back to back; every run has
+// an advection-only context (its own grid, Poisson factors and fields) on
+// its slice of those buffers.  A time step advects every run on its own
+// stream, then collides every class on its own stream; lp_batch_step
+// replays that step from one captured CUDA graph.
+struct lp_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+    std::string err;
+    struct Run {
+        lp_ctx *adv = nullptr;
+        int cls = 0, cell0 = 0;
+        cudaStream_t st = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    struct Cls {
+        lp_ctx *eng = nullptr;
+        std::vector<int> runs;
+        int ncell = 0;
+        bool collide = false;  // some run has nu > 0
+        double tuned_ms = 0.;
+        cudaStream_t st = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Run> runs;
+    std::vector<Cls> cls;
+    cudaEvent_t fork = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;
+};
+
+namespace {
+
+lp_status bfail(lp_batch *b, lp_status s, const std::string &msg) {
+    if (b) b->err = msg;
+    return s;
+}
+
+#define LPB_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return bfail(b, LP_ERR_CUDA, std::string(#call) + ": " +     \
+                                                                cudaGetErrorString(e_));    \
+    } while (0)
+
+void batch_destroy(lp_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (auto &r : b->runs) {
+        if (r.adv) { cudaStreamSynchronize(r.adv->stream); destroy(r.adv); }
+        if (r.st) cudaStreamDestroy(r.st);
+        if (r.done) cudaEventDestroy(r.done);
+    }
+    for (auto &k : b->cls) {
+        if (k.eng) { cudaStreamSynchronize(k.eng->stream); destroy(k.eng); }
+        if (k.st) cudaStreamDestroy(k.st);
+        if (k.done) cudaEventDestroy(k.done);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    delete b;
+}
+
+// One time step (or one of its halves) of every run, forked from b->stream
+// onto the runs' and classes' streams and joined back; also the body of the
+// captured step graph.
+lp_status batch_body(lp_batch *b, bool adv, bool col) {
+    cudaStream_t S = b->stream;
+    if (adv) {
+        LPB_CUDA(cudaEventRecord(b->fork, S));
+        for (auto &r : b->runs) {
+            LPB_CUDA(cudaStreamWaitEvent(r.st, b->fork, 0));
+            r.adv->stream = r.st;
+            const lp_status s = advect(r.adv);
+            if (s != LP_OK) return bfail(b, s, "advection: " + r.adv->err);
+            LPB_CUDA(cudaEventRecord(r.done, r.st));
+            LPB_CUDA(cudaStreamWaitEvent(S, r.done, 0));
+        }
+    }
+    if (col) {
+        LPB_CUDA(cudaEventRecord(b->fork, S));
+        for (auto &k : b->cls) {
+            if (!k.collide) continue;
+            LPB_CUDA(cudaStreamWaitEvent(k.st, b->fork, 0));
+            k.eng->stream = k.st;
+            const lp_status s = collide(k.eng, 0, k.ncell);
+            if (s != LP_OK) return bfail(b, s, "collision: " + k.eng->err);
+            LPB_CUDA(cudaEventRecord(k.done, k.st));
+            LPB_CUDA(cudaStreamWaitEvent(S, k.done, 0));
+        }
+    }
+    return LP_OK;
+}
+
+bool batch_ready(lp_batch *b) {
+    for (auto &r : b->runs)
+        if (!r.adv->has_state) return false;
+    return true;
+}
+
+std::string class_key(const lp_batch::Cls &k) {
+    const lp::Tables &T = k.eng->T;
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, k.eng->device);
+    char buf[512];
+    snprintf(buf, sizeof(buf), "n%d_nv%d_lv%.17g_cells%d_%s_%s", T.n, T.nv, T.prm.lv, k.ncell,
+             k.eng->mixed ? "mixed" : "fp64", prop.name);
+    std::string s(buf);
+    for (char &ch : s)
+        if (ch == ' ') ch = '-';
+    return s;
+}
+
+// Time one collision step of class k with the current schedule: the class
+// state is restored from its copy in `backup` before every run, and only the
+// collision is inside the events.
+lp_status time_class(lp_batch *b, lp_batch::Cls &k, double *backup, int reps, double *ms) {
+    lp_ctx *e = k.eng;
+    const size_t bytes = sizeof(double) * (size_t)e->T.size * 7;
+    cudaEvent_t e0, e1;
+    LPB_CUDA(cudaEventCreate(&e0));
+    LPB_CUDA(cudaEventCreate(&e1));
+    e->stream = b->stream;
+    double best = 1e300;
+    for (int i = 0; i <= reps; ++i) {  // the first run is a warm-up
+        LPB_CUDA(cudaMemcpyAsync(e->U, backup, bytes, cudaMemcpyDeviceToDevice, b->stream));
+        LPB_CUDA(cudaEventRecord(e0, b->stream));
+        const lp_status s = collide(e, 0, k.ncell);
+        if (s != LP_OK) return bfail(b, s, "autotune: " + e->err);
+        LPB_CUDA(cudaEventRecord(e1, b->stream));
+        LPB_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        LPB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        if (i > 0) best = std::min(best, (double)t);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = best;
+    return LP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lp_status lp_batch_create(const lp_params *ps, int count, lp_batch **out) {
+    if (!ps || !out || count < 1) return LP_ERR_INVALID;
+    *out = nullptr;
+    const unsigned fixes = ps[0].fixes;
+    const int prec = ps[0].precision;
+    for (int r = 0; r < count; ++r) {
+        if (ps[r].fixes != fixes || ps[r].precision != prec) return LP_ERR_INVALID;  // shared fixes and precision
+        const int ncell = ps[r].nx1 * ps[r].nx2;
+        const int ncollide = (fixes & LP_FIX_F3) ? ncell : std::min(ps[r].nx1, ncell);
+        if (ncollide != ncell) return LP_ERR_INVALID;  // 2-D runs need LP_FIX_F3
+    }
+    if (!(fixes & LP_FIX_F1)) return LP_ERR_INVALID;  // collisions run in passes of cells
+    lp_batch *b = new lp_batch();
+    cudaGetDevice(&b->device);
+    if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+        batch_destroy(b);
+        return LP_ERR_CUDA;
+    }
+    b->stream = b->own_stream;
+    // classes by (n, nv, lv), in order of first appearance
+    b->runs.resize(count);
+    for (int r = 0; r < count; ++r) {
+        int k = 0;
+        for (; k < (int)b->cls.size(); ++k) {
+            const lp_params &q = ps[b->cls[k].runs[0]];
+            if (q.n == ps[r].n && q.nv == ps[r].nv && q.lv == ps[r].lv) break;
+        }
+        if (k == (int)b->cls.size()) b->cls.emplace_back();
+        auto &K = b->cls[k];
+        b->runs[r].cls = k;
+        b->runs[r].cell0 = K.ncell;
+        K.runs.push_back(r);
+        K.ncell += ps[r].nx1 * ps[r].nx2;
+        if (ps[r].nu > 0.) K.collide = true;
+    }
+    lp_status s = LP_OK;
+    for (auto &K : b->cls) {
+        lp_params pe = ps[K.runs[0]];
+        pe.nx1 = K.ncell; pe.nx2 = 1; pe.nu = 1.0; pe.dt = 1.0;
+        CtxOpts o;
+        o.advect = false;
+        s = ctx_create(&pe, o, &K.eng);
+        if (s != LP_OK) break;
+        // per-cell nu and dt, padded by one pass
+        std::vector<double> nu(K.ncell + K.eng->Bcap, 0.), dt(K.ncell + K.eng->Bcap, 0.);
+        for (int r : K.runs) {
+            const int nc = ps[r].nx1 * ps[r].nx2;
+            for (int i = 0; i < nc; ++i) {
+                nu[b->runs[r].cell0 + i] = ps[r].nu;
+                dt[b->runs[r].cell0 + i] = ps[r].dt;
+            }
+        }
+        s = upload(K.eng, &K.eng->cnu, nu.data(), nu.size());
+        if (s == LP_OK) s = upload(K.eng, &K.eng->cdt, dt.data(), dt.size());
+        if (s == LP_OK && (cudaStreamCreateWithFlags(&K.st, cudaStreamNonBlocking) != cudaSuccess ||
+                           cudaEventCreateWithFlags(&K.done, cudaEventDisableTiming) != cudaSuccess))
+            s = LP_ERR_CUDA;
+        if (s != LP_OK) break;
+    }
+    for (int r = 0; r < count && s == LP_OK; ++r) {
+        auto &R = b->runs[r];
+        lp_ctx *eng = b->cls[R.cls].eng;
+        const size_t off = (size_t)R.cell0 * eng->T.nv3 * 7;
+        CtxOpts o;
+        o.collide = false;
+        o.U = eng->U + off; o.U1 = eng->U1 + off; o.Ut = eng->Ut + off;
+        s = ctx_create(&ps[r], o, &R.adv);
+        if (s == LP_OK && (cudaStreamCreateWithFlags(&R.st, cudaStreamNonBlocking) != cudaSuccess ||
+                           cudaEventCreateWithFlags(&R.done, cudaEventDisableTiming) != cudaSuccess))
+            s = LP_ERR_CUDA;
+    }
+    if (s != LP_OK) {
+        batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return LP_OK;
+}
+
+lp_status lp_batch_destroy(lp_batch *b) {
+    if (!b) return LP_ERR_INVALID;
+    batch_destroy(b);
+    return LP_OK;
+}
+
+lp_status lp_batch_set_stream(lp_batch *b, void *st) {
+    if (!b) return LP_ERR_INVALID;
+    b->stream = st ? (cudaStream_t)st : b->own_stream;
+    return LP_OK;
+}
+
+lp_status lp_batch_synchronize(lp_batch *b) {
+    if (!b) return LP_ERR_INVALID;
+    LPB_CUDA(cudaStreamSynchronize(b->stream));
+    return LP_OK;
+}
+
+const char *lp_batch_last_error(const lp_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+size_t lp_batch_device_bytes(const lp_batch *b) {
+    if (!b) return 0;
+    size_t n = 0;
+    for (auto &r : b->runs) n += r.adv->bytes;
+    for (auto &k : b->cls) n += k.eng->bytes;
+    return n;
+}
+
+lp_status lp_batch_set_state(lp_batch *b, int run, const double *U, size_t n) {
+    if (!b || run < 0 || run >= (int)b->runs.size()) return LP_ERR_INVALID;
+    lp_ctx *c = b->runs[run].adv;
+    c->stream = b->stream;
+    const lp_status s = lp_set_state(c, U, n);
+    return s == LP_OK ? s : bfail(b, s, c->err);
+}
+
+lp_status lp_batch_get_state(lp_batch *b, int run, double *U, size_t n) {
+    if (!b || run < 0 || run >= (int)b->runs.size()) return LP_ERR_INVALID;
+    lp_ctx *c = b->runs[run].adv;
+    c->stream = b->stream;
+    const lp_status s = lp_get_state(c, U, n);
+    return s == LP_OK ? s : bfail(b, s, c->err);
+}
+
+lp_status lp_batch_set_init(lp_batch *b, int run, int kind, double u) {
+    if (!b || run < 0 || run >= (int)b->runs.size()) return LP_ERR_INVALID;
+    lp_ctx *c = b->runs[run].adv;
+    c->stream = b->stream;
+    const lp_status s = lp_set_init(c, kind, u);
+    return s == LP_OK ? s : bfail(b, s, c->err);
+}
+
+lp_status lp_batch_moments(lp_batch *b, int run, double *out6) {
+    if (!b || run < 0 || run >= (int)b->runs.size()) return LP_ERR_INVALID;
+    lp_ctx *c = b->runs[run].adv;
+    LPB_CUDA(cudaStreamSynchronize(b->stream));
+    c->stream = b->stream;
+    const lp_status s = lp_moments(c, out6);
+    return s == LP_OK ? s : bfail(b, s, c->err);
+}
+
+lp_status lp_batch_advect_step(lp_batch *b) {
+    if (!b) return LP_ERR_INVALID;
+    if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
+    return batch_body(b, true, false);
+}
+
+lp_status lp_batch_collision_step(lp_batch *b) {
+    if (!b) return LP_ERR_INVALID;
+    if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
+    return batch_body(b, false, true);
+}
+
+lp_status lp_batch_step(lp_batch *b, int nsteps) {
+    if (!b || nsteps < 0) return LP_ERR_INVALID;
+    if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
+    if (nsteps == 0) return LP_OK;
+    if (!b->gexec || b->gstream != b->stream) {
+        if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        LPB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const lp_status s = batch_body(b, true, true);
+        const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
+        if (e != cudaSuccess) return bfail(b, LP_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+        const cudaError_t e2 = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) return bfail(b, LP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e2));
+        b->gstream = b->stream;
+    }
+    for (int i = 0; i < nsteps; ++i) LPB_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    return LP_OK;
+}
+
+int lp_batch_classes(const lp_batch *b) { return b ? (int)b->cls.size() : 0; }
+
+lp_status lp_batch_class_info(const lp_batch *b, int k, int *info6, double *tuned_ms) {
+    if (!b || k < 0 || k >= (int)b->cls.size() || !info6) return LP_ERR_INVALID;
+    const auto &K = b->cls[k];
+    info6[0] = K.eng->T.n; info6[1] = K.eng->T.nv; info6[2] = (int)K.runs.size(); info6[3] = K.ncell;
+    info6[4] = K.eng->Bpass; info6[5] = K.eng->line_warps;
+    if (tuned_ms) *tuned_ms = K.tuned_ms;
+    return LP_OK;
+}
+
+lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path) {
+    if (!b || reps < 1) return LP_ERR_INVALID;
+    if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
+    LPB_CUDA(cudaStreamSynchronize(b->stream));
+    // cached schedules: lines "key pass_cells line_warps ms"
+    std::vector<std::string> cache_lines;
+    if (cache_path) {
+        if (FILE *fp = fopen(cache_path, "r")) {
+            char line[512];
+            while (fgets(line, sizeof(line), fp)) cache_lines.emplace_back(line);
+            fclose(fp);
+        }
+    }
+    bool changed = false;
+    for (auto &K : b->cls) {
+        lp_ctx *e = K.eng;
+        const std::string key = class_key(K);
+        bool found = false;
+        for (const auto &l : cache_lines) {
+            char kbuf[400];
+            int bp = 0, lw = 0;
+            double ms = 0.;
+            if (sscanf(l.c_str(), "%399s %d %d %lf", kbuf, &bp, &lw, &ms) == 4 && key == kbuf && bp >= 32 &&
+                bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4)) {
+                e->Bpass = bp; e->line_warps = lw; K.tuned_ms = ms;
+                found = true;
+            }
+        }
+        if (found || !K.collide) continue;
+        // candidates: passes of 64..Bcap cells (every pass one launch set),
+        // and 2 or 4 warps per line block in the line-tiled contraction
+        std::vector<int> passes;
+        for (int bp = 64; bp < e->Bcap; bp *= 2) passes.push_back(bp);
+        passes.push_back(e->Bcap);
+        std::vector<int> warps = {2};
+        if (e->LW) warps.push_back(4);
+        LPB_CUDA(cudaMemcpyAsync(e->U1, e->U, sizeof(double) * (size_t)e->T.size * 7, cudaMemcpyDeviceToDevice,
+                                 b->stream));
+        double best = 1e300;
+        int bbp = e->Bcap, blw = 2;
+        for (int bp : passes)
+            for (int lw : warps) {
+                e->Bpass = bp; e->line_warps = lw;
+                double ms = 0.;
+                const lp_status s = time_class(b, K, e->U1, reps, &ms);
+                if (s != LP_OK) return s;
+                if (ms < best) { best = ms; bbp = bp; blw = lw; }
+            }
+        LPB_CUDA(cudaMemcpyAsync(e->U, e->U1, sizeof(double) * (size_t)e->T.size * 7, cudaMemcpyDeviceToDevice,
+                                 b->stream));
+        LPB_CUDA(cudaStreamSynchronize(b->stream));
+        e->Bpass = bbp; e->line_warps = blw; K.tuned_ms = best;
+        char line[768];
+        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), bbp, blw, best);
+        cache_lines.emplace_back(line);
+        changed = true;
+    }
+    if (changed && cache_path) {
+        if (FILE *fp = fopen(cache_path, "w")) {
+            for (const auto &l : cache_lines) fputs(l.c_str(), fp);
+            fclose(fp);
+        }
+    }
+    if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }  // recapture with the new schedule
     return LP_OK;
 }
 

@@ -5,6 +5,7 @@
 //   S = source/SetInit_1.cpp             MC = source/MomentCalculations.cpp
 #include "lp_kernels.cuh"
 
+#include <algorithm>
 #include <cstdint>
 #include <type_traits>
 
@@ -100,7 +101,8 @@ __global__ void k_nodes(const double *__restrict__ U, int nv, int n, int c0, int
 template <typename R, typename TIn, int OUT>
 __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict__ out,
                       const R *__restrict__ M, int n, int ax, int Bp, int stage, R dt, R nu,
-                      const R *__restrict__ f, R *__restrict__ qn, R *__restrict__ f1) {
+                      const R *__restrict__ f, R *__restrict__ qn, R *__restrict__ f1,
+                      const double *__restrict__ cnu, const double *__restrict__ cdt) {
     using C = typename V2<R>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *Ms = reinterpret_cast<C *>(smem_raw);
@@ -126,23 +128,26 @@ __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict_
     if constexpr (OUT == 0) {
         out[o] = mk2<R>(sr, si);
     } else {
-        // RK4 node-value stages (C:831-862).
+        // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
+        R dtc = dt, nuc = nu;
+        if (cnu) { nuc = (R)cnu[c]; dtc = (R)cdt[c]; }
         if (stage == 0) {
             qn[o] = sr;
-            f1[o] = f[o] + dt * sr * nu;
+            f1[o] = f[o] + dtc * sr * nuc;
         } else {
-            f1[o] = f[o] + R(0.5) * dt * qn[o] * nu + R(0.5) * dt * sr * nu;
+            f1[o] = f[o] + R(0.5) * dtc * qn[o] * nuc + R(0.5) * dtc * sr * nuc;
         }
     }
 }
 
 template <typename R, typename TIn, int OUT>
 cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
-                     double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st) {
+                     double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{}) {
     using C = typename V2<R>::t;
     const size_t smem = sizeof(C) * (size_t)(n * n + 32 * n);
     dim3 grid(n * n, Bp / 32), block(32, n);
-    k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1);
+    k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1, rates.nu,
+                                                  rates.dt);
     return cudaGetLastError();
 }
 
@@ -230,7 +235,6 @@ template <> struct LinesCfg<8> { static constexpr int KT = 8; };
 template <> struct LinesCfg<16> { static constexpr int KT = 8; };
 template <> struct LinesCfg<24> { static constexpr int KT = 12; };
 template <> struct LinesCfg<32> { static constexpr int KT = 8; };
-constexpr int kLineWarps = 2;  // warps of a block share one output line tile
 
 __device__ __forceinline__ float pick4(const float4 &v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w)); }
 
@@ -265,10 +269,9 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// One k-tile of output lines.  The kLineWarps warps of a block take the
+// One k-tile of output lines.  The LW warps of a block take the
 // plane pairs of the same (line, tile, 32 cells) in turn; each warp stages
 // the plane pair's two F lines in shared memory with cp.async (one buffer:
 // every lane copies and reads only its own cell's column, and the copy of
@@ -279,8 +282,8 @@ __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_g
 // Re = U.x - U.y, Im = V.x + V.y; each plane's partials enter a
 // Kahan-compensated FP32 accumulator, and the warps' results are summed in
 // FP64 in a fixed order.
-template <int N, int TILE>
-__global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
+template <int N, int TILE, int LW>
+__global__ void __launch_bounds__(32 * LW, 12 / LW) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
                                                             const long long *__restrict__ line_off, int Bp,
                                                             double2 *__restrict__ q) {
     constexpr int KT = LinesCfg<N>::KT, h = N / 2, K0 = TILE * KT;
@@ -290,13 +293,14 @@ __global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *_
     // per warp: [2 lines][N][32 lanes] float2; then per warp [2 buffers][TT]
     // weights; the reduction area reuses the space after the loop
     float2 *stage = reinterpret_cast<float2 *>(lines_smem);
-    float *wstage = reinterpret_cast<float *>(lines_smem + sizeof(float2) * 2 * N * 32 * kLineWarps);
+    float *wstage = reinterpret_cast<float *>(lines_smem + sizeof(float2) * 2 * N * 32 * LW);
     double2 *red = reinterpret_cast<double2 *>(lines_smem);  // reuses the staging area after the loop
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2 *mybuf = stage + (long long)warp * 2 * N * 32;
     float *mywbuf = wstage + warp * 2 * TT;
     const int G = Bp / 32;
-    const int g = (int)(blockIdx.x % G), ij = (int)(blockIdx.x / G);
+    // line_off holds N^2 + 1 weight offsets, then the lines longest first
+    const int g = (int)(blockIdx.x % G), ij = (int)line_off[N * N + 1 + blockIdx.x / G];
     const int i = ij / N, j = ij % N;
     const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
     const int sj = j < h ? 0 : j - h + 1, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
@@ -331,8 +335,8 @@ __global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *_
     }
     cp_async_commit();
     int it = 0;
-    for (int pp = warp; pp < npp; pp += kLineWarps, ++it) {
-        const int nxt = pp + kLineWarps;
+    for (int pp = warp; pp < npp; pp += LW, ++it) {
+        const int nxt = pp + LW;
         cp_async_wait0();
         __syncwarp();
         // (issued before the line reads: the copy instructions order the
@@ -386,10 +390,10 @@ __global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *_
     for (int kk = 0; kk < KT; ++kk)
         red[(warp * KT + kk) * 32 + lane] = make_double2((double)sr[kk] - (double)cr[kk], (double)sim[kk] - (double)ci[kk]);
     __syncthreads();
-    for (int kk = warp; kk < KT; kk += kLineWarps) {
+    for (int kk = warp; kk < KT; kk += LW) {
         double2 acc = red[kk * 32 + lane];
 #pragma unroll
-        for (int w = 1; w < kLineWarps; ++w) {
+        for (int w = 1; w < LW; ++w) {
             const double2 v = red[(w * KT + kk) * 32 + lane];
             acc.x += v.x; acc.y += v.y;
         }
@@ -397,11 +401,11 @@ __global__ void __launch_bounds__(32 * kLineWarps, 6) k_cq_lines(const float2 *_
     }
 }
 
-template <int N, int T> constexpr size_t lines_smem_bytes() {
+template <int N, int T, int LW> constexpr size_t lines_smem_bytes() {
     constexpr int KT = LinesCfg<N>::KT;
-    constexpr size_t staging = sizeof(float2) * 2 * N * 32 * kLineWarps +
-                               sizeof(float) * 2 * tile_floats<N>(T * KT, T * KT + KT) * kLineWarps;
-    constexpr size_t reduction = sizeof(double2) * kLineWarps * KT * 32;
+    constexpr size_t staging = sizeof(float2) * 2 * N * 32 * LW +
+                               sizeof(float) * 2 * tile_floats<N>(T * KT, T * KT + KT) * LW;
+    constexpr size_t reduction = sizeof(double2) * LW * KT * 32;
     return staging > reduction ? staging : reduction;
 }
 
@@ -507,9 +511,11 @@ __global__ void k_cons_apply(double2 *__restrict__ q, const double *__restrict__
 template <typename R>
 __global__ void k_qcomb(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
                         const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
-                        long long total, typename V2<R>::t *__restrict__ Qc) {
+                        long long total, int Bp, const double *__restrict__ cnu,
+                        typename V2<R>::t *__restrict__ Qc) {
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= total) return;
+    if (cnu) nu = cnu[tid % Bp];
     const double2 a = q0[tid], b = q1[tid], d = q2[tid], e = q3[tid];
     constexpr double sixth = 1. / 6.;
     const double re = nu * (0.5 * a.x + (b.x + d.x + e.x) * sixth);
@@ -612,13 +618,14 @@ __global__ void k_proj2(const typename V2<R>::t *__restrict__ Y, const R *__rest
 template <typename R>
 __global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__restrict__ tf, int n, int nv,
                         int Bp, int B, int c0, const double *__restrict__ U, int ustride, int4 us, int us4,
-                        double dt, double kfac, double *__restrict__ dU) {
+                        double dt, double kfac, const double *__restrict__ cdt, double *__restrict__ dU) {
     const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nv3 = (long long)nv * nv * nv;
     if (tid >= (long long)nv * nv * nch * Bp) return;
     const int c = (int)(tid % Bp);
     if (c >= B) return;
+    if (cdt) dt = cdt[c];
     long long r = tid / Bp;
     const int j3 = (int)(r % nv); r /= nv;
     const int j2 = (int)(r % nv), ch = (int)(r / nv);
@@ -677,10 +684,11 @@ __global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__rest
 // coefficients carry exactly the FP64 moments.
 __global__ void k_mom_target(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
                              const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
-                             const double *__restrict__ gmom, int n3, int Bp, int nchunk,
-                             double *__restrict__ part) {
+                             const double *__restrict__ cnu, const double *__restrict__ gmom, int n3, int Bp,
+                             int nchunk, double *__restrict__ part) {
     __shared__ double red[8][5][32];
     const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
+    if (cnu) nu = cnu[c];
     const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
     double t[5] = {0, 0, 0, 0, 0};
     for (int pt = p0 + y; pt < p1; pt += 8) {
@@ -743,10 +751,11 @@ __global__ void k_mom_actual(const double *__restrict__ dU, const double *__rest
 }
 
 __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const double *__restrict__ apart,
-                             int nrc, const double *__restrict__ gm_inv, double scale, int B, int Bp,
-                             double *__restrict__ lam) {
+                             int nrc, const double *__restrict__ gm_inv, double scale, double kfac,
+                             const double *__restrict__ cdt, int B, int Bp, double *__restrict__ lam) {
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
+    if (cdt) scale = cdt[c] * kfac;
     double tg[5] = {0, 0, 0, 0, 0}, ac[5] = {0, 0, 0, 0, 0};
     for (int k = lane; k < nchunk; k += 32)
         for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
@@ -799,56 +808,121 @@ __global__ void k_scatter(const double *__restrict__ dU, long long nrec, long lo
 // Charge moments per spatial cell: the sums over the cell's
 // records of scalev (U0 + U6/4), scalev U1 and scalev U2.  The right-hand
 // side of the Poisson problem is the small difference rho - 1, so the
-// summation order matters at the 1e-12 level; the terms are staged in shared
-// memory and each moment is accumulated by one thread in the reference's
-// record order, without FMA, which gives the reference's sums bit for bit.
-constexpr int kChargeChunk = 2048;
-__global__ void k_charge(const double *__restrict__ U, int nv3, double scalev, double *__restrict__ rt) {
-    __shared__ double term[3][kChargeChunk];
+// summation order matters at the 1e-12 level.  k_charge_seq accumulates each
+// moment in one thread in the reference's record order without FMA, which
+// gives the reference's sums bit for bit: warp 0 sums one chunk of terms
+// while the other warps stage the next chunk in shared memory.
+constexpr int kChargeChunk = 1024;
+__global__ void __launch_bounds__(256) k_charge_seq(const double *__restrict__ U, int nv3, double scalev,
+                                                   double *__restrict__ rt) {
+    __shared__ double term[2][3][kChargeChunk];
     const int s = blockIdx.x, t = threadIdx.x;
     const double *base = U + 7 * (long long)s * nv3;
-    double acc = 0.0;
-    for (int c0 = 0; c0 < nv3; c0 += kChargeChunk) {
-        const int len = min(kChargeChunk, nv3 - c0);
-        for (int j = t; j < len; j += blockDim.x) {
+    const int nchunk = (nv3 + kChargeChunk - 1) / kChargeChunk;
+    auto stage = [&](int ch, int tid, int nthr) {
+        const int c0 = ch * kChargeChunk, len = min(kChargeChunk, nv3 - c0);
+        for (int j = tid; j < len; j += nthr) {
             const double *u = base + 7 * (long long)(c0 + j);
-            term[0][j] = __dmul_rn(scalev, __dadd_rn(u[0], __dmul_rn(0.25, u[6])));
-            term[1][j] = __dmul_rn(scalev, u[1]);
-            term[2][j] = __dmul_rn(scalev, u[2]);
+            term[ch & 1][0][j] = __dmul_rn(scalev, __dadd_rn(u[0], __dmul_rn(0.25, u[6])));
+            term[ch & 1][1][j] = __dmul_rn(scalev, u[1]);
+            term[ch & 1][2][j] = __dmul_rn(scalev, u[2]);
         }
-        __syncthreads();
-        if (t < 3) {
-            const double *tt = term[t];
+    };
+    stage(0, t, blockDim.x);
+    __syncthreads();
+    double acc = 0.0;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        if (t < 32) {
+            if (t < 3) {
+                const int len = min(kChargeChunk, nv3 - ch * kChargeChunk);
+                const double *tt = term[ch & 1][t];
 #pragma unroll 8
-            for (int j = 0; j < len; ++j) acc = __dadd_rn(acc, tt[j]);
+                for (int j = 0; j < len; ++j) acc = __dadd_rn(acc, tt[j]);
+            }
+        } else if (ch + 1 < nchunk) {
+            stage(ch + 1, t - 32, blockDim.x - 32);
         }
         __syncthreads();
     }
     if (t < 3) rt[3 * s + t] = acc;
 }
 
+// Block sums of (U0 + U6/4, U1, U2) over 128 consecutive records, written to
+// part[blockIdx.x][3] in a fixed order; the Poisson kernel adds a cell's
+// blocks in order and scales by scalev (the mixed path's charge).
+__device__ __forceinline__ void charge_block_sum(double a0, double a1, double a2, double *__restrict__ part) {
+    __shared__ double red[3][4];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    const int t = threadIdx.x;
+    if ((t & 31) == 0) { red[0][t >> 5] = a0; red[1][t >> 5] = a1; red[2][t >> 5] = a2; }
+    __syncthreads();
+    if (t < 3) part[3 * (long long)blockIdx.x + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
+}
+
+// FP32 copy of the state for the FP32 flux, with the charge partial sums of
+// the same records (one record per thread, 128 records per block).
+__global__ void __launch_bounds__(128) k_state_f32(const double *__restrict__ U, long long size,
+                                                  float *__restrict__ Uf, double *__restrict__ part) {
+    const long long k = blockIdx.x * 128ll + threadIdx.x;
+    double a0 = 0., a1 = 0., a2 = 0.;
+    if (k < size) {
+        const double *u = U + 7 * k;
+        double v[7];
+#pragma unroll
+        for (int l = 0; l < 7; ++l) { v[l] = u[l]; Uf[7 * k + l] = (float)v[l]; }
+        a0 = v[0] + 0.25 * v[6]; a1 = v[1]; a2 = v[2];
+    }
+    if (part) charge_block_sum(a0, a1, a2, part);
+}
+
 // pois2d in one block: right-hand side, the band solve of DGBTRS
-// replayed on one warp in the host factorisation's operation order (no FMA),
-// field reconstruction and the cell integrals used by the advection.
-__global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *__restrict__ bg,
+// replayed on one warp in the host factorisation's operation order, field
+// reconstruction and the cell integrals used by the advection.  With
+// pd.rdiag == nullptr every operation is the host's, without FMA (the
+// reference's result bit for bit); otherwise (mixed path) divisions become
+// products with precomputed reciprocals and the charge comes as npart block
+// partial sums per cell.
+__global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, int npart, double *__restrict__ bg,
                           double *__restrict__ potc, double *__restrict__ phix, double *__restrict__ phiy,
                           double *__restrict__ fields) {
     extern __shared__ double b[];
     const int t = threadIdx.x, nc = pd.nx * pd.ny, nd = pd.ndim;
+    const bool fast = pd.rdiag != nullptr;
+    // shared memory: b[nd], the band factors (when they fit), the pivots
+    double *sab = b + nd;
+    int *spiv = reinterpret_cast<int *>(sab + (pd.staged ? (size_t)pd.ldab * nd : 0));
+    if (pd.staged)
+        for (long long i = t; i < (long long)pd.ldab * nd; i += blockDim.x) sab[i] = pd.ab[i];
+    for (int i = t; i < nd; i += blockDim.x) spiv[i] = pd.ipiv[i];
+    const double *AB = pd.staged ? sab : pd.ab;
     for (int ii = t; ii < nc; ii += blockDim.x) {
         const double DXv = pd.dxp, DYv = pd.dyp;
-        b[3 * ii] = __dmul_rn(__dmul_rn(__dsub_rn(rt[3 * ii], 1.0), DXv), DYv);
-        b[3 * ii + 1] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 1], DXv), DYv), 12.);
-        b[3 * ii + 2] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 2], DXv), DYv), 12.);
+        if (!fast) {
+            b[3 * ii] = __dmul_rn(__dmul_rn(__dsub_rn(rt[3 * ii], 1.0), DXv), DYv);
+            b[3 * ii + 1] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 1], DXv), DYv), 12.);
+            b[3 * ii + 2] = __ddiv_rn(__dmul_rn(__dmul_rn(rt[3 * ii + 2], DXv), DYv), 12.);
+        } else {
+            double r0 = 0., r1 = 0., r2 = 0.;
+            const double *pp = rt + 3 * (long long)ii * npart;
+            for (int p = 0; p < npart; ++p) { r0 += pp[3 * p]; r1 += pp[3 * p + 1]; r2 += pp[3 * p + 2]; }
+            b[3 * ii] = (r0 * pd.cscale - 1.0) * DXv * DYv;
+            b[3 * ii + 1] = r1 * pd.cscale * DXv * DYv * (1. / 12.);
+            b[3 * ii + 2] = r2 * pd.cscale * DXv * DYv * (1. / 12.);
+        }
     }
     __syncthreads();
     const int ldab = pd.ldab;
-#define ABD(i, j) pd.ab[((i) - 1) + (long long)((j) - 1) * ldab]
+#define ABD(i, j) AB[((i) - 1) + (long long)((j) - 1) * ldab]
     if (t < 32) {
         const int kd = pd.ku + pd.kl + 1;
         for (int j = 1; j <= nd - 1; ++j) {
             const int lm = min(pd.kl, nd - j);
-            const int l = pd.ipiv[j - 1];
+            const int l = spiv[j - 1];
             if (t == 0 && l != j) { const double tmp = b[l - 1]; b[l - 1] = b[j - 1]; b[j - 1] = tmp; }
             __syncwarp();
             const double bj = b[j - 1];
@@ -864,7 +938,7 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *
             __syncwarp();
             if (bj != 0.0) {
                 const int l = kplus1 - j;
-                const double xj = __ddiv_rn(bj, ABD(kplus1, j));
+                const double xj = fast ? bj * pd.rdiag[j - 1] : __ddiv_rn(bj, ABD(kplus1, j));
                 const int ilo = max(1, j - k);
                 for (int i = j - 1 - t; i >= ilo; i -= 32) b[i - 1] = __dsub_rn(b[i - 1], __dmul_rn(xj, ABD(l + i, j)));
                 if (t == 0) b[j - 1] = xj;
@@ -878,6 +952,8 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *
     __syncthreads();
     const double *acvx = pd.blk[0], *acyrr = pd.blk[1], *acyrl = pd.blk[2];
     const double *acvy = pd.blk[3], *acxrr = pd.blk[4], *acxrl = pd.blk[5];
+    const double rdxp = pd.rdxp, rdyp = pd.rdyp;
+    auto div = [&](double a, double d, double rd) { return fast ? a * rd : __ddiv_rn(a, d); };
     for (int ii = t; ii < nc; ii += blockDim.x) {
         const int ix = ii / pd.ny + 1, jy = ii % pd.ny + 1;
         const int il = ii - pd.ny, ib = ii - 1;
@@ -895,12 +971,12 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *
                     s = __dsub_rn(__dadd_rn(s, __dmul_rn(__dadd_rn(acvx[3 * k + kk], acyrr[3 * k + kk]), b[3 * ii + kk])),
                                   __dmul_rn(acyrl[3 * k + kk], b[3 * il + kk]));
             }
-            phix[3 * ii + k] = __ddiv_rn(-s, pd.dxp);
+            phix[3 * ii + k] = div(-s, pd.dxp, rdxp);
         }
         for (int k = 0; k < 3; ++k) {  // E_y
             double s = 0.;
             if (jy == 1) {
-                phiy[3 * ii + k] = (k == 0) ? __ddiv_rn(-b[3 * ii + 2], pd.dyp) : 0.;
+                phiy[3 * ii + k] = (k == 0) ? div(-b[3 * ii + 2], pd.dyp, rdyp) : 0.;
                 continue;
             }
             if (jy == pd.ny && pd.gate[ix]) {
@@ -912,122 +988,126 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, double *
                     s = __dsub_rn(__dadd_rn(s, __dmul_rn(__dadd_rn(acvy[3 * k + kk], acxrr[3 * k + kk]), b[3 * ii + kk])),
                                   __dmul_rn(acxrl[3 * k + kk], b[3 * ib + kk]));
             }
-            phiy[3 * ii + k] = __ddiv_rn(-s, pd.dyp);
+            phiy[3 * ii + k] = div(-s, pd.dyp, rdyp);
         }
         // cell integrals of the field
         const double ex0 = phix[3 * ii], ex1 = phix[3 * ii + 1], ex2 = phix[3 * ii + 2];
         const double ey0 = phiy[3 * ii], ey1 = phiy[3 * ii + 1], ey2 = phiy[3 * ii + 2];
+        constexpr double r12 = 1. / 12.;
         fields[0 * nc + ii] = ex0;
-        fields[1 * nc + ii] = __ddiv_rn(ex1, 12.);
-        fields[2 * nc + ii] = __ddiv_rn(ex2, 12.);
-        fields[3 * nc + ii] = __ddiv_rn(ex0, 12.);
+        fields[1 * nc + ii] = div(ex1, 12., r12);
+        fields[2 * nc + ii] = div(ex2, 12., r12);
+        fields[3 * nc + ii] = div(ex0, 12., r12);
         fields[4 * nc + ii] = 0.;
-        fields[5 * nc + ii] = __ddiv_rn(ex0, 12.);
+        fields[5 * nc + ii] = div(ex0, 12., r12);
         fields[6 * nc + ii] = ey0;
-        fields[7 * nc + ii] = __ddiv_rn(ey1, 12.);
-        fields[8 * nc + ii] = __ddiv_rn(ey2, 12.);
-        fields[9 * nc + ii] = __ddiv_rn(ey0, 12.);
+        fields[7 * nc + ii] = div(ey1, 12., r12);
+        fields[8 * nc + ii] = div(ey2, 12., r12);
+        fields[9 * nc + ii] = div(ey0, 12., r12);
         fields[10 * nc + ii] = 0.;
-        fields[11 * nc + ii] = __ddiv_rn(ey0, 12.);
+        fields[11 * nc + ii] = div(ey0, 12., r12);
         fields[12 * nc + ii] = ex0 > 0. ? 1. : -1.;
         fields[13 * nc + ii] = ey0 > 0. ? 1. : -1.;
     }
 }
 
 // ---------------------------------------------------------------- advection
-// Right-hand side H of one record (I1, I2, I3, I5 at A:213-405 combined as at
-// A:455-467; H[2] = 0) and the SSP-RK3 stage (A:469, A:527, A:581).
-__global__ void k_flux(AdvectDev ad, const double *__restrict__ U0, const double *__restrict__ Us,
-                       const double *__restrict__ fields, int stage, double *__restrict__ Uout) {
-    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (k >= ad.size) return;
+// Right-hand side H of record k (I1, I2, I3, I5 at A:213-405 combined as at
+// A:455-467; H[2] = 0) in arithmetic T from stage values of type S.  Constant
+// divisions are products with reciprocals (within 2 ulp of the reference's).
+template <typename T, typename S>
+__device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restrict__ Us,
+                                         const double *__restrict__ fields, long long k, T H[7]) {
     const int nv = ad.nv;
     const long long sv = (long long)nv * nv * nv;
     const long long jm = k % sv, s = k / sv;
     const int j3 = (int)(jm % nv), j2 = (int)((jm / nv) % nv), j1 = (int)(jm / ((long long)nv * nv));
     const int i2 = (int)(s % ad.nx2), i1 = (int)(s / ad.nx2);
-    const double dv = ad.dv;
-    const double G = -ad.lv + (j1 + 0.5) * dv;
-    const double *u = Us + 7 * k;
-    constexpr double i12 = 1. / 12., i720_19 = 19. / 720., i240_19 = 19. / 240., i5_12 = 5. / 12.,
-                     i720_133 = 133. / 720., i6 = 1. / 6.;
+    const T dv = (T)ad.dv, rdv = (T)ad.rdv;
+    const T G = (T)(-ad.lv + (j1 + 0.5) * ad.dv);
+    const T i12 = T(1. / 12.), i720_19 = T(19. / 720.), i240_19 = T(19. / 240.), i5_12 = T(5. / 12.),
+            i720_133 = T(133. / 720.), i6 = T(1. / 6.), h = T(0.5), q4 = T(0.25);
+    T u[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) u[q] = (T)Us[7 * k + q];
     // x1 upwind neighbours by the sign of v1, periodic (I3).
-    long long kr3, kl3;
-    double ur3, ul3;
+    T R3[7], L3[7], ur3, ul3;
     if (j1 < nv / 2) {
         int iir = i1 + 1;
         if (iir == ad.nx1) iir = 0;
-        kr3 = (long long)iir * ad.nx2 * sv + (long long)i2 * sv + jm;
-        kl3 = k;
-        ur3 = -Us[kr3 * 7 + 1];
-        ul3 = -Us[kl3 * 7 + 1];
+        const long long kr3 = (long long)iir * ad.nx2 * sv + (long long)i2 * sv + jm;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) { R3[q] = (T)Us[7 * kr3 + q]; L3[q] = u[q]; }
+        ur3 = -R3[1];
+        ul3 = -L3[1];
     } else {
         int iil = i1 - 1;
         if (iil == -1) iil = ad.nx1 - 1;
-        kr3 = k;
-        kl3 = (long long)iil * ad.nx2 * sv + (long long)i2 * sv + jm;
-        ur3 = Us[kr3 * 7 + 1];
-        ul3 = Us[kl3 * 7 + 1];
+        const long long kl3 = (long long)iil * ad.nx2 * sv + (long long)i2 * sv + jm;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) { L3[q] = (T)Us[7 * kl3 + q]; R3[q] = u[q]; }
+        ur3 = R3[1];
+        ul3 = L3[1];
     }
-    const double *R3 = Us + 7 * kr3, *L3 = Us + 7 * kl3;
     // v1 upwind neighbours by the sign of the cell-average E_x, no inflow (I5).
     const long long nc = (long long)ad.nx1 * ad.nx2;
-    const double ie = fields[s], ixe = fields[nc + s], ixxe = fields[3 * nc + s];
-    int j1r, j1l;
-    long long kr5, kl5;
-    double ur5 = 0., ul5 = 0.;
-    if (ie > 0) {
-        j1r = j1 + 1; j1l = j1;
-        kr5 = s * sv + ((long long)j1r * nv * nv + j2 * nv + j3);
-        kl5 = k;
-        if (j1r < nv) ur5 = -Us[kr5 * 7 + 3];
-        ul5 = -Us[kl5 * 7 + 3];
+    const double ie_d = fields[s];
+    const T ie = (T)ie_d, ixe = (T)fields[nc + s], ixxe = (T)fields[3 * nc + s];
+    T R5[7], L5[7], ur5 = T(0), ul5 = T(0);
+    bool hasr, hasl;
+    if (ie_d > 0) {
+        hasr = j1 + 1 < nv;
+        hasl = true;
+        const long long kr5 = s * sv + ((long long)(j1 + 1) * nv * nv + j2 * nv + j3);
+#pragma unroll
+        for (int q = 0; q < 7; ++q) { R5[q] = hasr ? (T)Us[7 * kr5 + q] : T(0); L5[q] = u[q]; }
+        if (hasr) ur5 = -R5[3];
+        ul5 = -L5[3];
     } else {
-        j1r = j1; j1l = j1 - 1;
-        kr5 = k;
-        kl5 = s * sv + ((long long)j1l * nv * nv + j2 * nv + j3);
-        ur5 = Us[kr5 * 7 + 3];
-        if (j1l > -1) ul5 = Us[kl5 * 7 + 3];
+        hasr = true;
+        hasl = j1 - 1 > -1;
+        const long long kl5 = s * sv + ((long long)(j1 - 1) * nv * nv + j2 * nv + j3);
+#pragma unroll
+        for (int q = 0; q < 7; ++q) { L5[q] = hasl ? (T)Us[7 * kl5 + q] : T(0); R5[q] = u[q]; }
+        ur5 = R5[3];
+        if (hasl) ul5 = L5[3];
     }
-    const bool hasr = j1r < nv, hasl = j1l > -1;
-    double R5[7] = {0, 0, 0, 0, 0, 0, 0}, L5[7] = {0, 0, 0, 0, 0, 0, 0};
-    if (hasr) for (int q = 0; q < 7; ++q) R5[q] = Us[kr5 * 7 + q];
-    if (hasl) for (int q = 0; q < 7; ++q) L5[q] = Us[kl5 * 7 + q];
-    const double dv2 = dv * dv, dv3 = dv * dv * dv;
-    double tp[6];
+    const T dv2 = dv * dv, dv3 = dv * dv * dv;
+    T tp[6];
     // l = 0
     {
-        double i3 = dv3 * ((R3[0] + 0.5 * ur3 - L3[0] - 0.5 * ul3) * G + (R3[3] - L3[3]) * dv * i12 + (R3[6] - L3[6]) * G * 0.25);
-        double i5 = 0.;
-        if (hasr && hasl) i5 = dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12 - L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ie + dv2 * (R5[1] - L5[1]) * ixe;
-        else if (hasr) i5 = dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe;
-        else if (hasl) i5 = dv2 * (-L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ie - dv2 * L5[1] * ixe;
+        T i3 = dv3 * ((R3[0] + h * ur3 - L3[0] - h * ul3) * G + (R3[3] - L3[3]) * dv * i12 + (R3[6] - L3[6]) * G * q4);
+        T i5 = T(0);
+        if (hasr && hasl) i5 = dv2 * (R5[0] + h * ur5 + R5[6] * i5_12 - L5[0] - h * ul5 - L5[6] * i5_12) * ie + dv2 * (R5[1] - L5[1]) * ixe;
+        else if (hasr) i5 = dv2 * (R5[0] + h * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe;
+        else if (hasl) i5 = dv2 * (-L5[0] - h * ul5 - L5[6] * i5_12) * ie - dv2 * L5[1] * ixe;
         tp[0] = -i3 + i5;
     }
     // l = 1
     {
-        double i1v = dv3 * (G * u[0] + dv * u[3] * i12 + u[6] * G * 0.25);
-        double i3 = 0.5 * dv3 * ((R3[0] + 0.5 * ur3 + L3[0] + 0.5 * ul3) * G + (R3[3] + L3[3]) * dv * i12 + (R3[6] + L3[6]) * G * 0.25);
-        double i5 = 0.;
-        if (hasr && hasl) i5 = dv2 * ((R5[0] + 0.5 * ur5 + R5[6] * i5_12 - L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ixe + (R5[1] - L5[1]) * ixxe);
-        else if (hasr) i5 = dv2 * ((R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ixe + R5[1] * ixxe);
-        else if (hasl) i5 = dv2 * ((-L5[0] - 0.5 * ul5 - L5[6] * i5_12) * ixe - L5[1] * ixxe);
+        T i1v = dv3 * (G * u[0] + dv * u[3] * i12 + u[6] * G * q4);
+        T i3 = h * dv3 * ((R3[0] + h * ur3 + L3[0] + h * ul3) * G + (R3[3] + L3[3]) * dv * i12 + (R3[6] + L3[6]) * G * q4);
+        T i5 = T(0);
+        if (hasr && hasl) i5 = dv2 * ((R5[0] + h * ur5 + R5[6] * i5_12 - L5[0] - h * ul5 - L5[6] * i5_12) * ixe + (R5[1] - L5[1]) * ixxe);
+        else if (hasr) i5 = dv2 * ((R5[0] + h * ur5 + R5[6] * i5_12) * ixe + R5[1] * ixxe);
+        else if (hasl) i5 = dv2 * ((-L5[0] - h * ul5 - L5[6] * i5_12) * ixe - L5[1] * ixxe);
         tp[1] = i1v - i3 + i5;
     }
     // l = 3 (v1 slope)
     {
-        double i2 = (((u[0] + u[6] * 0.25) * ie + u[1] * ixe) * ad.scalev) / dv;
-        double i3 = dv2 * (((R3[0] - L3[0]) * dv2 + (ur3 - ul3) * 0.5 * dv2 + (R3[3] - L3[3]) * dv * G) * i12 + (R3[6] - L3[6]) * dv2 * i720_19);
-        double i5 = 0.;
-        if (hasr && hasl) i5 = 0.5 * (dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12 + L5[0] + 0.5 * ul5 + L5[6] * i5_12) * ie + dv2 * (R5[1] + L5[1]) * ixe);
-        else if (hasr) i5 = 0.5 * (dv2 * (R5[0] + 0.5 * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe);
-        else if (hasl) i5 = 0.5 * (dv2 * (L5[0] + 0.5 * ul5 + L5[6] * i5_12) * ie + dv2 * L5[1] * ixe);
+        T i2 = (((u[0] + u[6] * q4) * ie + u[1] * ixe) * (T)ad.scalev) * rdv;
+        T i3 = dv2 * (((R3[0] - L3[0]) * dv2 + (ur3 - ul3) * h * dv2 + (R3[3] - L3[3]) * dv * G) * i12 + (R3[6] - L3[6]) * dv2 * i720_19);
+        T i5 = T(0);
+        if (hasr && hasl) i5 = h * (dv2 * (R5[0] + h * ur5 + R5[6] * i5_12 + L5[0] + h * ul5 + L5[6] * i5_12) * ie + dv2 * (R5[1] + L5[1]) * ixe);
+        else if (hasr) i5 = h * (dv2 * (R5[0] + h * ur5 + R5[6] * i5_12) * ie + dv2 * R5[1] * ixe);
+        else if (hasl) i5 = h * (dv2 * (L5[0] + h * ul5 + L5[6] * i5_12) * ie + dv2 * L5[1] * ixe);
         tp[2] = -i2 - i3 + i5;
     }
     // l = 4, 5 (v2, v3 slopes)
+#pragma unroll
     for (int q = 4; q <= 5; ++q) {
-        double i3 = (R3[q] - L3[q]) * G * dv3 * i12;
-        double i5 = 0.;
+        T i3 = (R3[q] - L3[q]) * G * dv3 * i12;
+        T i5 = T(0);
         if (hasr && hasl) i5 = (R5[q] - L5[q]) * ie * dv2 * i12;
         else if (hasr) i5 = R5[q] * ie * dv2 * i12;
         else if (hasl) i5 = -L5[q] * ie * dv2 * i12;
@@ -1035,34 +1115,252 @@ __global__ void k_flux(AdvectDev ad, const double *__restrict__ U0, const double
     }
     // l = 6 (|v|^2 mode)
     {
-        double i2 = u[3] * dv2 * ie * i6;
-        double i3 = dv3 * ((R3[0] + 0.5 * ur3 - L3[0] - 0.5 * ul3) * G * 0.25 + (R3[3] - L3[3]) * dv * i720_19 + (R3[6] - L3[6]) * G * i240_19);
-        double i5 = 0.;
-        if (hasr && hasl) i5 = dv2 * (((R5[0] + 0.5 * ur5 - L5[0] - 0.5 * ul5) * i5_12 + (R5[6] - L5[6]) * i720_133) * ie + (R5[1] - L5[1]) * ixe * i5_12);
-        else if (hasr) i5 = dv2 * (((R5[0] + 0.5 * ur5) * i5_12 + R5[6] * i720_133) * ie + R5[1] * ixe * i5_12);
-        else if (hasl) i5 = -dv2 * (((L5[0] + 0.5 * ul5) * i5_12 + L5[6] * i720_133) * ie + L5[1] * ixe * i5_12);
+        T i2 = u[3] * dv2 * ie * i6;
+        T i3 = dv3 * ((R3[0] + h * ur3 - L3[0] - h * ul3) * G * q4 + (R3[3] - L3[3]) * dv * i720_19 + (R3[6] - L3[6]) * G * i240_19);
+        T i5 = T(0);
+        if (hasr && hasl) i5 = dv2 * (((R5[0] + h * ur5 - L5[0] - h * ul5) * i5_12 + (R5[6] - L5[6]) * i720_133) * ie + (R5[1] - L5[1]) * ixe * i5_12);
+        else if (hasr) i5 = dv2 * (((R5[0] + h * ur5) * i5_12 + R5[6] * i720_133) * ie + R5[1] * ixe * i5_12);
+        else if (hasl) i5 = -dv2 * (((L5[0] + h * ul5) * i5_12 + L5[6] * i720_133) * ie + L5[1] * ixe * i5_12);
         tp[5] = -i2 - i3 + i5;
     }
-    const double inv = 1.0 / ad.dx / ad.scalev;
-    double H[7];
-    H[0] = (19 * tp[0] * 0.25 - 15 * tp[5]) * inv;
-    H[6] = (60 * tp[5] - 15 * tp[0]) * inv;
-    H[1] = tp[1] * 12. * inv;
-    H[2] = 0.;
-    H[3] = tp[2] * 12. * inv;
-    H[4] = tp[3] * 12. * inv;
-    H[5] = tp[4] * 12. * inv;
-    const double dt = ad.dt;
-    const double *u0 = U0 + 7 * k;
-    double *o = Uout + 7 * k;
+    const T inv = (T)ad.inv, c12 = T(12);
+    H[0] = (T(19) * tp[0] * q4 - T(15) * tp[5]) * inv;
+    H[6] = (T(60) * tp[5] - T(15) * tp[0]) * inv;
+    H[1] = tp[1] * c12 * inv;
+    H[2] = T(0);
+    H[3] = tp[2] * c12 * inv;
+    H[4] = tp[3] * c12 * inv;
+    H[5] = tp[4] * c12 * inv;
+}
+
+// One SSP-RK3 stage (A:469, A:527, A:581): H from the stage values Uin (type
+// S, evaluated in T), the combination with U0 and Us in FP64.  Optionally
+// writes an FP32 copy of the result (the next stage's Uin) and the charge
+// partial sums of the result per block of 128 records (the next Poisson
+// solve's right-hand side); both need the records of a block to belong to
+// one spatial cell (nv^3 a multiple of 128).
+template <typename T, typename S>
+__global__ void __launch_bounds__(128) k_flux(AdvectDev ad, const double *__restrict__ U0, const double *__restrict__ Us,
+                                             const S *__restrict__ Uin, const double *__restrict__ fields, int stage,
+                                             double *__restrict__ Uout, float *__restrict__ Uoutf,
+                                             double *__restrict__ part) {
+    const long long k = blockIdx.x * 128ll + threadIdx.x;
+    double a0 = 0., a1 = 0., a2 = 0.;
+    if (k < ad.size) {
+        T H[7];
+        flux_rhs<T, S>(ad, Uin, fields, k, H);
+        const double dt = ad.dt;
+        const double *u0 = U0 + 7 * k, *u = Us + 7 * k;
+        double r[7];
 #pragma unroll
-    for (int l = 0; l < 7; ++l) {
-        double r;
-        if (stage == 0) r = u0[l] + dt * H[l];
-        else if (stage == 1) r = 0.75 * u0[l] + 0.25 * u[l] + 0.25 * dt * H[l];
-        else r = u0[l] / 3. + u[l] * 2. / 3. + dt * H[l] * 2. / 3.;
-        o[l] = r;
+        for (int l = 0; l < 7; ++l) {
+            const double hl = (double)H[l];
+            if (stage == 0) r[l] = u0[l] + dt * hl;
+            else if (stage == 1) r[l] = 0.75 * u0[l] + 0.25 * u[l] + 0.25 * dt * hl;
+            else r[l] = u0[l] * (1. / 3.) + u[l] * (2. / 3.) + dt * hl * (2. / 3.);
+        }
+        double *o = Uout + 7 * k;
+#pragma unroll
+        for (int l = 0; l < 7; ++l) o[l] = r[l];
+        if (Uoutf) {
+#pragma unroll
+            for (int l = 0; l < 7; ++l) Uoutf[7 * k + l] = (float)r[l];
+        }
+        a0 = r[0] + 0.25 * r[6]; a1 = r[1]; a2 = r[2];
     }
+    if (part) charge_block_sum(a0, a1, a2, part);
+}
+
+// ---------------------------------------------------------------- mixed-path advection
+// FP64 <-> FP32 conversions by bit manipulation, so that the stage copies of
+// the mixed path do not occupy the narrow FP64 unit: FP64 -> FP32 truncates
+// toward zero (within one FP32 ulp) and flushes magnitudes below the FP32
+// normal range to signed zero; FP32 -> FP64 is exact for normal numbers and
+// zero (FP32 subnormals become signed zero).
+__device__ __forceinline__ float f64_to_f32_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned u = __float_as_uint(f), sign = u & 0x80000000u, e = (u >> 23) & 0xffu;
+    if (e == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
+    const unsigned long long ee = e == 255 ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double(
+        (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// FP32 copy of the state and the FP64 charge moments of every group of 128
+// consecutive records (one warp per group, four records per lane):
+// part[3 * group] = (sum U0 + U6/4, sum U1, sum U2).
+__global__ void __launch_bounds__(128) k_state_f32_grp(const double *__restrict__ U, long long size,
+                                                      float *__restrict__ Uf, double *__restrict__ part) {
+    const int lane = threadIdx.x & 31;
+    const long long g = blockIdx.x * 4ll + (threadIdx.x >> 5);
+    double a0 = 0., a1 = 0., a2 = 0.;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const long long k = g * 128 + j * 32 + lane;
+        if (k < size) {
+            const double *u = U + 7 * k;
+            double v[7];
+#pragma unroll
+            for (int l = 0; l < 7; ++l) { v[l] = u[l]; Uf[7 * k + l] = f64_to_f32_bits(v[l]); }
+            a0 += v[0] + 0.25 * v[6]; a1 += v[1]; a2 += v[2];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0 && g * 128 < size) { part[3 * g] = a0; part[3 * g + 1] = a1; part[3 * g + 2] = a2; }
+}
+
+// Mixed path, increment form of SSP-RK3 (the reference's stages A:469-581 in
+// exact arithmetic): with H_s = H(U_s) evaluated in FP32,
+//   U1 = U + dt H0,   U2 = U + dt/4 (H0 + H1),   U_new = U + dt/6 (H0 + H1 + 4 H2).
+// Stages 0 and 1 read the FP32 copy of U_s (own and neighbour records), keep
+// the running FP32 sum S of the H's, write the FP32 copy Uf0 + c S of the next
+// stage's values and the FP32 sums of S over every group of 128 records (the
+// charge moments are linear: rho(U_{s+1}) = rho(U) + c sum S).  Only stage 2
+// touches the FP64 state: U += dt/6 (S + 4 H2).
+template <int STAGE>
+__global__ void __launch_bounds__(128) k_flux_inc(AdvectDev ad, const float *__restrict__ Uin,
+                                                 const float *__restrict__ Uf0, const double *__restrict__ fields,
+                                                 float *__restrict__ S, float *__restrict__ Uoutf,
+                                                 double *__restrict__ U, float *__restrict__ ipart) {
+    const long long k = blockIdx.x * 128ll + threadIdx.x;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    if (k < ad.size) {
+        float H[7];
+        flux_rhs<float, float>(ad, Uin, fields, k, H);
+        if (STAGE < 2) {
+            const float c = STAGE == 0 ? ad.dt_f : 0.25f * ad.dt_f;
+            float s[7];
+#pragma unroll
+            for (int l = 0; l < 7; ++l) {
+                s[l] = STAGE == 0 ? H[l] : S[7 * k + l] + H[l];
+                S[7 * k + l] = s[l];
+                Uoutf[7 * k + l] = Uf0[7 * k + l] + c * s[l];
+            }
+            a0 = s[0] + 0.25f * s[6]; a1 = s[1]; a2 = s[2];
+        } else {
+            double *u = U + 7 * k;
+#pragma unroll
+            for (int l = 0; l < 7; ++l) u[l] += ad.dt6 * f32_to_f64_bits(S[7 * k + l] + 4.f * H[l]);
+        }
+    }
+    if (STAGE < 2) {
+        __shared__ float red[3][4];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        }
+        const int t = threadIdx.x;
+        if ((t & 31) == 0) { red[0][t >> 5] = a0; red[1][t >> 5] = a1; red[2][t >> 5] = a2; }
+        __syncthreads();
+        if (t < 3) ipart[3 * (long long)blockIdx.x + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
+    }
+}
+
+// Mixed-path Poisson solve in three kernels: the right-hand side from the
+// group partials (one warp per cell), x = A^-1 b with the dense inverse of
+// the LDG matrix (one warp per row), and the field reconstruction and cell
+// integrals (one thread per cell; pois2d P:1292-1467).
+__global__ void k_prhs(PoissonDev pd, const double *__restrict__ base, const float *__restrict__ inc,
+                       double iscale, int npart, double *__restrict__ b) {
+    const int lane = threadIdx.x & 31;
+    const int ii = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (ii >= pd.nx * pd.ny) return;
+    double r[3] = {0., 0., 0.}, d[3] = {0., 0., 0.};
+    for (int p = lane; p < npart; p += 32)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            r[m] += base[3 * ((long long)ii * npart + p) + m];
+            if (inc) d[m] += (double)inc[3 * ((long long)ii * npart + p) + m];
+        }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        double v = r[m] + iscale * d[m];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        r[m] = v * pd.cscale;
+    }
+    if (lane == 0) {
+        const double DXv = pd.dxp, DYv = pd.dyp;
+        b[3 * ii] = (r[0] - 1.0) * DXv * DYv;
+        b[3 * ii + 1] = r[1] * DXv * DYv * (1. / 12.);
+        b[3 * ii + 2] = r[2] * DXv * DYv * (1. / 12.);
+    }
+}
+
+__global__ void k_psolve_dense(const double *__restrict__ Ainv, const double *__restrict__ b, int nd,
+                               double *__restrict__ x) {
+    const int lane = threadIdx.x & 31;
+    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= nd) return;
+    const double *a = Ainv + (long long)row * nd;
+    double s = 0.;
+    for (int j = lane; j < nd; j += 32) s += a[j] * b[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = s;
+}
+
+__global__ void k_pfields(PoissonDev pd, const double *__restrict__ b, double *__restrict__ phix,
+                          double *__restrict__ phiy, double *__restrict__ fields) {
+    const int nc = pd.nx * pd.ny;
+    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ii >= nc) return;
+    const double *acvx = pd.blk[0], *acyrr = pd.blk[1], *acyrl = pd.blk[2];
+    const double *acvy = pd.blk[3], *acxrr = pd.blk[4], *acxrl = pd.blk[5];
+    const int ix = ii / pd.ny + 1, jy = ii % pd.ny + 1;
+    const int il = ii - pd.ny, ib = ii - 1;
+    double ex[3], ey[3];
+    for (int k = 0; k < 3; ++k) {  // E_x
+        double s = 0.;
+        for (int kk = 0; kk < 3; ++kk) {
+            const double bc = b[3 * ii + kk];
+            if (ix == 1) s += (acvx[3 * k + kk] + acyrr[3 * k + kk]) * bc;
+            else if (ix == pd.nx) s += acvx[3 * k + kk] * bc - acyrl[3 * k + kk] * b[3 * il + kk];
+            else s += (acvx[3 * k + kk] + acyrr[3 * k + kk]) * bc - acyrl[3 * k + kk] * b[3 * il + kk];
+        }
+        ex[k] = -s * pd.rdxp;
+    }
+    for (int k = 0; k < 3; ++k) {  // E_y
+        if (jy == 1) { ey[k] = (k == 0) ? -b[3 * ii + 2] * pd.rdyp : 0.; continue; }
+        double s = 0.;
+        const bool top = (jy == pd.ny && pd.gate[ix]);
+        for (int kk = 0; kk < 3; ++kk) {
+            const double bc = b[3 * ii + kk];
+            if (top) s += acvy[3 * k + kk] * bc - acxrl[3 * k + kk] * b[3 * ib + kk];
+            else s += (acvy[3 * k + kk] + acxrr[3 * k + kk]) * bc - acxrl[3 * k + kk] * b[3 * ib + kk];
+        }
+        ey[k] = -s * pd.rdyp;
+    }
+    constexpr double r12 = 1. / 12.;
+    for (int k = 0; k < 3; ++k) { phix[3 * ii + k] = ex[k]; phiy[3 * ii + k] = ey[k]; }
+    fields[0 * nc + ii] = ex[0];
+    fields[1 * nc + ii] = ex[1] * r12;
+    fields[2 * nc + ii] = ex[2] * r12;
+    fields[3 * nc + ii] = ex[0] * r12;
+    fields[4 * nc + ii] = 0.;
+    fields[5 * nc + ii] = ex[0] * r12;
+    fields[6 * nc + ii] = ey[0];
+    fields[7 * nc + ii] = ey[1] * r12;
+    fields[8 * nc + ii] = ey[2] * r12;
+    fields[9 * nc + ii] = ey[0] * r12;
+    fields[10 * nc + ii] = 0.;
+    fields[11 * nc + ii] = ey[0] * r12;
+    fields[12 * nc + ii] = ex[0] > 0. ? 1. : -1.;
+    fields[13 * nc + ii] = ey[0] > 0. ? 1. : -1.;
 }
 
 // ---------------------------------------------------------------- FMA peaks
@@ -1166,12 +1464,13 @@ cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t
 
 template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2, const R *M, int n,
-                            int Bp, int stage, double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st) {
+                            int Bp, int stage, double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st,
+                            Rates rates) {
     using C = typename V2<R>::t;
     cudaError_t e;
     if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
     if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st);
+    return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
 }
 
 template <typename R>
@@ -1203,6 +1502,19 @@ template <int N> long long lines_offsets(std::vector<long long> &line_off) {
         const int ni = i < h ? i + h + 1 : 3 * h - 1 - i, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
         line_off[ij + 1] = line_off[ij] + (long long)((ni * nj + 1) / 2) * TP;
     }
+    // then the lines in order of decreasing plane-pair count: blocks are
+    // dispatched longest first, so the last wave holds the short lines
+    std::vector<int> order(N * N);
+    for (int ij = 0; ij < N * N; ++ij) order[ij] = ij;
+    std::stable_sort(order.begin(), order.end(), [](int a, int b) {
+        auto npp = [](int ij) {
+            const int i = ij / N, j = ij % N;
+            const int ni = i < h ? i + h + 1 : 3 * h - 1 - i, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+            return (ni * nj + 1) / 2;
+        };
+        return npp(a) > npp(b);
+    });
+    for (int r = 0; r < N * N; ++r) line_off.push_back(order[r]);
     return line_off[(size_t)N * N];
 }
 }  // namespace
@@ -1230,33 +1542,41 @@ cudaError_t launch_lines_table(const double *eta, const double *shat, const doub
 }
 
 namespace {
-template <int N, int T>
+template <int N, int T, int LW>
 void launch_tiles(const float2 *F, const float *W, const long long *line_off, int Bp, double2 *q, cudaStream_t st) {
     constexpr int NT = N / LinesCfg<N>::KT;
     if constexpr (T < NT) {
         const unsigned blocks = (unsigned)((long long)N * N * (Bp / 32));
-        constexpr size_t smem = lines_smem_bytes<N, T>();
+        constexpr size_t smem = lines_smem_bytes<N, T, LW>();
         static bool attr_set = false;  // one attribute call per instantiation
         if (!attr_set) {
-            cudaFuncSetAttribute(k_cq_lines<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_cq_lines<N, T, LW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr_set = true;
         }
-        k_cq_lines<N, T><<<blocks, 32 * kLineWarps, smem, st>>>(F, W, line_off, Bp, q);
-        launch_tiles<N, T + 1>(F, W, line_off, Bp, q, st);
+        k_cq_lines<N, T, LW><<<blocks, 32 * LW, smem, st>>>(F, W, line_off, Bp, q);
+        launch_tiles<N, T + 1, LW>(F, W, line_off, Bp, q, st);
     }
+}
+
+template <int LW>
+cudaError_t computeq_lines(const float2 *F, const float *W, const long long *line_off, int n, int Bp, double2 *q,
+                           cudaStream_t st) {
+    switch (n) {
+    case 8: launch_tiles<8, 0, LW>(F, W, line_off, Bp, q, st); break;
+    case 16: launch_tiles<16, 0, LW>(F, W, line_off, Bp, q, st); break;
+    case 24: launch_tiles<24, 0, LW>(F, W, line_off, Bp, q, st); break;
+    case 32: launch_tiles<32, 0, LW>(F, W, line_off, Bp, q, st); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 }  // namespace
 
 cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n, int Bp,
-                                  double2 *q, cudaStream_t st) {
-    switch (n) {
-    case 8: launch_tiles<8, 0>(F, W, line_off, Bp, q, st); break;
-    case 16: launch_tiles<16, 0>(F, W, line_off, Bp, q, st); break;
-    case 24: launch_tiles<24, 0>(F, W, line_off, Bp, q, st); break;
-    case 32: launch_tiles<32, 0>(F, W, line_off, Bp, q, st); break;
-    default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+                                  double2 *q, cudaStream_t st, int warps) {
+    if (warps == 4) return computeq_lines<4>(F, W, line_off, n, Bp, q, st);
+    if (warps == 2) return computeq_lines<2>(F, W, line_off, n, Bp, q, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
@@ -1272,27 +1592,28 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
                            const R *tfac, int n, int nv, int Bp, int B, int c0, const double *U, int ustride,
                            const int *uslot, double dt, double scalev, double scaleL, double scale3,
                            typename V2<R>::t *Qc, typename V2<R>::t *Y, typename V2<R>::t *Z, double *dU,
-                           cudaStream_t st) {
-    const long long n3 = (long long)n * n * n, nv3 = (long long)nv * nv * nv;
-    k_qcomb<R><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Qc);
+                           cudaStream_t st, Rates rates) {
+    const long long n3 = (long long)n * n * n;
+    k_qcomb<R><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Bp, rates.nu, Qc);
     const int nch = (nv + JB - 1) / JB;
     k_proj3<R><<<grid1((long long)n * n * nch * Bp, 128), 128, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
     k_proj2<R><<<grid1((long long)n * nv * nch * Bp, 128), 128, 0, st>>>(Y, tfac, n, nv, Bp, Z);
     const double kfac = 1. / scalev / scaleL / scale3;
     int4 us = make_int4(uslot[0], uslot[1], uslot[2], uslot[3]);
     k_proj1<R><<<grid1((long long)nv * nv * nch * Bp, 128), 128, 0, st>>>(Z, tfac, n, nv, Bp, B, c0, U, ustride, us,
-                                                                             uslot[4], dt, kfac, dU);
+                                                                             uslot[4], dt, kfac, rates.dt, dU);
     return cudaGetLastError();
 }
 
 cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
                               double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
                               const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
-                              double *apart, const double *gm_inv, double scale, double *lam, double *dU,
-                              cudaStream_t st) {
-    k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, gmom, n3, Bp, nchunk, tpart);
+                              double *apart, const double *gm_inv, double scale, double kfac, double *lam,
+                              double *dU, cudaStream_t st, Rates rates) {
+    k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, rates.nu, gmom, n3, Bp, nchunk,
+                                                               tpart);
     k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, c0, nrc, apart);
-    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, B, Bp, lam);
+    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, kfac, rates.dt, B, Bp, lam);
     const long long nrec = (long long)B * nv * nv * nv;
     k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, nrec);
     return cudaGetLastError();
@@ -1305,24 +1626,66 @@ cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, 
 }
 
 cudaError_t launch_charge(const double *U, int ncell, int nv3, double scalev, double *rt, cudaStream_t st) {
-    k_charge<<<ncell, 256, 0, st>>>(U, nv3, scalev, rt);
+    k_charge_seq<<<ncell, 256, 0, st>>>(U, nv3, scalev, rt);
     return cudaGetLastError();
 }
 
-cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, double *b, double *potc, double *phix,
+cudaError_t launch_state_f32(const double *U, long long size, float *Uf, double *part, cudaStream_t st) {
+    k_state_f32<<<grid1(size, 128), 128, 0, st>>>(U, size, Uf, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, int npart, double *b, double *potc, double *phix,
                            double *phiy, double *fields, cudaStream_t st) {
-    const size_t smem = sizeof(double) * (size_t)pd.ndim;
+    // the band solve is a dependent chain over ndim columns: read the band
+    // factors from shared memory when they fit
+    PoissonDev d = pd;
+    const size_t base = (sizeof(double) + sizeof(int)) * (size_t)pd.ndim;
+    const size_t band = sizeof(double) * (size_t)pd.ldab * pd.ndim;
+    d.staged = (base + band <= 200 * 1024) ? 1 : 0;
+    const size_t smem = base + (d.staged ? band : 0);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_poisson<<<1, 256, smem, st>>>(pd, rt, b, potc, phix, phiy, fields);
+    k_poisson<<<1, 256, smem, st>>>(d, rt, npart, b, potc, phix, phiy, fields);
     return cudaGetLastError();
 }
 
-cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const double *fields,
-                              int stage, double *Uout, cudaStream_t st) {
-    k_flux<<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, fields, stage, Uout);
+cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const float *Uin_f32,
+                              const double *fields, int stage, double *Uout, float *Uout_f32, double *part,
+                              cudaStream_t st) {
+    if (Uin_f32)
+        k_flux<float, float><<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, Uin_f32, fields, stage, Uout, Uout_f32,
+                                                                 part);
+    else
+        k_flux<double, double><<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, Us, fields, stage, Uout, Uout_f32,
+                                                                   part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_f32_grp(const double *U, long long size, float *Uf, double *part, cudaStream_t st) {
+    k_state_f32_grp<<<grid1(size, 512), 128, 0, st>>>(U, size, Uf, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flux_inc(const AdvectDev &ad, int stage, const float *Uin, const float *Uf0,
+                            const double *fields, float *S, float *Uoutf, double *U, float *ipart,
+                            cudaStream_t st) {
+    const dim3 g = grid1(ad.size, 128);
+    if (stage == 0) k_flux_inc<0><<<g, 128, 0, st>>>(ad, Uin, Uf0, fields, S, Uoutf, U, ipart);
+    else if (stage == 1) k_flux_inc<1><<<g, 128, 0, st>>>(ad, Uin, Uf0, fields, S, Uoutf, U, ipart);
+    else k_flux_inc<2><<<g, 128, 0, st>>>(ad, Uin, Uf0, fields, S, Uoutf, U, ipart);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_dense(const PoissonDev &pd, const double *base, const float *inc, double iscale,
+                                 int npart, const double *Ainv, double *b, double *potc, double *phix,
+                                 double *phiy, double *fields, cudaStream_t st) {
+    const int nc = pd.nx * pd.ny;
+    k_prhs<<<(nc + 7) / 8, 256, 0, st>>>(pd, base, inc, iscale, npart, b);
+    k_psolve_dense<<<(pd.ndim + 7) / 8, 256, 0, st>>>(Ainv, b, pd.ndim, potc);
+    k_pfields<<<(nc + 127) / 128, 128, 0, st>>>(pd, potc, phix, phiy, fields);
     return cudaGetLastError();
 }
 
@@ -1346,7 +1709,7 @@ cudaError_t launch_moments(const double *U, long long size, long long kend, int 
     template cudaError_t launch_fwd_complex<R>(const V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, int,   \
                                                cudaStream_t);                                                   \
     template cudaError_t launch_fs_stage<R>(const double2 *, V2<R>::t *, V2<R>::t *, const R *, int, int, int,  \
-                                            double, double, const R *, R *, R *, cudaStream_t);                 \
+                                            double, double, const R *, R *, R *, cudaStream_t, Rates);          \
     template cudaError_t launch_fs_full<R>(const double2 *, V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, \
                                            int, cudaStream_t);                                                  \
     template cudaError_t launch_computeq<R>(const V2<R>::t *, const R *, const unsigned *, const int *, int,    \
@@ -1354,7 +1717,7 @@ cudaError_t launch_moments(const double *U, long long size, long long kend, int 
     template cudaError_t launch_project<R>(const double2 *, const double2 *, const double2 *, const double2 *,  \
                                            double, const R *, int, int, int, int, int, const double *, int,     \
                                            const int *, double, double, double, double, V2<R>::t *,             \
-                                           V2<R>::t *, V2<R>::t *, double *, cudaStream_t);
+                                           V2<R>::t *, V2<R>::t *, double *, cudaStream_t, Rates);
 LP_INST(double)
 LP_INST(float)
 #undef LP_INST

@@ -35,13 +35,20 @@ template <typename R>
 cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, const R *M, int n,
                        int Bp, cudaStream_t st);
 
+// Per-cell collision frequency and time step of the cells of one pass
+// (indexed by the cell's lane position 0..Bp-1); nullptr: the scalars.
+struct Rates {
+    const double *nu = nullptr;
+    const double *dt = nullptr;
+};
+
 // Inverse transform FS of q (FP64 complex), real part only, fused with the
 // RK4 stage update of the node values: stage 0 stores Q = Re FS(q) in qn and
 // writes f1 = f + dt Q nu; stages 1, 2 write f1 = f + dt/2 Q nu + dt/2 Re FS(q) nu.
 template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
                             const R *M, int n, int Bp, int stage, double dt, double nu,
-                            const R *f, R *qn, R *f1, cudaStream_t st);
+                            const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{});
 
 // Inverse transform FS of q, full complex output (for the reference-shaped FS).
 template <typename R>
@@ -68,8 +75,9 @@ long long lines_table_floats(int n, std::vector<long long> &line_off);
 cudaError_t launch_lines_table(const double *eta, const double *shat, const double *ahat,
                                const unsigned char *rzero, const double *cw, const long long *line_off,
                                int n, float *W, cudaStream_t st);
+// warps (2 or 4): warps of a block splitting the plane pairs of one line.
 cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n,
-                                  int Bp, double2 *q, cudaStream_t st);
+                                  int Bp, double2 *q, cudaStream_t st, int warps = 2);
 
 // Moment-conserving projection of q in place (FP64).
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
@@ -84,22 +92,27 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
                            int B, int c0, const double *U, int ustride, const int *uslot,
                            double dt, double scalev, double scaleL, double scale3,
                            typename V2<R>::t *Qc, typename V2<R>::t *Y, typename V2<R>::t *Z,
-                           double *dU, cudaStream_t st);
+                           double *dU, cudaStream_t st, Rates rates = Rates{});
 
 // Mixed path: reconcile the 5 DG moments of each cell's increment with their
 // FP64 values from the mode array (minimal-norm 5x5 Lagrange correction).
 cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
                               double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
                               const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
-                              double *apart, const double *gm_inv, double scale, double *lam, double *dU,
-                              cudaStream_t st);
+                              double *apart, const double *gm_inv, double scale, double kfac, double *lam,
+                              double *dU, cudaStream_t st, Rates rates = Rates{});
 
 // U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU.
 cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st);
 
-// ---- advection and Poisson (FP64) ----
+// ---- advection and Poisson ----
+// Charge moments of every spatial cell summed in the reference's record order
+// (scalev included): rt[3*ncell].
 cudaError_t launch_charge(const double *U, int ncell, int nv3, double scalev, double *rt,
                           cudaStream_t st);
+// FP32 copy of the state (size records of 7) and, when part != nullptr, the
+// charge partial sums of every block of 128 records: part[3 * size/128].
+cudaError_t launch_state_f32(const double *U, long long size, float *Uf, double *part, cudaStream_t st);
 
 struct PoissonDev {
     int nx, ny, ndim, kl, ku, ldab;
@@ -108,18 +121,49 @@ struct PoissonDev {
     double dxp, dyp;
     const unsigned char *gate;  // per x1 cell, 1-based
     double blk[6][9];           // acvx, acyrr, acyrl, acvy, acxrr, acxrl
+    // fast variant (mixed path): reciprocals of the band diagonal (nullptr:
+    // the host's operations, divisions included), of dxp and dyp, and the
+    // factor applied to the summed charge partials
+    const double *rdiag;
+    double rdxp, rdyp, cscale;
+    int staged;  // set by the launcher: band factors copied to shared memory
 };
-cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, double *b, double *potc,
+// rt: 3 charge sums per cell (npart = 1) or npart block partials per cell.
+cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, int npart, double *b, double *potc,
                            double *phix, double *phiy, double *fields, cudaStream_t st);
 
 struct AdvectDev {
     int nx1, nx2, nv;
     long long size;
     double lv, dv, dx, scalev, dt;
+    double rdv, inv;  // 1/dv and 1/dx/scalev
+    float dt_f;       // dt in FP32 (mixed-path stage copies)
+    double dt6;       // dt/6 (mixed-path final stage)
 };
-// One SSP-RK3 stage: Uout = combination(U0, Us, H(Us)).
-cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us,
-                              const double *fields, int stage, double *Uout, cudaStream_t st);
+// One SSP-RK3 stage: Uout = combination(U0, Us, H).  H is evaluated in FP64
+// from Us when Uin_f32 is nullptr, else in FP32 from the FP32 stage values
+// Uin_f32.  Uout_f32 (optional) receives an FP32 copy of Uout and part
+// (optional) the charge partial sums of Uout per block of 128 records.
+cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const float *Uin_f32,
+                              const double *fields, int stage, double *Uout, float *Uout_f32, double *part,
+                              cudaStream_t st);
+
+// ---- mixed-path advection (increment form of SSP-RK3, FP32 fluxes) ----
+// FP32 copy of the state and FP64 charge partials of every group of 128
+// records (part[3 * size/128]).
+cudaError_t launch_state_f32_grp(const double *U, long long size, float *Uf, double *part, cudaStream_t st);
+// Stage s in {0, 1, 2}: H from Uin (FP32 copy of U_s); stages 0, 1 update the
+// FP32 running sum S, write the FP32 copy of U_{s+1} and the FP32 charge
+// partials of S (ipart); stage 2 adds dt/6 (S + 4 H2) to the FP64 state U.
+cudaError_t launch_flux_inc(const AdvectDev &ad, int stage, const float *Uin, const float *Uf0,
+                            const double *fields, float *S, float *Uoutf, double *U, float *ipart,
+                            cudaStream_t st);
+// Poisson solve from charge partials base + iscale * inc (npart groups per
+// cell; inc may be nullptr) with the dense inverse Ainv (ndim x ndim,
+// row-major): potential into potc, fields as launch_poisson.  b is scratch.
+cudaError_t launch_poisson_dense(const PoissonDev &pd, const double *base, const float *inc, double iscale,
+                                 int npart, const double *Ainv, double *b, double *potc, double *phix,
+                                 double *phiy, double *fields, cudaStream_t st);
 
 // FMA-throughput microbenchmarks (FP32 packed f32x2 and FP64).
 cudaError_t launch_fma_peak(bool fp64, int blocks, int iters, double *sink, cudaStream_t st);

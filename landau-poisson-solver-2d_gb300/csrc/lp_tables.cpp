@@ -342,52 +342,10 @@ double weight_host(const Tables &t, int xi, int om) {
     return t.rzero[om] ? -res : t.ahat[om] - res;
 }
 
-lp_status build_tables(const lp_params &p, Tables &t, std::string &err) {
-    if (p.nx1 < 2 || p.nx2 < 1 || p.nv < 2 || p.n < 4 || (p.n % 2) != 0 || p.n > 32) {
-        err = "need nx1 >= 2, nx2 >= 1, nv >= 2 and an even n in [4, 32]";
-        return LP_ERR_INVALID;
-    }
-    if (!(p.lv > 0) || !(p.lx > 0) || !(p.dt > 0) || p.nu < 0 || !(p.k_wave > 0)) {
-        err = "need lv, lx, dt, k_wave > 0 and nu >= 0";
-        return LP_ERR_INVALID;
-    }
-    if ((long long)p.nx1 * p.nx2 * p.nv * p.nv * p.nv * 7 > (1LL << 40)) {
-        err = "state too large";
-        return LP_ERR_INVALID;
-    }
-    if (p.precision != LP_PREC_FP64 && p.precision != LP_PREC_MIXED) {
-        err = "unknown precision";
-        return LP_ERR_INVALID;
-    }
-    t.prm = p;
-    t.n = p.n; t.nv = p.nv;
-    t.n3 = p.n * p.n * p.n;
-    t.nv3 = p.nv * p.nv * p.nv;
-    t.ncell = p.nx1 * p.nx2;
-    t.size = (long long)t.ncell * t.nv3;
-    t.ncollide = (p.fixes & LP_FIX_F3) ? t.ncell : std::min(p.nx1, t.ncell);
-    // Grids and constants (M:38-40, M:66, M:270-284).
-    t.PI = M_PI;
-    t.dv = 2. * p.lv / p.nv;
-    t.dx = p.lx / p.nx1;
-    t.dy = p.lx / p.nx2;
-    t.scaleL = 8 * p.lv * p.lv * p.lv;
-    t.scalev = t.dv * t.dv * t.dv;
-    t.scale = 1.0 / std::sqrt(2.0 * M_PI);
-    t.scale3 = std::pow(t.scale, 3.0);
-    t.L_v = p.lv; t.R_v = p.lv;
-    t.L_eta = 0.5 * (double)(p.n - 1) * t.PI / t.L_v;
-    t.h_v = 2.0 * t.L_v / (double)(p.n - 1);
-    t.h_eta = 2.0 * t.L_eta / (double)(p.n);
+// The collision operator's tables: omega factors of the weight, conservation
+// rows, node map, IntModes factors, DFT matrices, pair offsets, moment rows.
+static lp_status build_collision_tables(const lp_params &p, Tables &t, std::string &err) {
     const int n = p.n, nv = p.nv;
-    t.v.resize(n); t.eta.resize(n); t.wt.assign(n, 1.0);
-    for (int i = 0; i < n; ++i) {
-        t.eta[i] = -t.L_eta + (double)i * t.h_eta;
-        t.v[i] = -t.L_v + (double)i * t.h_v;
-    }
-    if ((p.fixes & LP_FIX_F11) && std::fabs(t.eta[n / 2]) < 1e-12 * t.L_eta) t.eta[n / 2] = 0.;
-    t.wt[0] = 0.5; t.wt[n - 1] = 0.5;  // trapezoidalRule (S:26-34)
-
     // Omega tables of gHat3 and the per-omega quadrature factor of ComputeQ
     // (C:745, C:804: prefactor*wtN[l]*wtN[m]*wtN[n] in that order).
     t.shat.resize(6 * (size_t)t.n3); t.ahat.resize(t.n3); t.rzero.resize(t.n3); t.cw.resize(t.n3);
@@ -581,7 +539,90 @@ lp_status build_tables(const lp_params &p, Tables &t, std::string &err) {
         t.pair_off[xi + 1] = t.pair_off[xi] + (cnt + 1) / 2;
     }
 
+    return LP_OK;
+}
+
+lp_status build_tables(const lp_params &p, Tables &t, std::string &err, unsigned parts) {
+    if (p.nx1 < 2 || p.nx2 < 1 || p.nv < 2 || p.n < 4 || (p.n % 2) != 0 || p.n > 32) {
+        err = "need nx1 >= 2, nx2 >= 1, nv >= 2 and an even n in [4, 32]";
+        return LP_ERR_INVALID;
+    }
+    if (!(p.lv > 0) || !(p.lx > 0) || !(p.dt > 0) || p.nu < 0 || !(p.k_wave > 0)) {
+        err = "need lv, lx, dt, k_wave > 0 and nu >= 0";
+        return LP_ERR_INVALID;
+    }
+    if ((long long)p.nx1 * p.nx2 * p.nv * p.nv * p.nv * 7 > (1LL << 40)) {
+        err = "state too large";
+        return LP_ERR_INVALID;
+    }
+    if (p.precision != LP_PREC_FP64 && p.precision != LP_PREC_MIXED) {
+        err = "unknown precision";
+        return LP_ERR_INVALID;
+    }
+    t.prm = p;
+    t.n = p.n; t.nv = p.nv;
+    t.n3 = p.n * p.n * p.n;
+    t.nv3 = p.nv * p.nv * p.nv;
+    t.ncell = p.nx1 * p.nx2;
+    t.size = (long long)t.ncell * t.nv3;
+    t.ncollide = (p.fixes & LP_FIX_F3) ? t.ncell : std::min(p.nx1, t.ncell);
+    // Grids and constants (M:38-40, M:66, M:270-284).
+    t.PI = M_PI;
+    t.dv = 2. * p.lv / p.nv;
+    t.dx = p.lx / p.nx1;
+    t.dy = p.lx / p.nx2;
+    t.scaleL = 8 * p.lv * p.lv * p.lv;
+    t.scalev = t.dv * t.dv * t.dv;
+    t.scale = 1.0 / std::sqrt(2.0 * M_PI);
+    t.scale3 = std::pow(t.scale, 3.0);
+    t.L_v = p.lv; t.R_v = p.lv;
+    t.L_eta = 0.5 * (double)(p.n - 1) * t.PI / t.L_v;
+    t.h_v = 2.0 * t.L_v / (double)(p.n - 1);
+    t.h_eta = 2.0 * t.L_eta / (double)(p.n);
+    const int n = p.n, nv = p.nv;
+    t.v.resize(n); t.eta.resize(n); t.wt.assign(n, 1.0);
+    for (int i = 0; i < n; ++i) {
+        t.eta[i] = -t.L_eta + (double)i * t.h_eta;
+        t.v[i] = -t.L_v + (double)i * t.h_v;
+    }
+    if ((p.fixes & LP_FIX_F11) && std::fabs(t.eta[n / 2]) < 1e-12 * t.L_eta) t.eta[n / 2] = 0.;
+    t.wt[0] = 0.5; t.wt[n - 1] = 0.5;  // trapezoidalRule (S:26-34)
+
+    if (parts & kTablesCollision) {
+        const lp_status s = build_collision_tables(p, t, err);
+        if (s != LP_OK) return s;
+    }
+    if (!(parts & kTablesPoisson)) return LP_OK;
     return build_poisson(t, err);
+}
+
+
+// Columns of A^-1 by the band solve of DGBTRS ('N') with the factors of
+// build_poisson: forward elimination with the row interchanges, then the
+// banded upper-triangular back substitution.
+void poisson_inverse(const PoissonTables &ps, std::vector<double> &inv) {
+    const int n = ps.ndim, kl = ps.kl, ku = ps.ku, ldab = ps.ldab, kd = ku + kl + 1, k = kl + ku;
+    auto AB = [&](int i, int j) { return ps.ab[(size_t)(i - 1) + (size_t)(j - 1) * ldab]; };
+    inv.assign((size_t)n * n, 0.);
+    std::vector<double> b(n);
+    for (int col = 0; col < n; ++col) {
+        std::fill(b.begin(), b.end(), 0.);
+        b[col] = 1.;
+        for (int j = 1; j <= n - 1; ++j) {
+            const int lm = std::min(kl, n - j), l = ps.ipiv[j - 1];
+            if (l != j) std::swap(b[l - 1], b[j - 1]);
+            const double bj = b[j - 1];
+            if (bj != 0.)
+                for (int i = 1; i <= lm; ++i) b[j + i - 1] -= AB(kd + i, j) * bj;
+        }
+        for (int j = n; j >= 1; --j) {
+            if (b[j - 1] == 0.) continue;
+            const double xj = b[j - 1] / AB(k + 1, j);
+            b[j - 1] = xj;
+            for (int i = std::max(1, j - k); i <= j - 1; ++i) b[i - 1] -= xj * AB(k + 1 - j + i, j);
+        }
+        for (int r = 0; r < n; ++r) inv[(size_t)r * n + col] = b[r];
+    }
 }
 
 }  // namespace lp

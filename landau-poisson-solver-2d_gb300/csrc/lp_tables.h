@@ -55,8 +55,14 @@ struct Tables {
     int ncollide = 0;            // spatial cells that are collided
 };
 
-// Validates p and fills t; returns LP_OK or LP_ERR_INVALID with err set.
-lp_status build_tables(const lp_params &p, Tables &t, std::string &err);
+// Validates p and fills t (grids and constants always, the collision and the
+// Poisson tables as `parts` asks); returns LP_OK or LP_ERR_INVALID with err set.
+constexpr unsigned kTablesCollision = 1u, kTablesPoisson = 2u, kTablesAll = 3u;
+lp_status build_tables(const lp_params &p, Tables &t, std::string &err, unsigned parts = kTablesAll);
+
+// Dense inverse of the LDG Poisson matrix (row-major ndim x ndim) from the
+// band LU factors.
+void poisson_inverse(const PoissonTables &ps, std::vector<double> &inv);
 
 // gHat3(eta_xi, eta_omega) from the omega tables (the reference's order).
 double weight_host(const Tables &t, int xi, int om);

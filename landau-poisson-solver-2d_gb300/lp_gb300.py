@@ -35,6 +35,10 @@ EXPORTS = [
     "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_last_fields", "lp_advect_step",
     "lp_collision_step", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
     "lp_conserve_noalloc",
+    "lp_batch_create", "lp_batch_destroy", "lp_batch_set_stream", "lp_batch_synchronize",
+    "lp_batch_last_error", "lp_batch_device_bytes", "lp_batch_set_state", "lp_batch_get_state",
+    "lp_batch_set_init", "lp_batch_moments", "lp_batch_advect_step", "lp_batch_collision_step",
+    "lp_batch_step", "lp_batch_classes", "lp_batch_class_info", "lp_batch_autotune",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -119,9 +123,27 @@ def lib():
         L.lp_time_kernel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
         L.lp_measure_fp_peaks.argtypes = [_dp, _dp]
         L.lp_conserve_noalloc.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
+        L.lp_batch_create.argtypes = [ctypes.POINTER(_Params), ctypes.c_int, ctypes.POINTER(_vp)]
+        for name in ["lp_batch_destroy", "lp_batch_synchronize", "lp_batch_advect_step",
+                     "lp_batch_collision_step"]:
+            getattr(L, name).argtypes = [_vp]
+        L.lp_batch_set_stream.argtypes = [_vp, _vp]
+        L.lp_batch_last_error.restype = ctypes.c_char_p
+        L.lp_batch_last_error.argtypes = [_vp]
+        L.lp_batch_device_bytes.restype = ctypes.c_size_t
+        L.lp_batch_device_bytes.argtypes = [_vp]
+        L.lp_batch_set_state.argtypes = [_vp, ctypes.c_int, _dp, ctypes.c_size_t]
+        L.lp_batch_get_state.argtypes = [_vp, ctypes.c_int, _dp, ctypes.c_size_t]
+        L.lp_batch_set_init.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.lp_batch_moments.argtypes = [_vp, ctypes.c_int, _dp]
+        L.lp_batch_step.argtypes = [_vp, ctypes.c_int]
+        L.lp_batch_classes.argtypes = [_vp]
+        L.lp_batch_class_info.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp]
+        L.lp_batch_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p]
         for name in EXPORTS:
             f = getattr(L, name)
-            if name not in ("lp_last_error", "lp_device_bytes"):
+            if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
+                            "lp_batch_device_bytes"):
                 f.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -277,3 +299,82 @@ class Context:
         out = np.zeros(6)
         self._chk(self.L.lp_moments(self.h, _p(out)))
         return out
+
+
+class Batch:
+    """Independent runs stepped together (lp_batch_* of the C ABI)."""
+
+    def __init__(self, params_list):
+        self.params = list(params_list)
+        self.L = lib()
+        arr = (_Params * len(self.params))(*[p._c() for p in self.params])
+        h = _vp()
+        st = self.L.lp_batch_create(arr, len(self.params), ctypes.byref(h))
+        if st != OK:
+            raise LPError(st, "lp_batch_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, st):
+        if st != OK:
+            raise LPError(st, self.L.lp_batch_last_error(self.h).decode())
+
+    @property
+    def device_bytes(self):
+        return int(self.L.lp_batch_device_bytes(self.h))
+
+    def set_stream(self, stream_handle):
+        self._chk(self.L.lp_batch_set_stream(self.h, _vp(stream_handle)))
+
+    def synchronize(self):
+        self._chk(self.L.lp_batch_synchronize(self.h))
+
+    def set_state(self, run, U):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+        self._chk(self.L.lp_batch_set_state(self.h, int(run), _p(U), U.size))
+
+    def get_state(self, run):
+        U = np.zeros(self.params[run].size * 7)
+        self._chk(self.L.lp_batch_get_state(self.h, int(run), _p(U), U.size))
+        return U
+
+    def set_init(self, run, kind=1, u=2.0):
+        self._chk(self.L.lp_batch_set_init(self.h, int(run), int(kind), float(u)))
+
+    def moments(self, run):
+        out = np.zeros(6)
+        self._chk(self.L.lp_batch_moments(self.h, int(run), _p(out)))
+        return out
+
+    def advect_step(self):
+        self._chk(self.L.lp_batch_advect_step(self.h))
+
+    def collision_step(self):
+        self._chk(self.L.lp_batch_collision_step(self.h))
+
+    def step(self, nsteps=1):
+        self._chk(self.L.lp_batch_step(self.h, int(nsteps)))
+
+    def classes(self):
+        """[(n, nv, runs, cells, cells_per_pass, line_warps, tuned_ms)] per class."""
+        out = []
+        for k in range(self.L.lp_batch_classes(self.h)):
+            info = (ctypes.c_int * 6)()
+            ms = ctypes.c_double()
+            self._chk(self.L.lp_batch_class_info(self.h, k, info, ctypes.byref(ms)))
+            out.append(tuple(info) + (ms.value,))
+        return out
+
+    def autotune(self, reps=3, cache_path=None):
+        self._chk(self.L.lp_batch_autotune(self.h, int(reps),
+                                           cache_path.encode() if cache_path else None))

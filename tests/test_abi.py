@@ -11,7 +11,7 @@ from conftest import ROOT
 
 def _declared():
     src = open(os.path.join(ROOT, "include", "lp_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:lp_status|const char \*|size_t)\s*\*?\s*(lp_\w+)\s*\(",
+    return sorted(set(re.findall(r"^\s*(?:lp_status|const char \*|size_t|int)\s*\*?\s*(lp_\w+)\s*\(",
                                  src, re.M)))
 
 
