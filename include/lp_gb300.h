@@ -147,6 +147,58 @@ lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
  * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */
 lp_status lp_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
 
+/* ---- diagnostics and state I/O ------------------------------------------ */
+/* The reference's per-step diagnostics of the resident state, computed on the
+ * device after a Poisson solve of that state (LP_ompi_1.cpp:452-470):
+ * out10 = {mass, p1, p2, p3, kinetic energy, electric energy EE, sqrt(EE),
+ * log sqrt(EE), total energy, entropy int f log f} (computeMass,
+ * computeMomentum, computeKiE, computeEleE in MomentCalculations.cpp,
+ * computeEntropy in EntropyCalculations.cpp:11-65; the entropy's integrand is
+ * evaluated in FP32). */
+lp_status lp_diagnostics(lp_ctx *ctx, double *out10);
+/* Appends the reference's moment line (9 values, "%11.8g") to moments_path
+ * and its entropy line (entropy, log|entropy|, log|log|entropy||) to
+ * entropy_path; either may be NULL. */
+lp_status lp_diagnostics_append(lp_ctx *ctx, const char *moments_path, const char *entropy_path);
+/* The reference's (x1, v1) marginal (PrintMarginal, MarginalCreation.cpp:174)
+ * at 4 x 4 points per (x1 cell, v1 cell): out[nx1*4][nv*4]. */
+lp_status lp_marginal_x1v1(lp_ctx *ctx, double *out);
+/* Snapshot files in the reference's format (LP_ompi_1.cpp:416-438, 628): raw
+ * native-endian doubles of the state, snapshots appended one after another;
+ * restart reads the last snapshot and rejects a file whose size is not a
+ * whole number of states. */
+lp_status lp_state_append(lp_ctx *ctx, const char *path);
+lp_status lp_state_restart(lp_ctx *ctx, const char *path);
+
+/* ---- adjoint ------------------------------------------------------------- */
+/* No counterpart in the reference.  Hand-written vector-Jacobian products of
+ * the FP64 path (contexts with LP_PREC_FP64 and LP_FIX_F1 | LP_FIX_F2 |
+ * LP_FIX_F3; Poisson matrix of order 3*nx1*nx2 <= 4096), evaluated at the
+ * resident state, which they leave unchanged.  Adjoint vectors are DEVICE
+ * pointers of ncell*nv^3*7 doubles in the state's layout.
+ *   collision step: the bilinear ComputeQ linearised (a correlation with the
+ *     pair weights), the transposed transforms, the self-adjoint conservation
+ *     projection and the transposed DG projection, through the RK4 stages;
+ *   advection step: the transposed upwind DG flux of each SSP-RK3 stage and
+ *     the transposed LDG Poisson solve of its field;
+ *   field energy J = 1/2 sum_cells dx dy (E_0^2 + (E_1^2 + E_2^2)/12) over E_x
+ *     and E_y of the Poisson solve on the state. */
+/* J of the resident state and, when lam_U_dev is not NULL, dJ/dU. */
+lp_status lp_field_energy(lp_ctx *ctx, double *J, double *lam_U_dev);
+/* lam_in = (d collision step / dU)^T lam_out; *dJ_dnu (optional) = the
+ * derivative of <lam_out, step output> with respect to nu. */
+lp_status lp_collision_vjp(lp_ctx *ctx, const double *lam_out_dev, double *lam_in_dev, double *dJ_dnu);
+/* lam_in = (d advection step / dU)^T lam_out. */
+lp_status lp_advect_vjp(lp_ctx *ctx, const double *lam_out_dev, double *lam_in_dev);
+/* The same for one whole time step (advection, then collisions). */
+lp_status lp_step_vjp(lp_ctx *ctx, const double *lam_out_dev, double *lam_in_dev, double *dJ_dnu);
+/* Gradient of the field energy after nsteps time steps from the resident
+ * (initial) state: J, dJ/dU0 (device) and dJ/dnu, by the adjoint with a
+ * checkpoint every `checkpoint` steps (the states between checkpoints are
+ * recomputed segment by segment). */
+lp_status lp_field_energy_gradient(lp_ctx *ctx, int nsteps, int checkpoint, double *J, double *dJ_dU0_dev,
+                                   double *dJ_dnu);
+
 /* ---- batches of independent runs ---------------------------------------- */
 /* No counterpart in the reference, which runs one instance per job.  A batch
  * steps `count` independent runs, each with its own lp_params (grid nx1 x nx2,

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "lp_gb300.h"
+#include "lp_adjoint.cuh"
 #include "lp_kernels.cuh"
 #include "lp_tables.h"
 
@@ -33,6 +34,8 @@ struct lp_ctx {
     void *P = nullptr;                                       // R precision
     unsigned *PI = nullptr;
     float *LW = nullptr;            // line-tiled weight table (mixed path)
+    cudaStream_t side = nullptr;    // second stream of the line-tiled contraction
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long *line_off = nullptr;
     double *ab = nullptr;
     // state and advection
@@ -63,6 +66,22 @@ struct lp_ctx {
     // moment reconciliation (mixed path)
     double *gmom = nullptr, *gm_inv = nullptr, *mtpart = nullptr, *mapart = nullptr, *mlam = nullptr;
     int nrc = 16;
+    // adjoint workspace (FP64 contexts, allocated by the first adjoint call)
+    struct Adj {
+        bool ready = false;
+        double2 *F[4] = {nullptr, nullptr, nullptr, nullptr};  // transforms of the stage node values
+        double *r1 = nullptr, *r2 = nullptr;                     // Re FS(q1), Re FS(q2)
+        double *lf = nullptr, *lqn = nullptr, *ls = nullptr, *ltp = nullptr;
+        double2 *lq = nullptr, *tq = nullptr, *lF = nullptr, *qs = nullptr;
+        double *mfH = nullptr, *miH = nullptr;  // conjugate transposes of the DFT matrices
+        int *nfirst = nullptr, *ncount = nullptr;
+        double *Ainv = nullptr, *lrt = nullptr, *lamF = nullptr, *lphix = nullptr, *lphiy = nullptr, *J = nullptr;
+        double *dnu = nullptr;  // per collided cell
+        double *lU = nullptr, *lU1 = nullptr, *lUt = nullptr, *lH = nullptr, *lC = nullptr, *Ukeep = nullptr;
+        std::vector<double *> ck;  // checkpoints
+        double *seg = nullptr;     // states of one checkpoint segment
+        int seg_len = 0;
+    } adj;
     // captured step
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
@@ -322,8 +341,18 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     if (c->LW) {
+        // the k-tiles run on two streams so that the short lines at the end
+        // of one tile overlap the next tile
+        if (c->side) {
+            LP_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+            LP_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        }
         LP_CUDA(lp::launch_computeq_lines((const float2 *)c->F, c->LW, c->line_off, T.n, Bp, q, c->stream,
-                                          c->line_warps));
+                                          c->line_warps, c->side));
+        if (c->side) {
+            LP_CUDA(cudaEventRecord(c->ev_join, c->side));
+            LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+        }
         return LP_OK;
     }
     LP_CUDA(lp::launch_computeq<R>((const C *)c->F, (const R *)c->P, c->PI, c->pair_off, T.n3, Bp, q, c->stream));
@@ -551,6 +580,9 @@ void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> 
 void destroy(lp_ctx *c) {
     if (!c) return;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     for (void *p : c->allocs) cudaFree(p);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
@@ -601,6 +633,11 @@ lp_status ctx_create(const lp_params *p, const CtxOpts &o, lp_ctx **out) {
     const lp::Tables &T = c->T;
     const size_t rec = (size_t)T.size * 7;
     if (o.collide) s = c->mixed ? upload_tables<float>(c) : upload_tables<double>(c);
+    if (s == LP_OK && c->LW &&
+        (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        s = LP_ERR_CUDA;
     if (s == LP_OK && c->owns_state) {
         s = dalloc(c, &c->U, rec);
         if (s == LP_OK) s = dalloc(c, &c->U1, rec);
@@ -617,6 +654,234 @@ lp_status ctx_create(const lp_params *p, const CtxOpts &o, lp_ctx **out) {
         return s;
     }
     *out = c;
+    return LP_OK;
+}
+
+// ============================================================== adjoint
+// Vector-Jacobian products of the FP64 path (see lp_adjoint.cu for the
+// conventions), evaluated at given states; every forward quantity they need
+// is recomputed from the state.
+
+lp_status adj_setup(lp_ctx *c) {
+    auto &A = c->adj;
+    if (A.ready) return LP_OK;
+    const lp::Tables &T = c->T;
+    if (c->mixed || !c->collide_on || !c->advect_on) return fail(c, LP_ERR_INVALID, "the adjoint needs an FP64 context");
+    if ((T.prm.fixes & (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3)) != (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3))
+        return fail(c, LP_ERR_INVALID, "the adjoint needs LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3");
+    if (T.pois.ndim > 4096) return fail(c, LP_ERR_INVALID, "the adjoint needs a Poisson matrix of order <= 4096");
+    const size_t n3 = T.n3, Bp = c->Bcap, rec = (size_t)T.size * 7, nc = T.ncell;
+    for (int s = 0; s < 4; ++s) LP_TRY(dalloc(c, &A.F[s], n3 * Bp));
+    LP_TRY(dalloc(c, &A.r1, n3 * Bp));
+    LP_TRY(dalloc(c, &A.r2, n3 * Bp));
+    LP_TRY(dalloc(c, &A.lf, n3 * Bp));
+    LP_TRY(dalloc(c, &A.lqn, n3 * Bp));
+    LP_TRY(dalloc(c, &A.ls, n3 * Bp));
+    LP_TRY(dalloc(c, &A.ltp, 5 * (size_t)T.nv3 * Bp));
+    LP_TRY(dalloc(c, &A.lq, n3 * Bp));
+    LP_TRY(dalloc(c, &A.tq, n3 * Bp));
+    LP_TRY(dalloc(c, &A.lF, n3 * Bp));
+    LP_TRY(dalloc(c, &A.qs, n3 * Bp));
+    // conjugate transposes of the per-axis matrices (out index major)
+    std::vector<double> fH(T.mfwd.size()), iH(T.minv.size());
+    const int n = T.n;
+    for (int p = 0; p < n; ++p)
+        for (int a = 0; a < n; ++a) {
+            fH[2 * (a * n + p)] = T.mfwd[2 * (p * n + a)];
+            fH[2 * (a * n + p) + 1] = -T.mfwd[2 * (p * n + a) + 1];
+            iH[2 * (a * n + p)] = T.minv[2 * (p * n + a)];
+            iH[2 * (a * n + p) + 1] = -T.minv[2 * (p * n + a) + 1];
+        }
+    LP_TRY(upload(c, &A.mfH, fH.data(), fH.size()));
+    LP_TRY(upload(c, &A.miH, iH.data(), iH.size()));
+    // spectral nodes inside each DG velocity cell (nodecell is nondecreasing)
+    std::vector<int> first(T.nv, 0), count(T.nv, 0);
+    for (int l = n - 1; l >= 0; --l) { first[T.nodecell[l]] = l; ++count[T.nodecell[l]]; }
+    LP_TRY(upload(c, &A.nfirst, first.data(), first.size()));
+    LP_TRY(upload(c, &A.ncount, count.data(), count.size()));
+    std::vector<double> inv;
+    lp::poisson_inverse(T.pois, inv);
+    LP_TRY(upload(c, &A.Ainv, inv.data(), inv.size()));
+    LP_TRY(dalloc(c, &A.lrt, 3 * nc));
+    LP_TRY(dalloc(c, &A.lamF, 3 * nc));
+    LP_TRY(dalloc(c, &A.lphix, 3 * nc));
+    LP_TRY(dalloc(c, &A.lphiy, 3 * nc));
+    LP_TRY(dalloc(c, &A.J, 1));
+    LP_TRY(dalloc(c, &A.dnu, (size_t)std::max(T.ncollide, 1)));
+    LP_TRY(dalloc(c, &A.lU, rec));
+    LP_TRY(dalloc(c, &A.lU1, rec));
+    LP_TRY(dalloc(c, &A.lUt, rec));
+    LP_TRY(dalloc(c, &A.lH, rec));
+    LP_TRY(dalloc(c, &A.lC, rec));
+    LP_TRY(dalloc(c, &A.Ukeep, rec));
+    A.ready = true;
+    return LP_OK;
+}
+
+// q = conserve(ComputeQ(F)) for the FP64 pair table
+lp_status adj_q(lp_ctx *c, const double2 *F, int Bp, double2 *q) {
+    const lp::Tables &T = c->T;
+    LP_CUDA(lp::launch_computeq<double>(F, (const double *)c->P, c->PI, c->pair_off, T.n3, Bp, q, c->stream));
+    LP_CUDA(lp::launch_conserve(q, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    return LP_OK;
+}
+
+// lam_f_out (=|+=) Re T^H conserve(lam_q) through the linearised ComputeQ at F
+lp_status adj_q_back(lp_ctx *c, const double2 *F, double2 *lq, int Bp, double *lf, double beta) {
+    const lp::Tables &T = c->T;
+    auto &A = c->adj;
+    const long long N = (long long)T.n3 * Bp;
+    LP_CUDA(lp::launch_conserve(lq, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_CUDA(lp::launch_qvjp(F, lq, (const double *)c->P, c->pair_off, T.n, Bp, A.lF, c->stream));
+    LP_CUDA(lp::launch_fwd_complex<double>(A.lF, (double2 *)c->t1, A.tq, A.mfH, T.n, Bp, c->stream));
+    LP_CUDA(lp::launch_add_re(lf, beta, A.tq, 1.0, N, c->stream));
+    return LP_OK;
+}
+
+// lam_in = (d collision step / dU at Uin)^T lam_out for cells [0, ncollide);
+// dnu[cell] += the cell's dL/dnu.  Uin is the collision's input state.
+lp_status collide_vjp(lp_ctx *c, const double *Uin, const double *lout, double *lin) {
+    LP_TRY(adj_setup(c));
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    const double dt = T.prm.dt, nu = T.prm.nu;
+    const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
+    // records of cells that are not collided keep their adjoint
+    LP_CUDA(cudaMemcpyAsync(lin, lout, sizeof(double) * (size_t)T.size * 7, cudaMemcpyDeviceToDevice, c->stream));
+    LP_CUDA(cudaMemsetAsync(A.dnu, 0, sizeof(double) * std::max(T.ncollide, 1), c->stream));
+    if (!(nu > 0.)) return LP_OK;
+    const double *Mf = (const double *)c->mfwd, *Mi = (const double *)c->minv;
+    double *f = (double *)c->f, *f1 = (double *)c->f1, *qn = (double *)c->qn;
+    for (int c0 = 0; c0 < T.ncollide; c0 += c->Bcap) {
+        const int B = std::min(c->Bcap, T.ncollide - c0), Bp = round32(B);
+        const long long N = (long long)T.n3 * Bp;
+        double2 *t1 = (double2 *)c->t1, *t2 = (double2 *)c->t2, *tc = (double2 *)c->Qc;
+        // forward recomputation of the stages
+        LP_CUDA(lp::launch_nodes<double>(Uin, T.nv, T.n, c0, B, Bp, 3, c->nodecell, c->nodeoff, T.dv, f, c->stream));
+        LP_CUDA(lp::launch_fwd<double>(f, t1, A.F[0], Mf, T.n, Bp, c->stream));
+        LP_TRY(adj_q(c, A.F[0], Bp, c->q[0]));
+        LP_CUDA(lp::launch_fs_full<double>(c->q[0], t1, t2, tc, Mi, T.n, Bp, c->stream));
+        LP_CUDA(lp::launch_add_re(qn, 0., tc, 1., N, c->stream));                  // qn = Re FS(q0)
+        LP_CUDA(cudaMemcpyAsync(f1, f, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+        LP_CUDA(lp::launch_axpby(f1, 1., qn, dt * nu, N, c->stream));                // f + dt nu qn
+        LP_CUDA(lp::launch_fwd<double>(f1, t1, A.F[1], Mf, T.n, Bp, c->stream));
+        LP_TRY(adj_q(c, A.F[1], Bp, c->q[1]));
+        double *rs[2] = {A.r1, A.r2};
+        for (int s = 1; s <= 2; ++s) {
+            LP_CUDA(lp::launch_fs_full<double>(c->q[s], t1, t2, tc, Mi, T.n, Bp, c->stream));
+            LP_CUDA(lp::launch_add_re(rs[s - 1], 0., tc, 1., N, c->stream));       // r_s = Re FS(q_s)
+            LP_CUDA(cudaMemcpyAsync(f1, f, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+            LP_CUDA(lp::launch_axpby(f1, 1., qn, 0.5 * dt * nu, N, c->stream));
+            LP_CUDA(lp::launch_axpby(f1, 1., rs[s - 1], 0.5 * dt * nu, N, c->stream));
+            LP_CUDA(lp::launch_fwd<double>(f1, t1, A.F[s + 1], Mf, T.n, Bp, c->stream));
+            LP_TRY(adj_q(c, A.F[s + 1], Bp, c->q[s + 1]));
+        }
+        // backward: the update of the collided coefficients and the projection
+        LP_CUDA(lp::launch_collide_out_vjp(lout, T.nv, c0, B, Bp, dt, kfac, A.ltp, lin, c->stream));
+        LP_CUDA(lp::launch_project_vjp(A.ltp, (const double *)c->tfac, T.n, T.nv, Bp, (double2 *)c->Z,
+                                       (double2 *)c->Y, tc, c->stream));           // tc = lam_Qc
+        LP_CUDA(lp::launch_qsum(c->q[0], c->q[1], c->q[2], c->q[3], N, A.qs, c->stream));
+        LP_CUDA(lp::launch_cdot_cell(tc, A.qs, T.n3, Bp, B, 1.0, A.dnu + c0, c->stream));
+        // q3 <- F3 <- f1_2 = f + dt nu/2 (qn + r2)
+        LP_CUDA(lp::launch_caxpby(A.lq, 0., tc, nu / 6., N, c->stream));
+        LP_TRY(adj_q_back(c, A.F[3], A.lq, Bp, A.ls, 0.));                       // ls = lam f1_2
+        LP_CUDA(cudaMemcpyAsync(A.lf, A.ls, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+        LP_CUDA(lp::launch_scale(A.lqn, A.ls, 0.5 * dt * nu, N, c->stream));
+        LP_CUDA(lp::launch_dot_cell(A.ls, qn, T.n3, Bp, B, 0.5 * dt, A.dnu + c0, c->stream));
+        LP_CUDA(lp::launch_dot_cell(A.ls, A.r2, T.n3, Bp, B, 0.5 * dt, A.dnu + c0, c->stream));
+        for (int s = 2; s >= 1; --s) {
+            // lam q_s = nu/6 lam_Qc + FS^H (dt nu/2 lam f1_s)
+            LP_CUDA(lp::launch_fwd<double>(A.ls, t1, A.lq, A.miH, T.n, Bp, c->stream));
+            LP_CUDA(lp::launch_caxpby(A.lq, 0.5 * dt * nu, tc, nu / 6., N, c->stream));
+            LP_TRY(adj_q_back(c, A.F[s], A.lq, Bp, A.ls, 0.));                   // ls = lam f1_{s-1}
+            LP_CUDA(lp::launch_axpby(A.lf, 1., A.ls, 1., N, c->stream));
+            if (s == 2) {  // f1_1 = f + dt nu/2 (qn + r1)
+                LP_CUDA(lp::launch_axpby(A.lqn, 1., A.ls, 0.5 * dt * nu, N, c->stream));
+                LP_CUDA(lp::launch_dot_cell(A.ls, qn, T.n3, Bp, B, 0.5 * dt, A.dnu + c0, c->stream));
+                LP_CUDA(lp::launch_dot_cell(A.ls, A.r1, T.n3, Bp, B, 0.5 * dt, A.dnu + c0, c->stream));
+            } else {       // f1_0 = f + dt nu qn
+                LP_CUDA(lp::launch_axpby(A.lqn, 1., A.ls, dt * nu, N, c->stream));
+                LP_CUDA(lp::launch_dot_cell(A.ls, qn, T.n3, Bp, B, dt, A.dnu + c0, c->stream));
+            }
+        }
+        // q0: nu/2 lam_Qc + FS^H lam_qn
+        LP_CUDA(lp::launch_fwd<double>(A.lqn, t1, A.lq, A.miH, T.n, Bp, c->stream));
+        LP_CUDA(lp::launch_caxpby(A.lq, 1., tc, nu / 2., N, c->stream));
+        LP_TRY(adj_q_back(c, A.F[0], A.lq, Bp, A.lf, 1.));
+        LP_CUDA(lp::launch_nodes_vjp(A.lf, T.nv, T.n, c0, B, Bp, 3, A.nfirst, A.ncount, c->nodeoff, lin, c->stream));
+    }
+    return LP_OK;
+}
+
+// lam (accumulated) += (d/dV of dt-scaled flux stage)^T: lamV += (dH/dV)^T lamH
+// with the Poisson solve of V included.
+lp_status flux_stage_vjp(lp_ctx *c, const double *V, const double *lamH, double *lamV) {
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    LP_TRY(poisson_on(c, V));  // fields of V
+    LP_CUDA(cudaMemsetAsync(A.lamF, 0, sizeof(double) * 3 * T.ncell, c->stream));
+    LP_CUDA(lp::launch_flux_vjp(advect_dev(c), V, c->fields, lamH, lamV, A.lamF, c->stream));
+    LP_CUDA(lp::launch_poisson_vjp(poisson_dev(c, false), A.lamF, nullptr, nullptr, A.Ainv, A.lrt, c->stream));
+    LP_CUDA(lp::launch_charge_vjp(A.lrt, T.size, T.nv3, T.scalev, lamV, c->stream));
+    return LP_OK;
+}
+
+// lam_in = (d RK3 step / dU at U)^T lam_out, with U1, Ut the step's stage
+// values (recomputed by the caller).
+lp_status advect_vjp(lp_ctx *c, const double *U, const double *U1, const double *Ut, const double *lout,
+                     double *lin) {
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    const long long n = (long long)T.size * 7;
+    const double dt = T.prm.dt;
+    // U_new = U/3 + 2/3 Ut + 2/3 dt H(Ut)
+    LP_CUDA(lp::launch_scale(lin, lout, 1. / 3., n, c->stream));
+    LP_CUDA(lp::launch_scale(A.lUt, lout, 2. / 3., n, c->stream));
+    LP_CUDA(lp::launch_scale(A.lH, lout, 2. / 3. * dt, n, c->stream));
+    LP_TRY(flux_stage_vjp(c, Ut, A.lH, A.lUt));
+    // Ut = 3/4 U + 1/4 U1 + 1/4 dt H(U1)
+    LP_CUDA(lp::launch_axpby(lin, 1., A.lUt, 0.75, n, c->stream));
+    LP_CUDA(lp::launch_scale(A.lU1, A.lUt, 0.25, n, c->stream));
+    LP_CUDA(lp::launch_scale(A.lH, A.lUt, 0.25 * dt, n, c->stream));
+    LP_TRY(flux_stage_vjp(c, U1, A.lH, A.lU1));
+    // U1 = U + dt H(U)
+    LP_CUDA(lp::launch_axpby(lin, 1., A.lU1, 1., n, c->stream));
+    LP_CUDA(lp::launch_scale(A.lH, A.lU1, dt, n, c->stream));
+    LP_TRY(flux_stage_vjp(c, U, A.lH, lin));
+    return LP_OK;
+}
+
+// Field energy J of state U (device) and, if lamU, dJ/dU into lamU.
+lp_status field_energy_at(lp_ctx *c, const double *U, double *lamU) {
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    LP_TRY(poisson_on(c, U));
+    LP_CUDA(lp::launch_field_energy(c->phix, c->phiy, T.ncell, T.dx * T.dy, A.J, A.lphix, A.lphiy, c->stream));
+    if (lamU) {
+        LP_CUDA(cudaMemsetAsync(lamU, 0, sizeof(double) * (size_t)T.size * 7, c->stream));
+        LP_CUDA(lp::launch_poisson_vjp(poisson_dev(c, false), nullptr, A.lphix, A.lphiy, A.Ainv, A.lrt, c->stream));
+        LP_CUDA(lp::launch_charge_vjp(A.lrt, T.size, T.nv3, T.scalev, lamU, c->stream));
+    }
+    return LP_OK;
+}
+
+// One time step's VJP at state Un (device, not c->U): lam <- (dStep/dU)^T lam,
+// adding the step's dL/dnu to *dnu_sum.  Uses c->U, U1, Ut as scratch.
+lp_status step_vjp(lp_ctx *c, const double *Un, double *lam, double *dnu_sum) {
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    const size_t bytes = sizeof(double) * (size_t)T.size * 7;
+    LP_CUDA(cudaMemcpyAsync(c->U, Un, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_TRY(advect(c));  // c->U = advected state, c->U1, c->Ut = stage values
+    LP_TRY(collide_vjp(c, c->U, lam, A.lC));
+    if (dnu_sum) {
+        std::vector<double> d(std::max(T.ncollide, 1));
+        LP_CUDA(cudaMemcpyAsync(d.data(), A.dnu, sizeof(double) * d.size(), cudaMemcpyDeviceToHost, c->stream));
+        LP_CUDA(cudaStreamSynchronize(c->stream));
+        if (T.prm.nu > 0.)
+            for (int i = 0; i < T.ncollide; ++i) *dnu_sum += d[i];
+    }
+    LP_TRY(advect_vjp(c, Un, c->U1, c->Ut, A.lC, lam));
     return LP_OK;
 }
 
@@ -1223,6 +1488,202 @@ lp_status lp_batch_step(lp_batch *b, int nsteps) {
         b->gstream = b->stream;
     }
     for (int i = 0; i < nsteps; ++i) LPB_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    return LP_OK;
+}
+
+// ---- diagnostics and state I/O ----
+lp_status lp_diagnostics(lp_ctx *c, double *out10) {
+    if (!c || !out10) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    if (!c->advect_on) return fail(c, LP_ERR_INVALID, "no Poisson tables in this context");
+    const lp::Tables &T = c->T;
+    LP_TRY(poisson_on(c, c->U));  // pois2d on the state, as before the reference's moment line
+    double m[6];
+    const lp_status s = lp_moments(c, m);
+    if (s != LP_OK) return s;
+    const long long kend = (T.prm.fixes & LP_FIX_F3) ? T.size : std::min<long long>(T.size, (long long)T.prm.nx1 * T.nv3);
+    LP_CUDA(lp::launch_entropy(c->U, kend, c->mpart, kMomBlocks, c->stream));
+    std::vector<double> part(kMomBlocks);
+    LP_CUDA(cudaMemcpyAsync(part.data(), c->mpart, sizeof(double) * kMomBlocks, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    double ent = 0.;
+    for (double v : part) ent += v;
+    ent *= 0.5 * T.dv * 0.5 * T.dv * 0.5 * T.dv * 0.5 * T.dx;
+    const double ee = m[5], r = std::sqrt(ee);
+    const double vals[10] = {m[0], m[1], m[2], m[3], m[4], ee, r, std::log(r), m[4] + ee, ent};
+    std::memcpy(out10, vals, sizeof(vals));
+    return LP_OK;
+}
+
+lp_status lp_diagnostics_append(lp_ctx *c, const char *moments_path, const char *entropy_path) {
+    if (!c) return LP_ERR_INVALID;
+    double d[10];
+    const lp_status s = lp_diagnostics(c, d);
+    if (s != LP_OK) return s;
+    if (moments_path) {
+        FILE *fp = fopen(moments_path, "a");
+        if (!fp) return fail(c, LP_ERR_INVALID, std::string("cannot open ") + moments_path);
+        fprintf(fp, "%11.8g %11.8g %11.8g  %11.8g  %11.8g  %11.8g  %11.8g  %11.8g  %11.8g \n", d[0], d[1], d[2], d[3],
+                d[4], d[5], d[6], d[7], d[8]);
+        fclose(fp);
+    }
+    if (entropy_path) {
+        FILE *fp = fopen(entropy_path, "a");
+        if (!fp) return fail(c, LP_ERR_INVALID, std::string("cannot open ") + entropy_path);
+        const double l1 = std::log(std::fabs(d[9]));
+        fprintf(fp, "%11.8g %11.8g %11.8g \n", d[9], l1, std::log(std::fabs(l1)));
+        fclose(fp);
+    }
+    return LP_OK;
+}
+
+lp_status lp_marginal_x1v1(lp_ctx *c, double *out) {
+    if (!c || !out) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    const lp::Tables &T = c->T;
+    const size_t n = (size_t)T.prm.nx1 * 4 * T.nv * 4;
+    double *d = nullptr;
+    LP_CUDA(cudaMallocAsync((void **)&d, sizeof(double) * n, c->stream));
+    LP_CUDA(lp::launch_marginal_x1v1(c->U, T.prm.nx1, T.prm.nx2, T.nv, T.dx, T.dv, T.prm.lv, d, c->stream));
+    LP_CUDA(cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaFreeAsync(d, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+lp_status lp_state_append(lp_ctx *c, const char *path) {
+    if (!c || !path) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    std::vector<double> U((size_t)c->T.size * 7);
+    const lp_status s = lp_get_state(c, U.data(), U.size());
+    if (s != LP_OK) return s;
+    FILE *fp = fopen(path, "ab");
+    if (!fp) return fail(c, LP_ERR_INVALID, std::string("cannot open ") + path);
+    const size_t w = fwrite(U.data(), sizeof(double), U.size(), fp);
+    fclose(fp);
+    return w == U.size() ? LP_OK : fail(c, LP_ERR_INVALID, "short write");
+}
+
+lp_status lp_state_restart(lp_ctx *c, const char *path) {
+    if (!c || !path) return LP_ERR_INVALID;
+    const size_t n = (size_t)c->T.size * 7, bytes = n * sizeof(double);
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(c, LP_ERR_INVALID, std::string("cannot open ") + path);
+    fseek(fp, 0, SEEK_END);
+    const long len = ftell(fp);
+    if (len <= 0 || (size_t)len % bytes != 0) {
+        fclose(fp);
+        return fail(c, LP_ERR_INVALID, "file size is not a whole number of states");
+    }
+    std::vector<double> U(n);
+    fseek(fp, len - (long)bytes, SEEK_SET);
+    const size_t r = fread(U.data(), sizeof(double), n, fp);
+    fclose(fp);
+    if (r != n) return fail(c, LP_ERR_INVALID, "short read");
+    return lp_set_state(c, U.data(), n);
+}
+
+// ---- adjoint ----
+lp_status lp_field_energy(lp_ctx *c, double *J, double *lamU) {
+    if (!c || !J) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(adj_setup(c));
+    LP_TRY(field_energy_at(c, c->U, lamU));
+    LP_CUDA(cudaMemcpyAsync(J, c->adj.J, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+lp_status lp_collision_vjp(lp_ctx *c, const double *lout, double *lin, double *dnu) {
+    if (!c || !lout || !lin) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(adj_setup(c));
+    LP_TRY(collide_vjp(c, c->U, lout, lin));
+    const lp::Tables &T = c->T;
+    std::vector<double> d(std::max(T.ncollide, 1));
+    LP_CUDA(cudaMemcpyAsync(d.data(), c->adj.dnu, sizeof(double) * d.size(), cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    if (dnu) {
+        *dnu = 0.;
+        if (T.prm.nu > 0.)
+            for (int i = 0; i < T.ncollide; ++i) *dnu += d[i];
+    }
+    return LP_OK;
+}
+
+lp_status lp_advect_vjp(lp_ctx *c, const double *lout, double *lin) {
+    if (!c || !lout || !lin) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(adj_setup(c));
+    auto &A = c->adj;
+    const size_t bytes = sizeof(double) * (size_t)c->T.size * 7;
+    LP_CUDA(cudaMemcpyAsync(A.Ukeep, c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_TRY(advect(c));
+    LP_TRY(advect_vjp(c, A.Ukeep, c->U1, c->Ut, lout, lin));
+    LP_CUDA(cudaMemcpyAsync(c->U, A.Ukeep, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    return LP_OK;
+}
+
+lp_status lp_step_vjp(lp_ctx *c, const double *lout, double *lin, double *dnu) {
+    if (!c || !lout || !lin) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(adj_setup(c));
+    auto &A = c->adj;
+    const size_t bytes = sizeof(double) * (size_t)c->T.size * 7;
+    double dn = 0.;
+    LP_CUDA(cudaMemcpyAsync(A.Ukeep, c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_CUDA(cudaMemcpyAsync(lin, lout, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_TRY(step_vjp(c, A.Ukeep, lin, &dn));
+    LP_CUDA(cudaMemcpyAsync(c->U, A.Ukeep, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    if (dnu) *dnu = dn;
+    return LP_OK;
+}
+
+lp_status lp_field_energy_gradient(lp_ctx *c, int nsteps, int checkpoint, double *J, double *dU0, double *dnu) {
+    if (!c || nsteps < 0 || checkpoint < 1 || !J || !dU0) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    LP_TRY(adj_setup(c));
+    auto &A = c->adj;
+    const lp::Tables &T = c->T;
+    const size_t rec = (size_t)T.size * 7, bytes = sizeof(double) * rec;
+    // checkpoints every `checkpoint` steps (index 0: the initial state)
+    const int nck = (nsteps + checkpoint - 1) / checkpoint + 1;
+    while ((int)A.ck.size() < nck) {
+        double *p = nullptr;
+        LP_TRY(dalloc(c, &p, rec));
+        A.ck.push_back(p);
+    }
+    if (A.seg_len < checkpoint) {
+        LP_TRY(dalloc(c, &A.seg, rec * (size_t)checkpoint));
+        A.seg_len = checkpoint;
+    }
+    LP_CUDA(cudaMemcpyAsync(A.ck[0], c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    for (int s = 0; s < nsteps; ++s) {
+        if (s > 0 && s % checkpoint == 0)
+            LP_CUDA(cudaMemcpyAsync(A.ck[s / checkpoint], c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        LP_TRY(one_step(c));
+    }
+    // J and dJ/dU at the final state
+    LP_CUDA(cudaMemcpyAsync(A.Ukeep, c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_TRY(field_energy_at(c, A.Ukeep, dU0));
+    LP_CUDA(cudaMemcpyAsync(J, A.J, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    double dn = 0.;
+    for (int seg = (nsteps - 1) / checkpoint; seg >= 0 && nsteps > 0; --seg) {
+        const int s0 = seg * checkpoint, s1 = std::min(nsteps, s0 + checkpoint);
+        // recompute the segment's states from its checkpoint
+        LP_CUDA(cudaMemcpyAsync(c->U, A.ck[seg], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        for (int s = s0; s < s1; ++s) {
+            LP_CUDA(cudaMemcpyAsync(A.seg + rec * (size_t)(s - s0), c->U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+            if (s + 1 < s1) LP_TRY(one_step(c));
+        }
+        for (int s = s1 - 1; s >= s0; --s) LP_TRY(step_vjp(c, A.seg + rec * (size_t)(s - s0), dU0, &dn));
+    }
+    // the context's state is the initial state again
+    LP_CUDA(cudaMemcpyAsync(c->U, A.ck[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    if (dnu) *dnu = dn;
     return LP_OK;
 }
 

@@ -1363,6 +1363,84 @@ __global__ void k_pfields(PoissonDev pd, const double *__restrict__ b, double *_
     fields[13 * nc + ii] = ey[0] > 0. ? 1. : -1.;
 }
 
+// ---------------------------------------------------------------- diagnostics
+// Entropy int f log f (computeEntropy, EntropyCalculations.cpp:11-65): the
+// 5-point Gauss-Legendre rule in x1, v1, v2, v3 of every record, f > 0 only
+// (the x2 slope is not sampled, as in the reference).  f and f log f in FP32
+// (a diagnostic; within 1e-6 of the FP64 sum), per-record sums added in FP64.
+__constant__ float c_gl_x[5] = {0.f, -0.5384693101056831f, 0.5384693101056831f, -0.9061798459386640f,
+                                0.9061798459386640f};
+__constant__ float c_gl_w[5] = {0.5688888888888889f, 0.4786286704993665f, 0.4786286704993665f,
+                                0.2369268850561891f, 0.2369268850561891f};
+__global__ void __launch_bounds__(256) k_entropy(const double *__restrict__ U, long long kend,
+                                                double *__restrict__ part) {
+    __shared__ double red[256];
+    double acc = 0.;
+    for (long long k = blockIdx.x * 256ll + threadIdx.x; k < kend; k += 256ll * gridDim.x) {
+        const double *u = U + 7 * k;
+        const float u0 = (float)u[0], u1 = (float)u[1], u3 = (float)u[3], u4 = (float)u[4], u5 = (float)u[5],
+                    u6 = (float)u[6];
+        float s = 0.f;
+        for (int a = 0; a < 5; ++a) {
+            const float fa = u0 + u1 * 0.5f * c_gl_x[a];
+            for (int p = 0; p < 5; ++p) {
+                const float b1 = 0.5f * c_gl_x[p];
+                const float fp = fa + u3 * b1, wp = c_gl_w[a] * c_gl_w[p];
+                for (int q = 0; q < 5; ++q) {
+                    const float b2 = 0.5f * c_gl_x[q];
+                    const float fq = fp + u4 * b2, wq = wp * c_gl_w[q], s12 = b1 * b1 + b2 * b2;
+                    for (int r = 0; r < 5; ++r) {
+                        const float b3 = 0.5f * c_gl_x[r];
+                        const float f = fq + u5 * b3 + u6 * (s12 + b3 * b3);
+                        if (f > 0.f) s += wq * c_gl_w[r] * f * __logf(f);
+                    }
+                }
+            }
+        }
+        acc += (double)s;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Marginal in (x1, v1) at 4 x 4 points per (x1 cell, v1 cell) (PrintMarginal
+// with f_marg2D_x1v1, MarginalCreation.cpp:35-61, 174-197): at x1 = x_i1 +
+// (-1/2 + a/4) dx, v1 = v_j1 + (-1/2 + b/4) dv, the sum over the x2 cells
+// and the (v2, v3) cells of dx dv^2 U0 + dv^2 U1 (x1 - x_i1) + dx dv U3 (v1 -
+// v_j1) + dx U6 ((v1 - v_j1)^2 + dv^2/6) -- dx times the (v2, v3) marginal.
+// out[(i1*4 + a) * (nv*4) + j1*4 + b].
+__global__ void k_marginal_x1v1(const double *__restrict__ U, int nx1, int nx2, int nv, double dx, double dv,
+                                double lv, double *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int npv = nv * 4;
+    if (t >= nx1 * 4 * npv) return;
+    const int row = t / npv, col = t % npv;
+    const int i1 = row / 4, a = row % 4, j1 = col / 4, b = col % 4;
+    // positions formed as the reference does (left edge + quarter cells, minus the centre)
+    const double xd = __dsub_rn(__dadd_rn(__dmul_rn(((double)i1 - 0.5) + 0.5, dx), __dmul_rn((double)a, dx / 4)),
+                                __dmul_rn((double)i1 + 0.5, dx));
+    const double v1 = __dadd_rn(__dadd_rn(-lv, __dmul_rn(((double)j1 - 0.5) + 0.5, dv)), __dmul_rn((double)b, dv / 4));
+    const double vd = __dsub_rn(v1, __dadd_rn(-lv, __dmul_rn((double)j1 + 0.5, dv)));
+    const long long nv3 = (long long)nv * nv * nv;
+    double r = 0.;
+    for (int i2 = 0; i2 < nx2; ++i2)
+        for (int jj = 0; jj < nv * nv; ++jj) {
+            const double *u = U + 7 * (((long long)i1 * nx2 + i2) * nv3 + (long long)j1 * nv * nv + jj);
+            // the reference's expression order, without FMA
+            double t0 = __dmul_rn(__dmul_rn(__dmul_rn(dx, dv), dv), u[0]);
+            t0 = __dadd_rn(t0, __dmul_rn(__dmul_rn(__dmul_rn(dv, dv), u[1]), xd));
+            t0 = __dadd_rn(t0, __dmul_rn(__dmul_rn(__dmul_rn(dx, dv), u[3]), vd));
+            t0 = __dadd_rn(t0, __dmul_rn(__dmul_rn(dx, u[6]), __dadd_rn(__dmul_rn(vd, vd), __ddiv_rn(__dmul_rn(dv, dv), 6.))));
+            r = __dadd_rn(r, t0);
+        }
+    out[t] = r;
+}
+
 // ---------------------------------------------------------------- FMA peaks
 // Eight independent dependent chains per thread of packed FP32x2 FMAs (two
 // FMAs each) or of FP64 FMAs; the result is written so nothing is elided.
@@ -1543,7 +1621,8 @@ cudaError_t launch_lines_table(const double *eta, const double *shat, const doub
 
 namespace {
 template <int N, int T, int LW>
-void launch_tiles(const float2 *F, const float *W, const long long *line_off, int Bp, double2 *q, cudaStream_t st) {
+void launch_tiles(const float2 *F, const float *W, const long long *line_off, int Bp, double2 *q, cudaStream_t st,
+                  cudaStream_t st_odd) {
     constexpr int NT = N / LinesCfg<N>::KT;
     if constexpr (T < NT) {
         const unsigned blocks = (unsigned)((long long)N * N * (Bp / 32));
@@ -1553,19 +1632,19 @@ void launch_tiles(const float2 *F, const float *W, const long long *line_off, in
             cudaFuncSetAttribute(k_cq_lines<N, T, LW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr_set = true;
         }
-        k_cq_lines<N, T, LW><<<blocks, 32 * LW, smem, st>>>(F, W, line_off, Bp, q);
-        launch_tiles<N, T + 1, LW>(F, W, line_off, Bp, q, st);
+        k_cq_lines<N, T, LW><<<blocks, 32 * LW, smem, (T & 1) ? st_odd : st>>>(F, W, line_off, Bp, q);
+        launch_tiles<N, T + 1, LW>(F, W, line_off, Bp, q, st, st_odd);
     }
 }
 
 template <int LW>
 cudaError_t computeq_lines(const float2 *F, const float *W, const long long *line_off, int n, int Bp, double2 *q,
-                           cudaStream_t st) {
+                           cudaStream_t st, cudaStream_t st_odd) {
     switch (n) {
-    case 8: launch_tiles<8, 0, LW>(F, W, line_off, Bp, q, st); break;
-    case 16: launch_tiles<16, 0, LW>(F, W, line_off, Bp, q, st); break;
-    case 24: launch_tiles<24, 0, LW>(F, W, line_off, Bp, q, st); break;
-    case 32: launch_tiles<32, 0, LW>(F, W, line_off, Bp, q, st); break;
+    case 8: launch_tiles<8, 0, LW>(F, W, line_off, Bp, q, st, st_odd); break;
+    case 16: launch_tiles<16, 0, LW>(F, W, line_off, Bp, q, st, st_odd); break;
+    case 24: launch_tiles<24, 0, LW>(F, W, line_off, Bp, q, st, st_odd); break;
+    case 32: launch_tiles<32, 0, LW>(F, W, line_off, Bp, q, st, st_odd); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1573,9 +1652,10 @@ cudaError_t computeq_lines(const float2 *F, const float *W, const long long *lin
 }  // namespace
 
 cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n, int Bp,
-                                  double2 *q, cudaStream_t st, int warps) {
-    if (warps == 4) return computeq_lines<4>(F, W, line_off, n, Bp, q, st);
-    if (warps == 2) return computeq_lines<2>(F, W, line_off, n, Bp, q, st);
+                                  double2 *q, cudaStream_t st, int warps, cudaStream_t st_odd) {
+    if (!st_odd) st_odd = st;
+    if (warps == 4) return computeq_lines<4>(F, W, line_off, n, Bp, q, st, st_odd);
+    if (warps == 2) return computeq_lines<2>(F, W, line_off, n, Bp, q, st, st_odd);
     return cudaErrorInvalidValue;
 }
 
@@ -1686,6 +1766,18 @@ cudaError_t launch_poisson_dense(const PoissonDev &pd, const double *base, const
     k_prhs<<<(nc + 7) / 8, 256, 0, st>>>(pd, base, inc, iscale, npart, b);
     k_psolve_dense<<<(pd.ndim + 7) / 8, 256, 0, st>>>(Ainv, b, pd.ndim, potc);
     k_pfields<<<(nc + 127) / 128, 128, 0, st>>>(pd, potc, phix, phiy, fields);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_entropy(const double *U, long long kend, double *part, int nblk, cudaStream_t st) {
+    k_entropy<<<nblk, 256, 0, st>>>(U, kend, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_marginal_x1v1(const double *U, int nx1, int nx2, int nv, double dx, double dv, double lv,
+                                 double *out, cudaStream_t st) {
+    const int total = nx1 * 4 * nv * 4;
+    k_marginal_x1v1<<<(total + 127) / 128, 128, 0, st>>>(U, nx1, nx2, nv, dx, dv, lv, out);
     return cudaGetLastError();
 }
 

@@ -76,8 +76,11 @@ cudaError_t launch_lines_table(const double *eta, const double *shat, const doub
                                const unsigned char *rzero, const double *cw, const long long *line_off,
                                int n, float *W, cudaStream_t st);
 // warps (2 or 4): warps of a block splitting the plane pairs of one line.
+// Odd k-tiles go to st_odd (nullptr: st); the caller orders st_odd after
+// the tile inputs and joins it back (the tiles write disjoint outputs).
 cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long long *line_off, int n,
-                                  int Bp, double2 *q, cudaStream_t st, int warps = 2);
+                                  int Bp, double2 *q, cudaStream_t st, int warps = 2,
+                                  cudaStream_t st_odd = nullptr);
 
 // Moment-conserving projection of q in place (FP64).
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
@@ -164,6 +167,15 @@ cudaError_t launch_flux_inc(const AdvectDev &ad, int stage, const float *Uin, co
 cudaError_t launch_poisson_dense(const PoissonDev &pd, const double *base, const float *inc, double iscale,
                                  int npart, const double *Ainv, double *b, double *potc, double *phix,
                                  double *phiy, double *fields, cudaStream_t st);
+
+// ---- diagnostics ----
+// Block partial sums of int f log f over records [0, kend) (5-point Gauss
+// rule; multiply the sum by (dv/2)^3 dx/2).
+cudaError_t launch_entropy(const double *U, long long kend, double *part, int nblk, cudaStream_t st);
+// The reference's (x1, v1) marginal at 4 x 4 points per cell pair:
+// out[nx1*4][nv*4].
+cudaError_t launch_marginal_x1v1(const double *U, int nx1, int nx2, int nv, double dx, double dv, double lv,
+                                 double *out, cudaStream_t st);
 
 // FMA-throughput microbenchmarks (FP32 packed f32x2 and FP64).
 cudaError_t launch_fma_peak(bool fp64, int blocks, int iters, double *sink, cudaStream_t st);

@@ -39,6 +39,8 @@ EXPORTS = [
     "lp_batch_last_error", "lp_batch_device_bytes", "lp_batch_set_state", "lp_batch_get_state",
     "lp_batch_set_init", "lp_batch_moments", "lp_batch_advect_step", "lp_batch_collision_step",
     "lp_batch_step", "lp_batch_classes", "lp_batch_class_info", "lp_batch_autotune",
+    "lp_field_energy", "lp_collision_vjp", "lp_advect_vjp", "lp_step_vjp", "lp_field_energy_gradient",
+    "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -140,6 +142,16 @@ def lib():
         L.lp_batch_classes.argtypes = [_vp]
         L.lp_batch_class_info.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp]
         L.lp_batch_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p]
+        L.lp_field_energy.argtypes = [_vp, _dp, _vp]
+        L.lp_collision_vjp.argtypes = [_vp, _vp, _vp, _dp]
+        L.lp_advect_vjp.argtypes = [_vp, _vp, _vp]
+        L.lp_step_vjp.argtypes = [_vp, _vp, _vp, _dp]
+        L.lp_field_energy_gradient.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _vp, _dp]
+        L.lp_diagnostics.argtypes = [_vp, _dp]
+        L.lp_diagnostics_append.argtypes = [_vp, ctypes.c_char_p, ctypes.c_char_p]
+        L.lp_marginal_x1v1.argtypes = [_vp, _dp]
+        L.lp_state_append.argtypes = [_vp, ctypes.c_char_p]
+        L.lp_state_restart.argtypes = [_vp, ctypes.c_char_p]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
@@ -299,6 +311,53 @@ class Context:
         out = np.zeros(6)
         self._chk(self.L.lp_moments(self.h, _p(out)))
         return out
+
+    def diagnostics(self):
+        """{mass, p1, p2, p3, KiE, EleE, sqrt EleE, log sqrt EleE, KiE + EleE, entropy}"""
+        out = np.zeros(10)
+        self._chk(self.L.lp_diagnostics(self.h, _p(out)))
+        return out
+
+    def diagnostics_append(self, moments_path=None, entropy_path=None):
+        self._chk(self.L.lp_diagnostics_append(self.h, moments_path.encode() if moments_path else None,
+                                               entropy_path.encode() if entropy_path else None))
+
+    def marginal_x1v1(self):
+        out = np.zeros(self.params.nx1 * 4 * self.params.nv * 4)
+        self._chk(self.L.lp_marginal_x1v1(self.h, _p(out)))
+        return out.reshape(self.params.nx1 * 4, self.params.nv * 4)
+
+    def state_append(self, path):
+        self._chk(self.L.lp_state_append(self.h, path.encode()))
+
+    def state_restart(self, path):
+        self._chk(self.L.lp_state_restart(self.h, path.encode()))
+
+    # adjoint: device pointers (e.g. torch tensors' data_ptr()) of state-sized
+    # FP64 vectors
+    def field_energy(self, lam_ptr=None):
+        J = ctypes.c_double()
+        self._chk(self.L.lp_field_energy(self.h, ctypes.byref(J), _vp(lam_ptr) if lam_ptr else None))
+        return J.value
+
+    def collision_vjp(self, lam_out_ptr, lam_in_ptr):
+        d = ctypes.c_double()
+        self._chk(self.L.lp_collision_vjp(self.h, _vp(lam_out_ptr), _vp(lam_in_ptr), ctypes.byref(d)))
+        return d.value
+
+    def advect_vjp(self, lam_out_ptr, lam_in_ptr):
+        self._chk(self.L.lp_advect_vjp(self.h, _vp(lam_out_ptr), _vp(lam_in_ptr)))
+
+    def step_vjp(self, lam_out_ptr, lam_in_ptr):
+        d = ctypes.c_double()
+        self._chk(self.L.lp_step_vjp(self.h, _vp(lam_out_ptr), _vp(lam_in_ptr), ctypes.byref(d)))
+        return d.value
+
+    def field_energy_gradient(self, nsteps, checkpoint, dU0_ptr):
+        J, d = ctypes.c_double(), ctypes.c_double()
+        self._chk(self.L.lp_field_energy_gradient(self.h, int(nsteps), int(checkpoint), ctypes.byref(J),
+                                                  _vp(dU0_ptr), ctypes.byref(d)))
+        return J.value, d.value
 
 
 class Batch:

@@ -1257,3 +1257,69 @@ void lpo_grids(const lpo_ctx *c, double *v, double *eta, double *wt, double *sc)
         memcpy(sc, s, sizeof(s));
     }
 }
+
+
+/* Entropy int f log f (EntropyCalculations.cpp:11-65): 5-point Gauss rule in
+ * x1, v1, v2, v3 over the records of the first nx1 spatial cells (cells
+ * s < nx1, as the reference's loop i < Nx), f > 0 only. */
+double lpo_entropy(const lpo_ctx *c, const double *U)
+{
+    static const double wt5[5] = {0.5688888888888889, 0.4786286704993665, 0.4786286704993665,
+                                  0.2369268850561891, 0.2369268850561891};
+    static const double vt5[5] = {0., -0.5384693101056831, 0.5384693101056831, -0.9061798459386640,
+                                  0.9061798459386640};
+    const int nv = c->p.nv;
+    const double dv = c->dv, dx = c->dx;
+    long ncell = (c->p.fixes & LPO_FIX_F3) ? (long)c->p.nx1 * c->p.nx2 : c->p.nx1;
+    if (ncell > (long)c->p.nx1 * c->p.nx2) ncell = (long)c->p.nx1 * c->p.nx2;
+    double ent = 0.;
+    for (long i = 0; i < ncell; ++i)
+        for (int j1 = 0; j1 < nv; ++j1)
+            for (int j2 = 0; j2 < nv; ++j2)
+                for (int j3 = 0; j3 < nv; ++j3) {
+                    const long k = i * c->nv3 + ((long)j1 * nv + j2) * nv + j3;
+                    const double *u = U + 7 * k;
+                    for (int nx = 0; nx < 5; ++nx)
+                        for (int a = 0; a < 5; ++a)
+                            for (int b = 0; b < 5; ++b)
+                                for (int e = 0; e < 5; ++e) {
+                                    const double xd = 0.5 * vt5[nx] * dx / dx, v1 = 0.5 * vt5[a] * dv / dv,
+                                                 v2 = 0.5 * vt5[b] * dv / dv, v3 = 0.5 * vt5[e] * dv / dv;
+                                    const double f = u[0] + u[1] * xd + u[3] * v1 + u[4] * v2 + u[5] * v3 +
+                                                     u[6] * (v1 * v1 + v2 * v2 + v3 * v3);
+                                    if (f > 0) ent += wt5[nx] * wt5[a] * wt5[b] * wt5[e] * f * log(f);
+                                }
+                }
+    return ent * 0.5 * dv * 0.5 * dv * 0.5 * dv * 0.5 * dx;
+}
+
+/* The (x1, v1) marginal of PrintMarginal / f_marg2D_x1v1
+ * (MarginalCreation.cpp:35-61, 174-197) at 4 x 4 points per cell pair:
+ * out[(i1*4 + a) * (nv*4) + j1*4 + b]. */
+void lpo_marginal_x1v1(const lpo_ctx *c, const double *U, double *out)
+{
+    const int nv = c->p.nv, nx1 = c->p.nx1, nx2 = c->p.nx2;
+    const double dv = c->dv, dx = c->dx;
+    const double ddx = dx / 4, ddv = dv / 4;
+    long o = 0;
+    /* sample positions as the reference forms them: left cell edge plus
+     * multiples of a quarter cell, then the offset from the centre */
+    for (int i1 = 0; i1 < nx1; ++i1)
+        for (int a = 0; a < 4; ++a) {
+            const double x1 = (((double)i1 - 0.5) + 0.5) * dx + a * ddx;
+            const double xd = x1 - ((double)i1 + 0.5) * dx;
+            for (int j1 = 0; j1 < nv; ++j1)
+                for (int b = 0; b < 4; ++b) {
+                    const double v1 = gridv(c, (double)j1 - 0.5) + b * ddv;
+                    const double vd = v1 - gridv(c, (double)j1);
+                    double r = 0.;
+                    for (int i2 = 0; i2 < nx2; ++i2)
+                        for (int jj = 0; jj < nv * nv; ++jj) {
+                            const double *u = U + 7 * (((long)i1 * nx2 + i2) * c->nv3 + (long)j1 * nv * nv + jj);
+                            r += dx * dv * dv * u[0] + dv * dv * u[1] * xd + dx * dv * u[3] * vd +
+                                 dx * u[6] * (vd * vd + dv * dv / 6.);
+                        }
+                    out[o++] = r;
+                }
+        }
+}

@@ -65,6 +65,8 @@ void lpo_step(const lpo_ctx *c, double *U, int direct);
 void lpo_moments(const lpo_ctx *c, const double *U, const double *phix, const double *phiy,
                  double *out6);
 void lpo_band(const lpo_ctx *c, int *dims, double *ab, int *ipiv);
+double lpo_entropy(const lpo_ctx *c, const double *U);
+void lpo_marginal_x1v1(const lpo_ctx *c, const double *U, double *out);
 
 #ifdef __cplusplus
 }

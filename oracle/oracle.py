@@ -99,6 +99,10 @@ def _oracle_lib():
                      "lpo_band"]:
             getattr(L, name).restype = None
         L.lpo_collide.restype = ctypes.c_int
+        L.lpo_entropy.restype = ctypes.c_double
+        L.lpo_entropy.argtypes = [ctypes.c_void_p, _dp]
+        L.lpo_marginal_x1v1.restype = None
+        L.lpo_marginal_x1v1.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.lpo_intmodes.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 6 + [_dp]
         L.lpo_rk4.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_int]
         L.lpo_nodes.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp]
@@ -223,6 +227,14 @@ class Oracle:
                            _p(out))
         return out
 
+    def entropy(self, U):
+        return float(self.L.lpo_entropy(self.h, _p(np.ascontiguousarray(U, dtype=np.float64))))
+
+    def marginal_x1v1(self, U):
+        out = np.zeros(self.case.nx1 * 4 * self.case.nv * 4)
+        self.L.lpo_marginal_x1v1(self.h, _p(np.ascontiguousarray(U, dtype=np.float64)), _p(out))
+        return out.reshape(self.case.nx1 * 4, self.case.nv * 4)
+
     def band(self):
         dims = np.zeros(4, np.int32)
         self.L.lpo_band(self.h, _p(dims), None, None)
@@ -255,6 +267,10 @@ def _ref_lib():
         L.ref_get_weights.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
         L.ref_collision_cells.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
         L.ref_get_band.argtypes = [_ip, _dp, _ip]
+        L.ref_entropy.argtypes = [_dp]
+        L.ref_entropy.restype = ctypes.c_double
+        L.ref_marginal_x1v1.argtypes = [_dp, _dp]
+        L.ref_marginal_x1v1.restype = None
         _rlib = L
     return _rlib
 
@@ -365,6 +381,14 @@ class Reference:
         du = np.zeros((l1 - l0) * self.nv3 * 5)
         assert self.L.ref_collision_cells(_p(U), int(l0), int(l1), _p(du)) == 0
         return du
+
+    def entropy(self, U):
+        return float(self.L.ref_entropy(_p(np.ascontiguousarray(U, dtype=np.float64))))
+
+    def marginal_x1v1(self, U):
+        out = np.zeros(self.case.nx1 * 4 * self.case.nv * 4)
+        self.L.ref_marginal_x1v1(_p(np.ascontiguousarray(U, dtype=np.float64)), _p(out))
+        return out.reshape(self.case.nx1 * 4, self.case.nv * 4)
 
     def moments(self, U, phix, phiy):
         out = np.zeros(6)

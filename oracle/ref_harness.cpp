@@ -8,6 +8,8 @@
 //
 // Test infrastructure only; never linked into the shipped library.
 #include "LP_ompi.h"
+#include "EntropyCalculations.h"
+#include "MarginalCreation.h"
 
 #include <cstring>
 #include <vector>
@@ -44,6 +46,9 @@ static void release_all() {
     free(wtN); free(v); free(eta);
     wtN = v = eta = nullptr;
 }
+
+// defined in MarginalCreation.cpp:35 without a declaration in its header
+double f_marg2D_x1v1(std::vector<double> &U_vals0, int i1, int j1, double x1, double v1);
 
 extern "C" {
 
@@ -297,6 +302,32 @@ void ref_moments(const double *U, const double *phix, const double *phiy, double
     out[1] = a[0]; out[2] = a[1]; out[3] = a[2];
     out[4] = computeKiE(g_U);
     out[5] = computeEleE(g_phix, g_phiy);
+}
+
+// Entropy (computeEntropy, EntropyCalculations.cpp:11) of U.
+double ref_entropy(const double *U) {
+    memcpy(g_U.data(), U, sizeof(double) * 7 * (size_t)size);
+    return computeEntropy(g_U);
+}
+
+
+// The (x1, v1) marginal values PrintMarginal writes (MarginalCreation.cpp:174-197),
+// out[(i1*4 + nx) * (Nv*4) + j1*4 + nv].
+void ref_marginal_x1v1(const double *U, double *out) {
+    memcpy(g_U.data(), U, sizeof(double) * 7 * (size_t)size);
+    const int np = 4;
+    const double ddx = dx / np, ddv = dv / np;
+    size_t o = 0;
+    for (int i1 = 0; i1 < Nx; i1++) {
+        const double x1_0 = Gridx((double)i1 - 0.5);
+        for (int nx = 0; nx < np; nx++) {
+            const double x1_val = x1_0 + nx * ddx;
+            for (int j1 = 0; j1 < Nv; j1++) {
+                const double v1_0 = Gridv((double)j1 - 0.5);
+                for (int nv = 0; nv < np; nv++) out[o++] = f_marg2D_x1v1(g_U, i1, j1, x1_val, v1_0 + nv * ddv);
+            }
+        }
+    }
 }
 
 }  // extern "C"

@@ -76,6 +76,7 @@ def make(name, case, rng):
     out.update(rk3_in=Up, rk3_out=U3)
     out.update(coll_in=Up, coll_du=R.collision_cells(Up, 0, case.nx1))
     out.update(moments=R.moments(U3, x3, y3), moments_phix=x3, moments_phiy=y3)
+    out.update(entropy=np.float64(R.entropy(U3)), marginal_x1v1=R.marginal_x1v1(U3))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")

@@ -104,3 +104,17 @@ def test_moments(gold):
     m = O.moments(g["rk3_out"], g["moments_phix"], g["moments_phiy"])
     # the reference reduces these sums in OpenMP order; the momentum sums cancel
     assert np.allclose(m, g["moments"], rtol=1e-13, atol=1e-14 * abs(g["moments"][0]))
+
+
+def test_entropy(gold):
+    g, O = gold
+    # int f log f over the first nx1 spatial cells (the reference's i < Nx),
+    # summed in OpenMP order by the reference
+    e = O.entropy(g["rk3_out"])
+    assert abs(e - float(g["entropy"])) <= 1e-13 * abs(float(g["entropy"]))
+
+
+def test_marginal_x1v1(gold):
+    g, O = gold
+    m = O.marginal_x1v1(g["rk3_out"])
+    assert np.array_equal(m.ravel(), g["marginal_x1v1"].ravel())
