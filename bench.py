@@ -36,6 +36,10 @@ WORKLOAD = dict(nx1=64, nx2=1, nv=24, n=24, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.
 METRIC = "collision+conserve cell-steps/s"
 UNIT = "cell-steps/s"
 L2_FLUSH_BYTES = 512 << 20
+# DRAM bytes of one contraction of this workload (both k-tiles of k_cq_lines,
+# dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
+# `bench.py --steps 2 --warmup 1 --no-cpu-baseline --fp64-steps 0`)
+CONTRACT_TRAFFIC_BYTES = 105.24e6 + 100.49e6
 # kernels of one mixed collision step at n = 24: nodes 1, forward transform
 # 3 x 4, contraction 2 tiles x 4, conservation 3 x 4, inverse transform 3 x 3,
 # DG projection 4, moment reconciliation 4, scatter 1
@@ -414,7 +418,9 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                         "d2h_bytes_per_step": nbytes},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                             "frac": achieved / peak,
+                             "traffic": CONTRACT_TRAFFIC_BYTES if args.precision == "mixed" else None,
+                             "algorithmic_bytes": contract_bytes, "peak_kind": peak_kind,
                              "kernel": "k_cq_lines (weighted contraction of ComputeQ, all tiles)",
                              "ms_per_launch": t_contract_ms,
                              "note": "the contraction is bound by the FP32 FMA pipe, see compute_roofline"},
