@@ -136,6 +136,17 @@ lp_status lp_step(lp_ctx *ctx, int nsteps);
  * Poisson solve}. */
 lp_status lp_moments(lp_ctx *ctx, double *out6);
 
+/* ---- schedule autotuner (no reference counterpart) ----------------------- */
+/* Times one collision step of the resident state (best of `reps` after a
+ * warm-up, CUDA events, the state restored before each run) for every
+ * candidate schedule -- cells per pass 64, 128, ... up to the workspace's
+ * capacity, and 2 or 4 warps per block of the line-tiled contraction -- and
+ * keeps the fastest; with cache_path, a schedule recorded there for the same
+ * key (n, nv, lv, cells, precision, device) is reused and new ones appended.
+ * The chosen schedule is returned in pass_cells and line_warps (optional).
+ * Leaves the state as it was. */
+lp_status lp_autotune(lp_ctx *ctx, int reps, const char *cache_path, int *pass_cells, int *line_warps);
+
 /* ---- measurement helpers (no reference counterpart) --------------------- */
 /* Average device time in ms of one launch of a hot-path stage on the
  * context's stream, over `reps` launches after one warm-up, timed with CUDA

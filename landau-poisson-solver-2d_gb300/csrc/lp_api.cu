@@ -271,6 +271,8 @@ lp::AdvectDev advect_dev(const lp_ctx *c) {
     a.lv = T.prm.lv; a.dv = T.dv; a.dx = T.dx; a.scalev = T.scalev; a.dt = T.prm.dt;
     a.rdv = 1.0 / T.dv; a.inv = 1.0 / T.dx / T.scalev;
     a.dt_f = (float)T.prm.dt; a.dt6 = T.prm.dt / 6.;
+    a.f.lv = (float)a.lv; a.f.dv = (float)a.dv; a.f.rdv = (float)a.rdv; a.f.scalev = (float)a.scalev;
+    a.f.inv = (float)a.inv;
     return a;
 }
 
@@ -381,7 +383,8 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp) {
     return LP_OK;
 }
 
-template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp) {
+// defer_fix: the mixed path's moment correction is left to the scatter
+template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool defer_fix = false) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     static const int fixed_slots[5] = {0, 3, 4, 5, 6}, ref_slots[5] = {0, 2, 3, 4, 5};
@@ -394,7 +397,8 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp) {
         const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
         LP_CUDA(lp::launch_moment_fix(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
                                       c->mtpart, c->U, T.nv, T.dv, T.prm.lv, c0, B, c->nrc, c->mapart, c->gm_inv,
-                                      T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream, rates_at(c, c0)));
+                                      T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream, rates_at(c, c0),
+                                      !defer_fix));
     }
     return LP_OK;
 }
@@ -411,7 +415,7 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_TRY(contract<R>(c, Bp, c->q[0]));
     LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
     LP_TRY(rk4_stages<R>(c, c0, Bp));
-    LP_TRY(project<R>(c, c0, B, Bp));
+    LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
 }
 
@@ -443,7 +447,9 @@ lp_status collide(lp_ctx *c, int c0, int c1) {
         if (total > pass && !(c->T.prm.fixes & LP_FIX_F1))
             return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one batch");
         LP_TRY(c->mixed ? collide_batch<float>(c, b0, B) : collide_batch<double>(c, b0, B));
-        LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream));
+        const bool fix = c->mixed && (c->T.prm.fixes & LP_FIX_F1);
+        LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream, fix ? c->mlam : nullptr, c->T.nv, c->T.dv,
+                                   c->T.prm.lv));
     }
     return LP_OK;
 }
@@ -1272,44 +1278,117 @@ bool batch_ready(lp_batch *b) {
     return true;
 }
 
-std::string class_key(const lp_batch::Cls &k) {
-    const lp::Tables &T = k.eng->T;
+// ---- autotuner (shared by contexts and batch classes) ----
+// Key of a collision engine's schedule: n, nv, lv, collided cells, precision
+// and device name.
+std::string engine_key(const lp_ctx *e, int ncell) {
+    const lp::Tables &T = e->T;
     cudaDeviceProp prop{};
-    cudaGetDeviceProperties(&prop, k.eng->device);
+    cudaGetDeviceProperties(&prop, e->device);
     char buf[512];
-    snprintf(buf, sizeof(buf), "n%d_nv%d_lv%.17g_cells%d_%s_%s", T.n, T.nv, T.prm.lv, k.ncell,
-             k.eng->mixed ? "mixed" : "fp64", prop.name);
+    snprintf(buf, sizeof(buf), "n%d_nv%d_lv%.17g_cells%d_%s_%s", T.n, T.nv, T.prm.lv, ncell,
+             e->mixed ? "mixed" : "fp64", prop.name);
     std::string s(buf);
     for (char &ch : s)
         if (ch == ' ') ch = '-';
     return s;
 }
 
-// Time one collision step of class k with the current schedule: the class
-// state is restored from its copy in `backup` before every run, and only the
-// collision is inside the events.
-lp_status time_class(lp_batch *b, lp_batch::Cls &k, double *backup, int reps, double *ms) {
-    lp_ctx *e = k.eng;
+std::vector<std::string> read_tune_cache(const char *path) {
+    std::vector<std::string> lines;
+    if (path) {
+        if (FILE *fp = fopen(path, "r")) {
+            char line[768];
+            while (fgets(line, sizeof(line), fp)) lines.emplace_back(line);
+            fclose(fp);
+        }
+    }
+    return lines;
+}
+
+void write_tune_cache(const char *path, const std::vector<std::string> &lines) {
+    if (!path) return;
+    if (FILE *fp = fopen(path, "w")) {
+        for (const auto &l : lines) fputs(l.c_str(), fp);
+        fclose(fp);
+    }
+}
+
+// Applies a cached schedule for `key` to e; returns whether one was found.
+bool tune_lookup(const std::vector<std::string> &lines, const std::string &key, lp_ctx *e, double *ms) {
+    bool found = false;
+    for (const auto &l : lines) {
+        char kbuf[512];
+        int bp = 0, lw = 0;
+        double t = 0.;
+        if (sscanf(l.c_str(), "%511s %d %d %lf", kbuf, &bp, &lw, &t) == 4 && key == kbuf && bp >= 32 &&
+            bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4 || !e->LW)) {
+            e->Bpass = bp;
+            e->line_warps = e->LW ? lw : 2;
+            *ms = t;
+            found = true;
+        }
+    }
+    return found;
+}
+
+// One collision step of cells [0, ncell) of engine e with its current
+// schedule, best of `reps` after a warm-up (CUDA events on st); the state is
+// restored from `backup` before every run and only the collision is timed.
+lp_status time_engine(lp_ctx *e, int ncell, cudaStream_t st, const double *backup, int reps, double *ms) {
+    lp_ctx *c = e;
     const size_t bytes = sizeof(double) * (size_t)e->T.size * 7;
     cudaEvent_t e0, e1;
-    LPB_CUDA(cudaEventCreate(&e0));
-    LPB_CUDA(cudaEventCreate(&e1));
-    e->stream = b->stream;
+    LP_CUDA(cudaEventCreate(&e0));
+    LP_CUDA(cudaEventCreate(&e1));
+    cudaStream_t keep = e->stream;
+    e->stream = st;
     double best = 1e300;
-    for (int i = 0; i <= reps; ++i) {  // the first run is a warm-up
-        LPB_CUDA(cudaMemcpyAsync(e->U, backup, bytes, cudaMemcpyDeviceToDevice, b->stream));
-        LPB_CUDA(cudaEventRecord(e0, b->stream));
-        const lp_status s = collide(e, 0, k.ncell);
-        if (s != LP_OK) return bfail(b, s, "autotune: " + e->err);
-        LPB_CUDA(cudaEventRecord(e1, b->stream));
-        LPB_CUDA(cudaEventSynchronize(e1));
+    lp_status s = LP_OK;
+    for (int i = 0; i <= reps && s == LP_OK; ++i) {
+        cudaMemcpyAsync(e->U, backup, bytes, cudaMemcpyDeviceToDevice, st);
+        cudaEventRecord(e0, st);
+        s = collide(e, 0, ncell);
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) s = LP_ERR_CUDA;
         float t = 0.f;
-        LPB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventElapsedTime(&t, e0, e1);
         if (i > 0) best = std::min(best, (double)t);
     }
+    e->stream = keep;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = best;
+    return s;
+}
+
+// Picks the fastest schedule of engine e for cells [0, ncell): cells per pass
+// 64, 128, ... up to the workspace capacity, and 2 or 4 warps per line block
+// of the line-tiled contraction.  e->U1 holds the state meanwhile.
+lp_status tune_engine(lp_ctx *e, int ncell, cudaStream_t st, int reps, double *best_ms) {
+    lp_ctx *c = e;
+    const size_t bytes = sizeof(double) * (size_t)e->T.size * 7;
+    std::vector<int> passes;
+    for (int bp = 64; bp < e->Bcap; bp *= 2) passes.push_back(bp);
+    passes.push_back(e->Bcap);
+    std::vector<int> warps = {2};
+    if (e->LW) warps.push_back(4);
+    LP_CUDA(cudaMemcpyAsync(e->U1, e->U, bytes, cudaMemcpyDeviceToDevice, st));
+    double best = 1e300;
+    int bbp = e->Bcap, blw = 2;
+    for (int bp : passes)
+        for (int lw : warps) {
+            e->Bpass = bp;
+            e->line_warps = lw;
+            double ms = 0.;
+            LP_TRY(time_engine(e, ncell, st, e->U1, reps, &ms));
+            if (ms < best) { best = ms; bbp = bp; blw = lw; }
+        }
+    LP_CUDA(cudaMemcpyAsync(e->U, e->U1, bytes, cudaMemcpyDeviceToDevice, st));
+    LP_CUDA(cudaStreamSynchronize(st));
+    e->Bpass = bbp;
+    e->line_warps = blw;
+    *best_ms = best;
     return LP_OK;
 }
 
@@ -1702,66 +1781,41 @@ lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path) {
     if (!b || reps < 1) return LP_ERR_INVALID;
     if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
     LPB_CUDA(cudaStreamSynchronize(b->stream));
-    // cached schedules: lines "key pass_cells line_warps ms"
-    std::vector<std::string> cache_lines;
-    if (cache_path) {
-        if (FILE *fp = fopen(cache_path, "r")) {
-            char line[512];
-            while (fgets(line, sizeof(line), fp)) cache_lines.emplace_back(line);
-            fclose(fp);
-        }
-    }
+    std::vector<std::string> lines = read_tune_cache(cache_path);  // "key pass_cells line_warps ms"
     bool changed = false;
     for (auto &K : b->cls) {
-        lp_ctx *e = K.eng;
-        const std::string key = class_key(K);
-        bool found = false;
-        for (const auto &l : cache_lines) {
-            char kbuf[400];
-            int bp = 0, lw = 0;
-            double ms = 0.;
-            if (sscanf(l.c_str(), "%399s %d %d %lf", kbuf, &bp, &lw, &ms) == 4 && key == kbuf && bp >= 32 &&
-                bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4)) {
-                e->Bpass = bp; e->line_warps = lw; K.tuned_ms = ms;
-                found = true;
-            }
-        }
-        if (found || !K.collide) continue;
-        // candidates: passes of 64..Bcap cells (every pass one launch set),
-        // and 2 or 4 warps per line block in the line-tiled contraction
-        std::vector<int> passes;
-        for (int bp = 64; bp < e->Bcap; bp *= 2) passes.push_back(bp);
-        passes.push_back(e->Bcap);
-        std::vector<int> warps = {2};
-        if (e->LW) warps.push_back(4);
-        LPB_CUDA(cudaMemcpyAsync(e->U1, e->U, sizeof(double) * (size_t)e->T.size * 7, cudaMemcpyDeviceToDevice,
-                                 b->stream));
-        double best = 1e300;
-        int bbp = e->Bcap, blw = 2;
-        for (int bp : passes)
-            for (int lw : warps) {
-                e->Bpass = bp; e->line_warps = lw;
-                double ms = 0.;
-                const lp_status s = time_class(b, K, e->U1, reps, &ms);
-                if (s != LP_OK) return s;
-                if (ms < best) { best = ms; bbp = bp; blw = lw; }
-            }
-        LPB_CUDA(cudaMemcpyAsync(e->U, e->U1, sizeof(double) * (size_t)e->T.size * 7, cudaMemcpyDeviceToDevice,
-                                 b->stream));
-        LPB_CUDA(cudaStreamSynchronize(b->stream));
-        e->Bpass = bbp; e->line_warps = blw; K.tuned_ms = best;
+        const std::string key = engine_key(K.eng, K.ncell);
+        if (tune_lookup(lines, key, K.eng, &K.tuned_ms) || !K.collide) continue;
+        const lp_status s = tune_engine(K.eng, K.ncell, b->stream, reps, &K.tuned_ms);
+        if (s != LP_OK) return bfail(b, s, "autotune: " + K.eng->err);
         char line[768];
-        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), bbp, blw, best);
-        cache_lines.emplace_back(line);
+        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), K.eng->Bpass, K.eng->line_warps, K.tuned_ms);
+        lines.emplace_back(line);
         changed = true;
     }
-    if (changed && cache_path) {
-        if (FILE *fp = fopen(cache_path, "w")) {
-            for (const auto &l : cache_lines) fputs(l.c_str(), fp);
-            fclose(fp);
-        }
-    }
+    if (changed) write_tune_cache(cache_path, lines);
     if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }  // recapture with the new schedule
+    return LP_OK;
+}
+
+lp_status lp_autotune(lp_ctx *c, int reps, const char *cache_path, int *pass_cells, int *line_warps) {
+    if (!c || reps < 1) return LP_ERR_INVALID;
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    if (!c->collide_on) return fail(c, LP_ERR_INVALID, "no collision tables in this context");
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<std::string> lines = read_tune_cache(cache_path);
+    const std::string key = engine_key(c, c->T.ncollide);
+    double ms = 0.;
+    if (!tune_lookup(lines, key, c, &ms) && c->T.ncollide > 0) {
+        LP_TRY(tune_engine(c, c->T.ncollide, c->stream, reps, &ms));
+        char line[768];
+        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), c->Bpass, c->line_warps, ms);
+        lines.emplace_back(line);
+        write_tune_cache(cache_path, lines);
+    }
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }  // recapture with the new schedule
+    if (pass_cells) *pass_cells = c->Bpass;
+    if (line_warps) *line_warps = c->line_warps;
     return LP_OK;
 }
 

@@ -96,8 +96,13 @@ __global__ void k_nodes(const double *__restrict__ U, int nv, int n, int c0, int
 // ---------------------------------------------------------------- DFT pass
 // out(pencil)[p][c] = sum_a M[p][a] in(pencil)[a][c] along axis ax of an
 // n x n x n x Bp array; M holds the per-axis DFT with the fft3D/FS phases and
-// scalings folded in.  Block (32 cells, n outputs), one pencil per block.
+// scalings folded in.  Block (32 cells, n outputs) over kDftPencils pencils
+// in turn: M is staged in shared memory once per block, and the next
+// pencil's element is loaded into a register while the current one is
+// computed (pencils alternate between two shared buffers).
 // OUT 0: complex store.  OUT 1: FS stage epilogue on the real part.
+constexpr int kDftPencils = 4;
+
 template <typename R, typename TIn, int OUT>
 __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict__ out,
                       const R *__restrict__ M, int n, int ax, int Bp, int stage, R dt, R nu,
@@ -106,37 +111,51 @@ __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict_
     using C = typename V2<R>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *Ms = reinterpret_cast<C *>(smem_raw);
-    C *pen = Ms + n * n;
+    C *pen = Ms + n * n;  // [2][n][32]
     const int cl = threadIdx.x, p = threadIdx.y;
-    const int pid = blockIdx.x, c = blockIdx.y * 32 + cl;
+    const int c = blockIdx.y * 32 + cl;
+    const int pid0 = blockIdx.x * kDftPencils, pend = min(n * n, pid0 + kDftPencils);
     for (int t = threadIdx.y * 32 + threadIdx.x; t < n * n; t += 32 * n) Ms[t] = mk2<R>(M[2 * t], M[2 * t + 1]);
-    long long base, stride;
-    if (ax == 2) { base = (long long)pid * n * Bp; stride = Bp; }
-    else if (ax == 1) { const int i0 = pid / n, i2 = pid % n; base = ((long long)i0 * n * n + i2) * Bp; stride = (long long)n * Bp; }
-    else { base = (long long)pid * Bp; stride = (long long)n * n * Bp; }
-    const long long o = base + p * stride + c;
-    if constexpr (std::is_same<TIn, double2>::value) pen[p * 32 + cl] = ld2c<R>(in + o);
-    else pen[p * 32 + cl] = ld2<R>(in + o);
-    __syncthreads();
-    R sr = R(0), si = R(0);
+    auto offset = [&](int pid) -> long long {
+        long long base, stride;
+        if (ax == 2) { base = (long long)pid * n * Bp; stride = Bp; }
+        else if (ax == 1) { const int i0 = pid / n, i2 = pid % n; base = ((long long)i0 * n * n + i2) * Bp; stride = (long long)n * Bp; }
+        else { base = (long long)pid * Bp; stride = (long long)n * n * Bp; }
+        return base + p * stride + c;
+    };
+    auto load = [&](long long o) -> C {
+        if constexpr (std::is_same<TIn, double2>::value) return ld2c<R>(in + o);
+        else return ld2<R>(in + o);
+    };
+    R dtc = dt, nuc = nu;
+    if (OUT == 1 && cnu) { nuc = (R)cnu[c]; dtc = (R)cdt[c]; }
+    long long o = offset(pid0);
+    C v = load(o);
+    for (int pid = pid0, j = 0; pid < pend; ++pid, ++j) {
+        C *pb = pen + (j & 1) * n * 32;
+        pb[p * 32 + cl] = v;
+        const long long onext = pid + 1 < pend ? offset(pid + 1) : o;
+        if (pid + 1 < pend) v = load(onext);
+        __syncthreads();
+        R sr = R(0), si = R(0);
 #pragma unroll 4
-    for (int a = 0; a < n; ++a) {
-        const C m = Ms[p * n + a], x = pen[a * 32 + cl];
-        sr += m.x * x.x - m.y * x.y;
-        si += m.x * x.y + m.y * x.x;
-    }
-    if constexpr (OUT == 0) {
-        out[o] = mk2<R>(sr, si);
-    } else {
-        // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
-        R dtc = dt, nuc = nu;
-        if (cnu) { nuc = (R)cnu[c]; dtc = (R)cdt[c]; }
-        if (stage == 0) {
-            qn[o] = sr;
-            f1[o] = f[o] + dtc * sr * nuc;
-        } else {
-            f1[o] = f[o] + R(0.5) * dtc * qn[o] * nuc + R(0.5) * dtc * sr * nuc;
+        for (int a = 0; a < n; ++a) {
+            const C m = Ms[p * n + a], x = pb[a * 32 + cl];
+            sr += m.x * x.x - m.y * x.y;
+            si += m.x * x.y + m.y * x.x;
         }
+        if constexpr (OUT == 0) {
+            out[o] = mk2<R>(sr, si);
+        } else {
+            // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
+            if (stage == 0) {
+                qn[o] = sr;
+                f1[o] = f[o] + dtc * sr * nuc;
+            } else {
+                f1[o] = f[o] + R(0.5) * dtc * qn[o] * nuc + R(0.5) * dtc * sr * nuc;
+            }
+        }
+        o = onext;
     }
 }
 
@@ -144,8 +163,8 @@ template <typename R, typename TIn, int OUT>
 cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
                      double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{}) {
     using C = typename V2<R>::t;
-    const size_t smem = sizeof(C) * (size_t)(n * n + 32 * n);
-    dim3 grid(n * n, Bp / 32), block(32, n);
+    const size_t smem = sizeof(C) * (size_t)(n * n + 2 * 32 * n);
+    dim3 grid((n * n + kDftPencils - 1) / kDftPencils, Bp / 32), block(32, n);
     k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1, rates.nu,
                                                   rates.dt);
     return cudaGetLastError();
@@ -664,13 +683,13 @@ __global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__rest
         const double tp0 = (double)a[0][jj], tp2 = (double)a[1][jj], tp3 = (double)a[2][jj], tp4 = (double)a[3][jj];
         const double tp5 = (double)a[4][jj] + (double)a[5][jj] + (double)a[6][jj];
         const double *u = U + (long long)ustride * ((long long)(c0 + c) * nv3 + kt);
-        const double p0 = u[us.x] + u[us4] / 4. + dt * tp0 * kfac;
+        const double p0 = u[us.x] + u[us4] * 0.25 + dt * tp0 * kfac;
         const double p2 = u[us.y] + dt * tp2 * 12. * kfac;
         const double p3 = u[us.z] + dt * tp3 * 12. * kfac;
         const double p4 = u[us.w] + dt * tp4 * 12. * kfac;
-        const double p5 = u[us.x] / 4. + u[us4] * 19. / 240. + dt * tp5 * kfac;
+        const double p5 = u[us.x] * 0.25 + u[us4] * (19. / 240.) + dt * tp5 * kfac;
         double *d = dU + 5 * ((long long)c * nv3 + kt);
-        d[0] = 19 * p0 / 4. - 15 * p5;
+        d[0] = 19 * p0 * 0.25 - 15 * p5;
         d[4] = 60 * p5 - 15 * p0;
         d[1] = p2; d[2] = p3; d[3] = p4;
     }
@@ -720,8 +739,14 @@ __device__ __forceinline__ void phi_row(double dv, double lv, int nv, long long 
     g2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
 }
 
+// dv/12, dv/6, dv^2/4 and 19 dv^2/240 of the DG moment rows, computed once on the host
+struct MomRow {
+    double dv12, dv6, dv2q, c19;
+};
+inline MomRow mom_row(double dv) { return MomRow{dv / 12., dv / 6., dv * dv / 4., 19. * dv * dv / 240.}; }
+
 __global__ void k_mom_actual(const double *__restrict__ dU, const double *__restrict__ U, int nv, double dv,
-                             double lv, int c0, int nrc, double *__restrict__ part) {
+                             double lv, MomRow mr, int c0, int nrc, double *__restrict__ part) {
     __shared__ double red[5][256];
     const int cc = blockIdx.y, t = threadIdx.x;
     const long long nv3 = (long long)nv * nv * nv;
@@ -734,11 +759,10 @@ __global__ void k_mom_actual(const double *__restrict__ dU, const double *__rest
         double G[3], g2;
         phi_row(dv, lv, nv, kt, G, g2);
         m[0] += d0 + 0.25 * d4;
-        m[1] += G[0] * d0 + dv / 12. * d1 + 0.25 * G[0] * d4;
-        m[2] += G[1] * d0 + dv / 12. * d2 + 0.25 * G[1] * d4;
-        m[3] += G[2] * d0 + dv / 12. * d3 + 0.25 * G[2] * d4;
-        m[4] += (g2 + dv * dv / 4.) * d0 + dv / 6. * (G[0] * d1 + G[1] * d2 + G[2] * d3) +
-                (19. * dv * dv / 240. + g2 / 4.) * d4;
+        m[1] += G[0] * d0 + mr.dv12 * d1 + 0.25 * G[0] * d4;
+        m[2] += G[1] * d0 + mr.dv12 * d2 + 0.25 * G[1] * d4;
+        m[3] += G[2] * d0 + mr.dv12 * d3 + 0.25 * G[2] * d4;
+        m[4] += (g2 + mr.dv2q) * d0 + mr.dv6 * (G[0] * d1 + G[1] * d2 + G[2] * d3) + (mr.c19 + 0.25 * g2) * d4;
     }
     for (int q = 0; q < 5; ++q) red[q][t] = m[q];
     __syncthreads();
@@ -777,29 +801,42 @@ __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const
     }
 }
 
+// delta = Phi^T lambda added to the 5 coefficients a of record kt
+// (columns of Phi: a0, a1, a2, a3, a4)
+__device__ __forceinline__ void mom_correct(double a[5], const double *l, double dv, double lv, int nv, long long kt,
+                                            const MomRow &mr) {
+    double G[3], g2;
+    phi_row(dv, lv, nv, kt, G, g2);
+    a[0] += l[0] + G[0] * l[1] + G[1] * l[2] + G[2] * l[3] + (g2 + mr.dv2q) * l[4];
+    a[1] += mr.dv12 * l[1] + mr.dv6 * G[0] * l[4];
+    a[2] += mr.dv12 * l[2] + mr.dv6 * G[1] * l[4];
+    a[3] += mr.dv12 * l[3] + mr.dv6 * G[2] * l[4];
+    a[4] += 0.25 * l[0] + 0.25 * (G[0] * l[1] + G[1] * l[2] + G[2] * l[3]) + (mr.c19 + 0.25 * g2) * l[4];
+}
+
 __global__ void k_mom_apply(double *__restrict__ dU, const double *__restrict__ lam, int nv, double dv, double lv,
-                            long long nrec) {
+                            MomRow mr, long long nrec) {
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     const long long nv3 = (long long)nv * nv * nv;
-    const long long cc = r / nv3, kt = r % nv3;
-    const double *l = lam + 5 * cc;
-    double G[3], g2;
-    phi_row(dv, lv, nv, kt, G, g2);
     double *a = dU + 5 * r;
-    // delta = Phi^T lambda (columns of Phi: a0, a1, a2, a3, a4)
-    a[0] += l[0] + G[0] * l[1] + G[1] * l[2] + G[2] * l[3] + (g2 + dv * dv / 4.) * l[4];
-    a[1] += dv / 12. * l[1] + dv / 6. * G[0] * l[4];
-    a[2] += dv / 12. * l[2] + dv / 6. * G[1] * l[4];
-    a[3] += dv / 12. * l[3] + dv / 6. * G[2] * l[4];
-    a[4] += 0.25 * l[0] + 0.25 * (G[0] * l[1] + G[1] * l[2] + G[2] * l[3]) + (19. * dv * dv / 240. + g2 / 4.) * l[4];
+    double v[5] = {a[0], a[1], a[2], a[3], a[4]};
+    mom_correct(v, lam + 5 * (r / nv3), dv, lv, nv, r % nv3, mr);
+    for (int q = 0; q < 5; ++q) a[q] = v[q];
 }
 
-// dU into slots {0,3,4,5,6} (LP_ompi_1.cpp:522-532).
-__global__ void k_scatter(const double *__restrict__ dU, long long nrec, long long r0, double *__restrict__ U) {
+// dU into slots {0,3,4,5,6} (LP_ompi_1.cpp:522-532), with the mixed path's
+// moment correction Phi^T lambda applied on the way when lam is given.
+__global__ void k_scatter(const double *__restrict__ dU, long long nrec, long long r0, double *__restrict__ U,
+                          const double *__restrict__ lam, int nv, double dv, double lv, MomRow mr) {
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= nrec) return;
-    const double *d = dU + 5 * r;
+    const double *dd = dU + 5 * r;
+    double d[5] = {dd[0], dd[1], dd[2], dd[3], dd[4]};
+    if (lam) {
+        const long long nv3 = (long long)nv * nv * nv;
+        mom_correct(d, lam + 5 * (r / nv3), dv, lv, nv, r % nv3, mr);
+    }
     double *u = U + 7 * (r0 + r);
     u[0] = d[0]; u[6] = d[4]; u[3] = d[1]; u[4] = d[2]; u[5] = d[3];
 }
@@ -1011,6 +1048,27 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, int npar
     }
 }
 
+// FP64 <-> FP32 conversions by bit manipulation, so that the stage copies of
+// the mixed path do not occupy the narrow FP64 unit: FP64 -> FP32 truncates
+// toward zero (within one FP32 ulp) and flushes magnitudes below the FP32
+// normal range to signed zero; FP32 -> FP64 is exact for normal numbers and
+// zero (FP32 subnormals become signed zero).
+__device__ __forceinline__ float f64_to_f32_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned u = __float_as_uint(f), sign = u & 0x80000000u, e = (u >> 23) & 0xffu;
+    if (e == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
+    const unsigned long long ee = e == 255 ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double(
+        (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // ---------------------------------------------------------------- advection
 // Right-hand side H of record k (I1, I2, I3, I5 at A:213-405 combined as at
 // A:455-467; H[2] = 0) in arithmetic T from stage values of type S.  Constant
@@ -1020,11 +1078,17 @@ __device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restric
                                          const double *__restrict__ fields, long long k, T H[7]) {
     const int nv = ad.nv;
     const long long sv = (long long)nv * nv * nv;
-    const long long jm = k % sv, s = k / sv;
-    const int j3 = (int)(jm % nv), j2 = (int)((jm / nv) % nv), j1 = (int)(jm / ((long long)nv * nv));
-    const int i2 = (int)(s % ad.nx2), i1 = (int)(s / ad.nx2);
-    const T dv = (T)ad.dv, rdv = (T)ad.rdv;
-    const T G = (T)(-ad.lv + (j1 + 0.5) * ad.dv);
+    // record decomposition in 32-bit arithmetic (the launcher keeps size < 2^31)
+    const int k32 = (int)k, sv32 = (int)sv, nvv = nv * nv;
+    const int jm32 = k32 % sv32, s32 = k32 / sv32;
+    const long long jm = jm32, s = s32;
+    const int j3 = jm32 % nv, j2 = (jm32 / nv) % nv, j1 = jm32 / nvv;
+    const int i2 = s32 % ad.nx2, i1 = s32 / ad.nx2;
+    // FP32 evaluation takes its constants from the FP32 copies and converts
+    // the FP64 fields by bit manipulation, so no FP64 instruction is issued
+    constexpr bool F32 = std::is_same<T, float>::value;
+    const T dv = F32 ? (T)ad.f.dv : (T)ad.dv, rdv = F32 ? (T)ad.f.rdv : (T)ad.rdv;
+    const T G = F32 ? (T)(-ad.f.lv + ((float)j1 + 0.5f) * ad.f.dv) : (T)(-ad.lv + (j1 + 0.5) * ad.dv);
     const T i12 = T(1. / 12.), i720_19 = T(19. / 720.), i240_19 = T(19. / 240.), i5_12 = T(5. / 12.),
             i720_133 = T(133. / 720.), i6 = T(1. / 6.), h = T(0.5), q4 = T(0.25);
     T u[7];
@@ -1052,10 +1116,17 @@ __device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restric
     // v1 upwind neighbours by the sign of the cell-average E_x, no inflow (I5).
     const long long nc = (long long)ad.nx1 * ad.nx2;
     const double ie_d = fields[s];
-    const T ie = (T)ie_d, ixe = (T)fields[nc + s], ixxe = (T)fields[3 * nc + s];
+    T ie, ixe, ixxe;
+    if constexpr (F32) {
+        ie = f64_to_f32_bits(ie_d); ixe = f64_to_f32_bits(fields[nc + s]); ixxe = f64_to_f32_bits(fields[3 * nc + s]);
+    } else {
+        ie = ie_d; ixe = fields[nc + s]; ixxe = fields[3 * nc + s];
+    }
+    // ie > 0 from the bit pattern (a positive double is a positive integer)
+    const bool ie_pos = F32 ? (__double_as_longlong(ie_d) > 0) : (ie_d > 0);
     T R5[7], L5[7], ur5 = T(0), ul5 = T(0);
     bool hasr, hasl;
-    if (ie_d > 0) {
+    if (ie_pos) {
         hasr = j1 + 1 < nv;
         hasl = true;
         const long long kr5 = s * sv + ((long long)(j1 + 1) * nv * nv + j2 * nv + j3);
@@ -1095,7 +1166,7 @@ __device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restric
     }
     // l = 3 (v1 slope)
     {
-        T i2 = (((u[0] + u[6] * q4) * ie + u[1] * ixe) * (T)ad.scalev) * rdv;
+        T i2 = (((u[0] + u[6] * q4) * ie + u[1] * ixe) * (F32 ? (T)ad.f.scalev : (T)ad.scalev)) * rdv;
         T i3 = dv2 * (((R3[0] - L3[0]) * dv2 + (ur3 - ul3) * h * dv2 + (R3[3] - L3[3]) * dv * G) * i12 + (R3[6] - L3[6]) * dv2 * i720_19);
         T i5 = T(0);
         if (hasr && hasl) i5 = h * (dv2 * (R5[0] + h * ur5 + R5[6] * i5_12 + L5[0] + h * ul5 + L5[6] * i5_12) * ie + dv2 * (R5[1] + L5[1]) * ixe);
@@ -1123,7 +1194,7 @@ __device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restric
         else if (hasl) i5 = -dv2 * (((L5[0] + h * ul5) * i5_12 + L5[6] * i720_133) * ie + L5[1] * ixe * i5_12);
         tp[5] = -i2 - i3 + i5;
     }
-    const T inv = (T)ad.inv, c12 = T(12);
+    const T inv = F32 ? (T)ad.f.inv : (T)ad.inv, c12 = T(12);
     H[0] = (T(19) * tp[0] * q4 - T(15) * tp[5]) * inv;
     H[6] = (T(60) * tp[5] - T(15) * tp[0]) * inv;
     H[1] = tp[1] * c12 * inv;
@@ -1172,27 +1243,6 @@ __global__ void __launch_bounds__(128) k_flux(AdvectDev ad, const double *__rest
 }
 
 // ---------------------------------------------------------------- mixed-path advection
-// FP64 <-> FP32 conversions by bit manipulation, so that the stage copies of
-// the mixed path do not occupy the narrow FP64 unit: FP64 -> FP32 truncates
-// toward zero (within one FP32 ulp) and flushes magnitudes below the FP32
-// normal range to signed zero; FP32 -> FP64 is exact for normal numbers and
-// zero (FP32 subnormals become signed zero).
-__device__ __forceinline__ float f64_to_f32_bits(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
-}
-__device__ __forceinline__ double f32_to_f64_bits(float f) {
-    const unsigned u = __float_as_uint(f), sign = u & 0x80000000u, e = (u >> 23) & 0xffu;
-    if (e == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
-    const unsigned long long ee = e == 255 ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
-    return __longlong_as_double(
-        (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
-}
-
 // FP32 copy of the state and the FP64 charge moments of every group of 128
 // consecutive records (one warp per group, four records per lane):
 // part[3 * group] = (sum U0 + U6/4, sum U1, sum U2).
@@ -1689,19 +1739,23 @@ cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double
                               double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
                               const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
                               double *apart, const double *gm_inv, double scale, double kfac, double *lam,
-                              double *dU, cudaStream_t st, Rates rates) {
+                              double *dU, cudaStream_t st, Rates rates, bool apply) {
     k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, rates.nu, gmom, n3, Bp, nchunk,
                                                                tpart);
-    k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, c0, nrc, apart);
+    const MomRow mr = mom_row(dv);
+    k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, mr, c0, nrc, apart);
     k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, kfac, rates.dt, B, Bp, lam);
-    const long long nrec = (long long)B * nv * nv * nv;
-    k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, nrec);
+    if (apply) {
+        const long long nrec = (long long)B * nv * nv * nv;
+        k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, mr, nrec);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st) {
+cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st, const double *lam,
+                           int nv, double dv, double lv) {
     const long long nrec = (long long)B * nv3;
-    k_scatter<<<grid1(nrec, 256), 256, 0, st>>>(dU, nrec, (long long)c0 * nv3, U);
+    k_scatter<<<grid1(nrec, 256), 256, 0, st>>>(dU, nrec, (long long)c0 * nv3, U, lam, nv, dv, lv, mom_row(dv));
     return cudaGetLastError();
 }
 
@@ -1735,6 +1789,7 @@ cudaError_t launch_poisson(const PoissonDev &pd, const double *rt, int npart, do
 cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const float *Uin_f32,
                               const double *fields, int stage, double *Uout, float *Uout_f32, double *part,
                               cudaStream_t st) {
+    if (ad.size >= (1ll << 31)) return cudaErrorInvalidValue;  // 32-bit record indexing in flux_rhs
     if (Uin_f32)
         k_flux<float, float><<<grid1(ad.size, 128), 128, 0, st>>>(ad, U0, Us, Uin_f32, fields, stage, Uout, Uout_f32,
                                                                  part);
@@ -1752,6 +1807,7 @@ cudaError_t launch_state_f32_grp(const double *U, long long size, float *Uf, dou
 cudaError_t launch_flux_inc(const AdvectDev &ad, int stage, const float *Uin, const float *Uf0,
                             const double *fields, float *S, float *Uoutf, double *U, float *ipart,
                             cudaStream_t st) {
+    if (ad.size >= (1ll << 31)) return cudaErrorInvalidValue;  // 32-bit record indexing in flux_rhs
     const dim3 g = grid1(ad.size, 128);
     if (stage == 0) k_flux_inc<0><<<g, 128, 0, st>>>(ad, Uin, Uf0, fields, S, Uoutf, U, ipart);
     else if (stage == 1) k_flux_inc<1><<<g, 128, 0, st>>>(ad, Uin, Uf0, fields, S, Uoutf, U, ipart);

@@ -103,10 +103,13 @@ cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double
                               double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
                               const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
                               double *apart, const double *gm_inv, double scale, double kfac, double *lam,
-                              double *dU, cudaStream_t st, Rates rates = Rates{});
+                              double *dU, cudaStream_t st, Rates rates = Rates{}, bool apply = true);
 
-// U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU.
-cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st);
+// U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU; with lam (the mixed path's
+// moment multipliers of launch_moment_fix with apply = false) the correction
+// is added on the way.
+cudaError_t launch_scatter(const double *dU, int nv3, int c0, int B, double *U, cudaStream_t st,
+                           const double *lam = nullptr, int nv = 0, double dv = 0., double lv = 0.);
 
 // ---- advection and Poisson ----
 // Charge moments of every spatial cell summed in the reference's record order
@@ -142,6 +145,9 @@ struct AdvectDev {
     double rdv, inv;  // 1/dv and 1/dx/scalev
     float dt_f;       // dt in FP32 (mixed-path stage copies)
     double dt6;       // dt/6 (mixed-path final stage)
+    struct {
+        float lv, dv, rdv, scalev, inv;
+    } f;              // FP32 copies for the FP32 flux
 };
 // One SSP-RK3 stage: Uout = combination(U0, Us, H).  H is evaluated in FP64
 // from Us when Uin_f32 is nullptr, else in FP32 from the FP32 stage values

@@ -41,6 +41,7 @@ EXPORTS = [
     "lp_batch_step", "lp_batch_classes", "lp_batch_class_info", "lp_batch_autotune",
     "lp_field_energy", "lp_collision_vjp", "lp_advect_vjp", "lp_step_vjp", "lp_field_energy_gradient",
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
+    "lp_autotune",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -148,6 +149,8 @@ def lib():
         L.lp_step_vjp.argtypes = [_vp, _vp, _vp, _dp]
         L.lp_field_energy_gradient.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _vp, _dp]
         L.lp_diagnostics.argtypes = [_vp, _dp]
+        L.lp_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_int)]
         L.lp_diagnostics_append.argtypes = [_vp, ctypes.c_char_p, ctypes.c_char_p]
         L.lp_marginal_x1v1.argtypes = [_vp, _dp]
         L.lp_state_append.argtypes = [_vp, ctypes.c_char_p]
@@ -311,6 +314,13 @@ class Context:
         out = np.zeros(6)
         self._chk(self.L.lp_moments(self.h, _p(out)))
         return out
+
+    def autotune(self, reps=3, cache_path=None):
+        """Pick the fastest collision schedule; returns (cells per pass, warps per line block)."""
+        bp, lw = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.L.lp_autotune(self.h, int(reps), cache_path.encode() if cache_path else None,
+                                     ctypes.byref(bp), ctypes.byref(lw)))
+        return bp.value, lw.value
 
     def diagnostics(self):
         """{mass, p1, p2, p3, KiE, EleE, sqrt EleE, log sqrt EleE, KiE + EleE, entropy}"""

@@ -102,3 +102,23 @@ def test_batch_rejects_mixed_settings(gpu_lib):
     runs[0].fixes = lp.FIX_F2 | lp.FIX_F3  # collisions in passes need F1 fixed
     with pytest.raises(lp.LPError):
         lp.Batch(runs)
+
+
+def test_context_autotune(gpu_lib, tmp_path):
+    lp = gpu_lib
+    P = lp.Params(nx1=8, nx2=1, nv=8, n=16, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.2, k_wave=0.5,
+                  fixes=lp.FIX_DEFAULT, precision=lp.PREC_MIXED)
+    a, b = lp.Context(P), lp.Context(P)
+    a.set_init(1)
+    b.set_init(1)
+    U0 = a.get_state()
+    cache = str(tmp_path / "t.txt")
+    bp, lw = a.autotune(reps=2, cache_path=cache)
+    assert bp % 32 == 0 and lw in (2, 4)
+    assert np.array_equal(a.get_state(), U0)
+    assert b.autotune(reps=2, cache_path=cache) == (bp, lw)  # from the cache
+    a.step(2)
+    c = lp.Context(P)
+    c.set_init(1)
+    c.step(2)
+    assert rel(a.get_state(), c.get_state()) < 1e-6

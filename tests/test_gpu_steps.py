@@ -95,3 +95,23 @@ def test_mixed_advection(gpu_lib, nx1, nx2, nv):
     _, px_o, _, _ = O.poisson(U)
     _, px_g, _, _ = ctx.poisson()
     assert rel(px_g, px_o) < 1e-6
+
+
+@pytest.mark.parametrize("n,nv", [(12, 6), (32, 4)], ids=["n12-pair-kernel", "n32-line-kernel"])
+def test_mixed_vs_fp64_other_n(gpu_lib, n, nv):
+    """The mixed path off the line-tiled sizes (n = 12: the FP32 pair kernel)
+    and at the largest n (32: four k-tiles), against the FP64 GPU path."""
+    lp = gpu_lib
+    kw = dict(nx1=4, nx2=1, nv=nv, n=n, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.5, k_wave=0.5,
+              fixes=FIX_DEFAULT)
+    mix = lp.Context(lp.Params(**kw, precision=lp.PREC_MIXED))
+    ref = lp.Context(lp.Params(**kw, precision=lp.PREC_FP64))
+    mix.set_init(1)
+    ref.set_init(1)
+    m0 = mix.moments()
+    mix.collision_step()
+    ref.collision_step()
+    assert rel(mix.get_state(), ref.get_state()) < 1e-6
+    m1 = mix.moments()
+    assert abs(m1[0] - m0[0]) / abs(m0[0]) < 1e-12
+    assert abs(m1[4] - m0[4]) / abs(m0[4]) < 1e-12
