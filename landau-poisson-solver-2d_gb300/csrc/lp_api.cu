@@ -389,16 +389,28 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool d
     const lp::Tables &T = c->T;
     static const int fixed_slots[5] = {0, 3, 4, 5, 6}, ref_slots[5] = {0, 2, 3, 4, 5};
     const bool f1 = (T.prm.fixes & LP_FIX_F1) != 0;
+    const bool fix = c->mixed && f1;
+    // the FP64 target moments need only q0..q3: on the side stream, beside the projection
+    cudaStream_t tst = (fix && c->side) ? c->side : c->stream;
+    if (fix) {
+        if (tst != c->stream) {
+            LP_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+            LP_CUDA(cudaStreamWaitEvent(tst, c->ev_fork, 0));
+        }
+        LP_CUDA(lp::launch_moment_target(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
+                                         c->mtpart, tst, rates_at(c, c0)));
+        if (tst != c->stream) LP_CUDA(cudaEventRecord(c->ev_join, tst));
+    }
     LP_CUDA(lp::launch_project<R>(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const R *)c->tfac, T.n, T.nv, Bp,
                                   B, c0, c->U, f1 ? 7 : 6, f1 ? fixed_slots : ref_slots, T.prm.dt, T.scalev,
                                   T.scaleL, T.scale3, (C *)c->Qc, (C *)c->Y, (C *)c->Z, c->dU, c->stream,
                                   rates_at(c, c0)));
-    if (c->mixed && f1) {
+    if (fix) {
+        if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
-        LP_CUDA(lp::launch_moment_fix(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
-                                      c->mtpart, c->U, T.nv, T.dv, T.prm.lv, c0, B, c->nrc, c->mapart, c->gm_inv,
-                                      T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream, rates_at(c, c0),
-                                      !defer_fix));
+        LP_CUDA(lp::launch_moment_finish(c->mtpart, c->nchunk, c->U, T.nv, T.dv, T.prm.lv, c0, B, Bp, c->nrc,
+                                         c->mapart, c->gm_inv, T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream,
+                                         rates_at(c, c0), !defer_fix));
     }
     return LP_OK;
 }

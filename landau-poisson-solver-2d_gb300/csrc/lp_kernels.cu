@@ -298,7 +298,7 @@ __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_g
 // latency hidden by the other resident warps) and its weights (double
 // buffered: the next plane pair's weights are copied during the computation).  Per plane pair, with a = A(k'), b = B(k+h-k') and
 // weight w: U += (w a) (bx, by) and V += (w a) (by, bx) in packed FP32x2, so
-// Re = U.x - U.y, Im = V.x + V.y; each plane's partials enter a
+// Re = U.x - U.y, Im = V.x + V.y; each plane pair's partials enter a
 // Kahan-compensated FP32 accumulator, and the warps' results are summed in
 // FP64 in a fixed order.
 template <int N, int TILE, int LW>
@@ -375,8 +375,6 @@ __global__ void __launch_bounds__(32 * LW, 12 / LW) k_cq_lines(const float2 *__r
         }
         float4 w4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int kk = 0; kk < KT; ++kk) { U[kk] = 0ull; V[kk] = 0ull; }
-#pragma unroll
         for (int n = 0; n < N; ++n) {
 #pragma unroll
             for (int k = klo_of<N>(n, K0); k <= khi_of<N>(n, K0 + KT); ++k) {
@@ -388,7 +386,8 @@ __global__ void __launch_bounds__(32 * LW, 12 / LW) k_cq_lines(const float2 *__r
                 V[k - K0] = fma2(wa, Bs[k + h - n], V[k - K0]);
             }
         }
-        {
+        // each plane pair's packed partials enter the Kahan sums (folding two
+        // plane pairs per update measured no faster)
 #pragma unroll
         for (int kk = 0; kk < KT; ++kk) {
             const float2 u2 = up2(U[kk]), v2 = up2(V[kk]);
@@ -397,7 +396,7 @@ __global__ void __launch_bounds__(32 * LW, 12 / LW) k_cq_lines(const float2 *__r
             cr[kk] = (tr - sr[kk]) - yr; sr[kk] = tr;
             float yi = pm - ci[kk], ti = sim[kk] + yi;
             ci[kk] = (ti - sim[kk]) - yi; sim[kk] = ti;
-        }
+            U[kk] = 0ull; V[kk] = 0ull;
         }
         __syncwarp();  // every lane is done with this plane pair's lines and weights
         if (nxt < npp) stage_lines(nxt);
@@ -1735,13 +1734,17 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
     return cudaGetLastError();
 }
 
-cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
-                              double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
-                              const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
-                              double *apart, const double *gm_inv, double scale, double kfac, double *lam,
-                              double *dU, cudaStream_t st, Rates rates, bool apply) {
+cudaError_t launch_moment_target(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
+                                 double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
+                                 cudaStream_t st, Rates rates) {
     k_mom_target<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q0, q1, q2, q3, nu, rates.nu, gmom, n3, Bp, nchunk,
                                                                tpart);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *U, int nv, double dv, double lv,
+                                 int c0, int B, int Bp, int nrc, double *apart, const double *gm_inv, double scale,
+                                 double kfac, double *lam, double *dU, cudaStream_t st, Rates rates, bool apply) {
     const MomRow mr = mom_row(dv);
     k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, mr, c0, nrc, apart);
     k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, kfac, rates.dt, B, Bp, lam);

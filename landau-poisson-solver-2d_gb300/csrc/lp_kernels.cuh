@@ -98,12 +98,17 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
                            double *dU, cudaStream_t st, Rates rates = Rates{});
 
 // Mixed path: reconcile the 5 DG moments of each cell's increment with their
-// FP64 values from the mode array (minimal-norm 5x5 Lagrange correction).
-cudaError_t launch_moment_fix(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
-                              double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
-                              const double *U, int nv, double dv, double lv, int c0, int B, int nrc,
-                              double *apart, const double *gm_inv, double scale, double kfac, double *lam,
-                              double *dU, cudaStream_t st, Rates rates = Rates{}, bool apply = true);
+// FP64 values from the mode array (minimal-norm 5x5 Lagrange correction), in
+// two parts: the FP64 target moments from q0..q3 (independent of the DG
+// projection, so they can run beside it) and, once dU exists, its actual
+// moments, the multipliers and (apply) the correction of dU.
+cudaError_t launch_moment_target(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
+                                 double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
+                                 cudaStream_t st, Rates rates = Rates{});
+cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *U, int nv, double dv, double lv,
+                                 int c0, int B, int Bp, int nrc, double *apart, const double *gm_inv, double scale,
+                                 double kfac, double *lam, double *dU, cudaStream_t st, Rates rates = Rates{},
+                                 bool apply = true);
 
 // U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU; with lam (the mixed path's
 // moment multipliers of launch_moment_fix with apply = false) the correction
