@@ -30,16 +30,24 @@ FLAGS=(-O2 -fPIC -ffp-contract=off -ftrivial-auto-var-init=zero -w
 UNITS=(LP_ompi_1 collisionRoutines_1 conservationRoutines SetInit_1 advection_1
        PoissonFunctions PoissonVariables MomentCalculations EntropyCalculations
        MarginalCreation NegativityChecks PoissonPrint)
-pids=()
-for u in "${UNITS[@]}"; do
-  extra=(-fopenmp)
-  [ "$u" = LP_ompi_1 ] && extra+=(-Dmain=lp_reference_main_unused)
-  [ "$u" = advection_1 ] && extra=()
-  "$CXX" "${FLAGS[@]}" "${extra[@]}" -c "$SRC/$u.cpp" -o "$OUT/obj/$u.o" &
-  pids+=($!)
-done
-"$CXX" "${FLAGS[@]}" -fopenmp -c "$HERE/shim/shim_impl.cpp" -o "$OUT/obj/shim_impl.o" & pids+=($!)
-"$CXX" "${FLAGS[@]}" -fopenmp -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+=($!)
-for p in "${pids[@]}"; do wait "$p"; done
-"$CXX" -shared -fopenmp -o "$OUT/libref.so" "$OUT"/obj/*.o
-echo "build_ref: built $OUT/libref.so"
+# two libraries: the default build (libref.so) and the two-species variant
+# compiled with the reference's own FullandLinear switch (libref_lin.so)
+build() {
+  local obj="$1" lib="$2"; shift 2
+  mkdir -p "$obj"
+  local pids=()
+  for u in "${UNITS[@]}"; do
+    local extra=(-fopenmp)
+    [ "$u" = LP_ompi_1 ] && extra+=(-Dmain=lp_reference_main_unused)
+    [ "$u" = advection_1 ] && extra=()
+    "$CXX" "${FLAGS[@]}" "$@" "${extra[@]}" -c "$SRC/$u.cpp" -o "$obj/$u.o" &
+    pids+=($!)
+  done
+  "$CXX" "${FLAGS[@]}" "$@" -fopenmp -c "$HERE/shim/shim_impl.cpp" -o "$obj/shim_impl.o" & pids+=($!)
+  "$CXX" "${FLAGS[@]}" "$@" -fopenmp -c "$HERE/ref_harness.cpp" -o "$obj/ref_harness.o" & pids+=($!)
+  for p in "${pids[@]}"; do wait "$p"; done
+  "$CXX" -shared -fopenmp -o "$lib" "$obj"/*.o
+  echo "build_ref: built $lib"
+}
+build "$OUT/obj" "$OUT/libref.so"
+build "$OUT/obj_lin" "$OUT/libref_lin.so" -DFullandLinear

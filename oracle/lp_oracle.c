@@ -51,6 +51,7 @@ struct lpo_ctx {
     unsigned char *rzero; /* n3: |omega| == 0 */
     double *c1, *c2;      /* 5 x n3 */
     double cct[25];
+    double cct_lin[4];    /* inverse 2x2 Gram matrix of rows C1[0], C1[4] (two-species variant) */
     int *nodecell;        /* n: DG cell of spectral node */
     double *tt;           /* 3 x n x nv complex: T0, T1, T2 per (k, j) */
     pois_t ps;
@@ -163,6 +164,18 @@ static void cons_tables(lpo_ctx *c)
     double work[5];
     lp_dgetf2(5, 5, c->cct, 5, piv);
     lp_dgetri(5, c->cct, 5, piv, work);
+    /* CCt_linear (K:190-199): rows C1[0] and C1[4] (C2[0] = C2[4] = 0) */
+    double t = 0., t1 = 0., t2 = 0.;
+    for (int k = 0; k < n3; ++k) {
+        t += c->c1[0 * n3 + k] * c->c1[0 * n3 + k] + c->c2[0 * n3 + k] * c->c2[0 * n3 + k];
+        t1 += c->c1[0 * n3 + k] * c->c1[4 * n3 + k] + c->c2[0 * n3 + k] * c->c2[4 * n3 + k];
+        t2 += c->c1[4 * n3 + k] * c->c1[4 * n3 + k] + c->c2[4 * n3 + k] * c->c2[4 * n3 + k];
+    }
+    c->cct_lin[0] = t; c->cct_lin[1] = t1; c->cct_lin[2] = t1; c->cct_lin[3] = t2;
+    int piv2[2];
+    double work2[2];
+    lp_dgetf2(2, 2, c->cct_lin, 2, piv2);
+    lp_dgetri(2, c->cct_lin, 2, piv2, work2);
 }
 
 void lpo_cons(const lpo_ctx *c, double *c1, double *c2, double *cct)
@@ -287,6 +300,99 @@ void lpo_compute_q(const lpo_ctx *c, const double *f, double *qhat)
     }
     free(fin);
     free(F);
+}
+
+/* ------------------------------------------------- two-species (linear) term */
+/* gHat3_linear(eta_xi, eta_omega) (C:71-96): -sum_ij Shat_ij(omega) xi_i (xi_j - omega_j)
+ * in the reference's (i, j) order. */
+static inline double weight_lin_of(const lpo_ctx *c, int xi, int om)
+{
+    const int n = c->p.n;
+    const double z[3] = {c->eta[xi / (n * n)], c->eta[(xi / n) % n], c->eta[xi % n]};
+    const double kk[3] = {c->eta[om / (n * n)], c->eta[(om / n) % n], c->eta[om % n]};
+    const double *s = c->sh + 6 * (long)om;
+    const double S[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
+    double r = 0.;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r += S[i][j] * z[i] * (z[j] - kk[j]);
+    return -r;
+}
+
+double lpo_weight_lin(const lpo_ctx *c, int xi, int om) { return weight_lin_of(c, xi, om); }
+
+/* ComputeQ of the two-species variant (C:551-635): qhat = Q(f,f) plus the
+ * linear term sum cw scale3 Wlin(xi, w) F(xi + n/2 - w), qhat_lin = that term. */
+void lpo_compute_q_lin(const lpo_ctx *c, const double *f, double *qhat, double *qlin)
+{
+    const int n = c->p.n, h = n / 2;
+    const long n3 = c->n3;
+    double *fin = (double *)calloc(2 * n3, sizeof(double));
+    double *F = (double *)malloc(sizeof(double) * 2 * n3);
+    for (long i = 0; i < n3; ++i) fin[2 * i] = f[i];
+    lpo_fft3d(c, fin, F);
+    const double pre = c->h_eta * c->h_eta * c->h_eta, s3 = c->scale3;
+    const double *wt = c->wt;
+#pragma omp parallel for schedule(dynamic)
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k) {
+                int si = i < h ? 0 : i - h + 1, ei = i < h ? i + h + 1 : n;
+                int sj = j < h ? 0 : j - h + 1, ej = j < h ? j + h + 1 : n;
+                int sk = k < h ? 0 : k - h + 1, ek = k < h ? k + h + 1 : n;
+                int xi = k + n * (j + n * i);
+                double t0 = 0., t1 = 0., t01 = 0., t11 = 0.;
+                for (int l = si; l < ei; ++l)
+                    for (int m = sj; m < ej; ++m)
+                        for (int q = sk; q < ek; ++q) {
+                            int x = i + h - l, y = j + h - m, z = k + h - q;
+                            long o = q + n * (m + (long)n * l), u = z + n * (y + (long)n * x);
+                            double w = weight_of(c, xi, (int)o), wl = weight_lin_of(c, xi, (int)o);
+                            t0 += pre * wt[l] * wt[m] * wt[q] * (w * (F[2 * o] * F[2 * u] - F[2 * o + 1] * F[2 * u + 1]) + s3 * wl * F[2 * u]);
+                            t1 += pre * wt[l] * wt[m] * wt[q] * (w * (F[2 * o] * F[2 * u + 1] + F[2 * o + 1] * F[2 * u]) + s3 * wl * F[2 * u + 1]);
+                            t01 += pre * wt[l] * wt[m] * wt[q] * s3 * wl * F[2 * u];
+                            t11 += pre * wt[l] * wt[m] * wt[q] * s3 * wl * F[2 * u + 1];
+                        }
+                qhat[2 * (long)xi] = t0;
+                qhat[2 * (long)xi + 1] = t1;
+                qlin[2 * (long)xi] = t01;
+                qlin[2 * (long)xi + 1] = t11;
+            }
+    }
+    free(fin);
+    free(F);
+}
+
+/* conserveAllMoments of the two-species variant (K:63-98): qhat with the 5
+ * constraints, qhat_lin's real part with mass and energy (CCt_linear). */
+void lpo_conserve_lin(const lpo_ctx *c, double *q, double *ql)
+{
+    const int n3 = c->n3;
+    lpo_conserve(c, q);
+    double t0 = 0., t1 = 0.;
+    for (int k = 0; k < n3; ++k) {
+        t0 += ql[2 * (long)k] * c->c1[0 * n3 + k];
+        t1 += ql[2 * (long)k] * c->c1[4 * n3 + k];
+    }
+    const double l0 = c->cct_lin[0] * t0 + c->cct_lin[1] * t1, l1 = c->cct_lin[2] * t0 + c->cct_lin[3] * t1;
+    for (int k = 0; k < n3; ++k) ql[2 * (long)k] -= (c->c1[0 * n3 + k] * l0 + c->c1[4 * n3 + k] * l1);
+}
+
+void lpo_cct_lin(const lpo_ctx *c, double *out4) { memcpy(out4, c->cct_lin, sizeof(double) * 4); }
+
+/* A stage's conserved mode array: ComputeQ and conserveAllMoments, and in the
+ * two-species variant the conserved linear part added (C:656-698). */
+static void stage_q(const lpo_ctx *c, const double *f1, double *q)
+{
+    if (c->p.linear_ei) {
+        double *ql = (double *)malloc(sizeof(double) * 2 * c->n3);
+        lpo_compute_q_lin(c, f1, q, ql);
+        lpo_conserve_lin(c, q, ql);
+        for (long i = 0; i < 2 * (long)c->n3; ++i) q[i] += ql[i];
+        free(ql);
+    } else {
+        lpo_compute_q(c, f1, q);
+        lpo_conserve(c, q);
+    }
 }
 
 /* ------------------------------------------------------------ projection */
@@ -487,16 +593,13 @@ static void rk4_impl(const lpo_ctx *c, const double *f, const double *qhat, cons
     double *qc = (double *)malloc(sizeof(double) * 2 * n3);
     lpo_fs(c, qhat, out);
     for (long i = 0; i < n3; ++i) { Qn[i] = out[2 * i]; f1[i] = f[i] + dt * Qn[i] * nu; }
-    lpo_compute_q(c, f1, q1);
-    lpo_conserve(c, q1);
+    stage_q(c, f1, q1);
     lpo_fs(c, q1, out);
     for (long i = 0; i < n3; ++i) { Q1n[i] = out[2 * i]; f1[i] = f[i] + 0.5 * dt * Qn[i] * nu + 0.5 * dt * Q1n[i] * nu; }
-    lpo_compute_q(c, f1, q2);
-    lpo_conserve(c, q2);
+    stage_q(c, f1, q2);
     lpo_fs(c, q2, out);
     for (long i = 0; i < n3; ++i) { Q1n[i] = out[2 * i]; f1[i] = f[i] + 0.5 * dt * Qn[i] * nu + 0.5 * dt * Q1n[i] * nu; }
-    lpo_compute_q(c, f1, q3);
-    lpo_conserve(c, q3);
+    stage_q(c, f1, q3);
     for (long i = 0; i < n3; ++i) {
         qc[2 * i] = nu * (0.5 * qhat[2 * i] + (q1[2 * i] + q2[2 * i] + q3[2 * i]) / 6.);
         qc[2 * i + 1] = nu * (0.5 * qhat[2 * i + 1] + (q1[2 * i + 1] + q2[2 * i + 1] + q3[2 * i + 1]) / 6.);
@@ -546,6 +649,22 @@ void lpo_rk4(const lpo_ctx *c, const double *f, const double *qhat, const double
     rk4_impl(c, f, qhat, ucell, 0, 7, fixed_slots, du, direct);
 }
 
+/* RK4 of the two-species variant (C:637-737) for spatial cell `cell` of the
+ * state U: the conserved qhat and qhat_lin are added first; with LPO_FIX_F1
+ * the stride-7 slots, else the compiled reference's stride-6 reads. */
+void lpo_rk4_lin(const lpo_ctx *c, const double *f, const double *qhat, const double *qlin, const double *U,
+                 int cell, double *du, int direct)
+{
+    static const int fixed_slots[5] = {0, 3, 4, 5, 6};
+    static const int ref_slots[5] = {0, 2, 3, 4, 5};
+    const long n3 = c->n3;
+    double *q0 = (double *)malloc(sizeof(double) * 2 * n3);
+    for (long i = 0; i < 2 * n3; ++i) q0[i] = qhat[i] + qlin[i];
+    if (c->p.fixes & LPO_FIX_F1) rk4_impl(c, f, q0, U + 7 * (long)cell * c->nv3, 0, 7, fixed_slots, du, direct);
+    else rk4_impl(c, f, q0, U, (long)cell * c->nv3, 6, ref_slots, du, direct);
+    free(q0);
+}
+
 /* -------------------------------------------------------- DG <-> nodes */
 /* setInit_spectral: the DG polynomial of the cell containing each
  * spectral node, evaluated at the node.  Slot 2 is the compiled reference's
@@ -589,8 +708,7 @@ int lpo_collide(const lpo_ctx *c, double *U, int direct)
     static const int ref_slots[5] = {0, 2, 3, 4, 5};
     for (int s = 0; s < ncol; ++s) {
         lpo_nodes(c, U, s, f);
-        lpo_compute_q(c, f, q);
-        lpo_conserve(c, q);
+        stage_q(c, f, q);
         if (c->p.fixes & LPO_FIX_F1)
             rk4_impl(c, f, q, U + 7 * (long)s * nv3, 0, 7, fixed_slots, du + 5 * (long)s * nv3, direct);
         else

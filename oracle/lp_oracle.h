@@ -31,6 +31,7 @@ typedef struct {
     int nx1, nx2, nv, n;
     double lv, lx, nu, dt, a_amp, k_wave;
     unsigned fixes;
+    int linear_ei; /* 1: the two-species variant (FullandLinear) */
 } lpo_params;
 
 typedef struct lpo_ctx lpo_ctx;
@@ -66,6 +67,13 @@ void lpo_moments(const lpo_ctx *c, const double *U, const double *phix, const do
                  double *out6);
 void lpo_band(const lpo_ctx *c, int *dims, double *ab, int *ipiv);
 double lpo_entropy(const lpo_ctx *c, const double *U);
+/* two-species variant (FullandLinear) */
+double lpo_weight_lin(const lpo_ctx *c, int xi, int om);
+void lpo_compute_q_lin(const lpo_ctx *c, const double *f, double *qhat, double *qlin);
+void lpo_conserve_lin(const lpo_ctx *c, double *q, double *qlin);
+void lpo_cct_lin(const lpo_ctx *c, double *out4);
+void lpo_rk4_lin(const lpo_ctx *c, const double *f, const double *qhat, const double *qlin, const double *U,
+                 int cell, double *du, int direct);
 void lpo_marginal_x1v1(const lpo_ctx *c, const double *U, double *out);
 
 #ifdef __cplusplus

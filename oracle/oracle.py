@@ -15,6 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liblp_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
+REF_LIN_SO = os.path.join(HERE, "_ref", "libref_lin.so")  # the FullandLinear build
 
 FIX_F1, FIX_F2, FIX_F3, FIX_F11 = 1, 2, 4, 8
 FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3
@@ -54,7 +55,7 @@ class _Params(ctypes.Structure):
     _fields_ = [("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nv", ctypes.c_int),
                 ("n", ctypes.c_int), ("lv", ctypes.c_double), ("lx", ctypes.c_double),
                 ("nu", ctypes.c_double), ("dt", ctypes.c_double), ("a_amp", ctypes.c_double),
-                ("k_wave", ctypes.c_double), ("fixes", ctypes.c_uint)]
+                ("k_wave", ctypes.c_double), ("fixes", ctypes.c_uint), ("linear_ei", ctypes.c_int)]
 
 
 @dataclass
@@ -70,6 +71,7 @@ class Case:
     dt: float = 0.01
     a_amp: float = 0.01
     k_wave: float = 0.5
+    linear_ei: int = 0  # 1: the two-species variant (FullandLinear)
 
     @property
     def ncell(self):
@@ -110,6 +112,14 @@ def _oracle_lib():
         L.lpo_collide.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.lpo_step.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.lpo_band.argtypes = [ctypes.c_void_p, _ip, _dp, _ip]
+        L.lpo_weight_lin.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.lpo_weight_lin.restype = ctypes.c_double
+        for name in ["lpo_compute_q_lin", "lpo_conserve_lin", "lpo_cct_lin", "lpo_rk4_lin"]:
+            getattr(L, name).restype = None
+        L.lpo_compute_q_lin.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.lpo_conserve_lin.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.lpo_cct_lin.argtypes = [ctypes.c_void_p, _dp]
+        L.lpo_rk4_lin.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, ctypes.c_int]
         _olib = L
     return _olib
 
@@ -122,7 +132,7 @@ class Oracle:
         self.fixes = fixes
         self.L = _oracle_lib()
         p = _Params(case.nx1, case.nx2, case.nv, case.n, case.lv, case.lx, case.nu, case.dt,
-                    case.a_amp, case.k_wave, fixes)
+                    case.a_amp, case.k_wave, fixes, int(case.linear_ei))
         h = ctypes.c_void_p()
         if self.L.lpo_create(ctypes.byref(p), ctypes.byref(h)) != 0:
             raise ValueError(f"oracle rejected case {case}")
@@ -227,6 +237,36 @@ class Oracle:
                            _p(out))
         return out
 
+    # two-species variant (FullandLinear)
+    def weight_lin(self, xi, om):
+        return self.L.lpo_weight_lin(self.h, int(xi), int(om))
+
+    def compute_q_lin(self, f):
+        q = np.zeros(self.n3, np.complex128)
+        ql = np.zeros(self.n3, np.complex128)
+        self.L.lpo_compute_q_lin(self.h, _p(np.ascontiguousarray(f, dtype=np.float64)),
+                                 _p(q.view(np.float64)), _p(ql.view(np.float64)))
+        return q, ql
+
+    def conserve_lin(self, q, ql):
+        q = np.array(q, dtype=np.complex128).reshape(-1)
+        ql = np.array(ql, dtype=np.complex128).reshape(-1)
+        self.L.lpo_conserve_lin(self.h, _p(q.view(np.float64)), _p(ql.view(np.float64)))
+        return q, ql
+
+    def cct_lin(self):
+        out = np.zeros(4)
+        self.L.lpo_cct_lin(self.h, _p(out))
+        return out.reshape(2, 2)
+
+    def rk4_lin(self, f, qhat, qlin, U, cell, direct=False):
+        du = np.zeros(self.nv3 * 5)
+        self.L.lpo_rk4_lin(self.h, _p(np.ascontiguousarray(f, dtype=np.float64)),
+                           _p(np.ascontiguousarray(qhat, dtype=np.complex128).view(np.float64)),
+                           _p(np.ascontiguousarray(qlin, dtype=np.complex128).view(np.float64)),
+                           _p(np.ascontiguousarray(U, dtype=np.float64)), int(cell), _p(du), int(direct))
+        return du
+
     def entropy(self, U):
         return float(self.L.lpo_entropy(self.h, _p(np.ascontiguousarray(U, dtype=np.float64))))
 
@@ -245,34 +285,45 @@ class Oracle:
         return dims, ab.reshape(ndim, ldab), piv
 
 
-_rlib = None
+_rlibs = {}
 
 
-def reference_available() -> bool:
-    return os.path.exists(REF_SO)
+def reference_available(linear: bool = False) -> bool:
+    return os.path.exists(REF_LIN_SO if linear else REF_SO)
 
 
-def _ref_lib():
-    global _rlib
-    if _rlib is None:
-        L = ctypes.CDLL(REF_SO)
+def _ref_lib(linear: bool = False):
+    if linear not in _rlibs:
+        L = ctypes.CDLL(REF_LIN_SO if linear else REF_SO)
         L.ref_setup.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 6 + [ctypes.c_int]
         L.ref_setup.restype = ctypes.c_int
         L.ref_ghat3.argtypes = [ctypes.c_double] * 6
         L.ref_ghat3.restype = ctypes.c_double
-        for name in ["ref_compute_q", "ref_rk4", "ref_get_weights", "ref_collision_cells"]:
-            getattr(L, name).restype = ctypes.c_int
-        L.ref_intmodes.argtypes = [ctypes.c_int] * 6 + [_dp]
-        L.ref_rk4.argtypes = [_dp, ctypes.c_int, _dp, _dp, _dp]
+        L.ref_get_weights.restype = ctypes.c_int
         L.ref_get_weights.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
-        L.ref_collision_cells.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
+        L.ref_intmodes.argtypes = [ctypes.c_int] * 6 + [_dp]
+        if linear:
+            for name in ["ref_compute_q_lin", "ref_rk4_lin", "ref_get_weights_lin"]:
+                getattr(L, name).restype = ctypes.c_int
+            L.ref_compute_q_lin.argtypes = [_dp, _dp, _dp]
+            L.ref_conserve_lin.argtypes = [_dp, _dp]
+            L.ref_conserve_lin.restype = None
+            L.ref_get_cct_lin.argtypes = [_dp]
+            L.ref_get_cct_lin.restype = None
+            L.ref_get_weights_lin.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
+            L.ref_rk4_lin.argtypes = [_dp, ctypes.c_int, _dp, _dp, _dp, _dp]
+        else:
+            for name in ["ref_compute_q", "ref_rk4", "ref_collision_cells"]:
+                getattr(L, name).restype = ctypes.c_int
+            L.ref_rk4.argtypes = [_dp, ctypes.c_int, _dp, _dp, _dp]
+            L.ref_collision_cells.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
         L.ref_get_band.argtypes = [_ip, _dp, _ip]
         L.ref_entropy.argtypes = [_dp]
         L.ref_entropy.restype = ctypes.c_double
         L.ref_marginal_x1v1.argtypes = [_dp, _dp]
         L.ref_marginal_x1v1.restype = None
-        _rlib = L
-    return _rlib
+        _rlibs[linear] = L
+    return _rlibs[linear]
 
 
 class Reference:
@@ -281,7 +332,7 @@ class Reference:
     def __init__(self, case: Case, with_weights: bool = True):
         assert case.nx1 == case.nx2, "the reference runs only the square 2-D layout"
         self.case = case
-        self.L = _ref_lib()
+        self.L = _ref_lib(bool(case.linear_ei))
         r = self.L.ref_setup(case.nx1, case.nv, case.n, case.lv, case.lx, case.nu, case.dt,
                              case.a_amp, case.k_wave, int(with_weights))
         if r != 0:
@@ -380,6 +431,38 @@ class Reference:
         U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
         du = np.zeros((l1 - l0) * self.nv3 * 5)
         assert self.L.ref_collision_cells(_p(U), int(l0), int(l1), _p(du)) == 0
+        return du
+
+    # two-species variant (the FullandLinear build)
+    def compute_q_lin(self, f):
+        q = np.zeros(self.n3, np.complex128)
+        ql = np.zeros(self.n3, np.complex128)
+        assert self.L.ref_compute_q_lin(_p(np.ascontiguousarray(f, dtype=np.float64)),
+                                        _p(q.view(np.float64)), _p(ql.view(np.float64))) == 0
+        return q, ql
+
+    def conserve_lin(self, q, ql):
+        q = np.array(q, dtype=np.complex128).reshape(-1)
+        ql = np.array(ql, dtype=np.complex128).reshape(-1)
+        self.L.ref_conserve_lin(_p(q.view(np.float64)), _p(ql.view(np.float64)))
+        return q, ql
+
+    def cct_lin(self):
+        out = np.zeros(4)
+        self.L.ref_get_cct_lin(_p(out))
+        return out.reshape(2, 2)
+
+    def weights_lin(self, r0, r1):
+        out = np.zeros((r1 - r0) * self.n3)
+        assert self.L.ref_get_weights_lin(r0, r1, _p(out)) == 0
+        return out.reshape(r1 - r0, self.n3)
+
+    def rk4_lin(self, f, l, qhat, qlin, U):
+        du = np.zeros(self.nv3 * 5)
+        assert self.L.ref_rk4_lin(_p(np.ascontiguousarray(f, dtype=np.float64)), int(l),
+                                  _p(np.ascontiguousarray(qhat, dtype=np.complex128).view(np.float64)),
+                                  _p(np.ascontiguousarray(qlin, dtype=np.complex128).view(np.float64)),
+                                  _p(np.ascontiguousarray(U, dtype=np.float64)), _p(du)) == 0
         return du
 
     def entropy(self, U):

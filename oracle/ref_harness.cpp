@@ -6,6 +6,9 @@
 // (source/LP_ompi_1.cpp:20-103) at run time and performs the set-up sequence of
 // main() (source/LP_ompi_1.cpp:154-387), then exposes each hot-path routine.
 //
+// Built twice: as is (libref.so) and with -DFullandLinear (libref_lin.so, the
+// two-species variant with the linear electron-ion operator).
+//
 // Test infrastructure only; never linked into the shipped library.
 #include "LP_ompi.h"
 #include "EntropyCalculations.h"
@@ -16,6 +19,10 @@
 
 static double **g_f = nullptr;            // node values per spatial cell (main's f)
 static double **g_conv = nullptr;         // conv_weights (main's local)
+#ifdef FullandLinear
+static double **g_conv_lin = nullptr;     // conv_weights_linear (main's local)
+static fftw_complex *g_qhat_lin = nullptr;
+#endif
 static fftw_complex *g_qhat = nullptr;    // main's qHat
 static int g_have_weights = 0;
 static std::vector<double> g_U, g_POTC, g_phix, g_phiy;
@@ -32,6 +39,11 @@ static int g_prev_chunk = 0, g_prev_ft = 0, g_prev_M = 0;
 static void release_all() {
     free_rows(g_f, g_prev_chunk);
     free_rows(g_conv, g_prev_ft);
+#ifdef FullandLinear
+    free_rows(g_conv_lin, g_prev_ft);
+    fftw_free(g_qhat_lin); fftw_free(Q1_fft_linear); fftw_free(Q2_fft_linear); fftw_free(Q3_fft_linear);
+    g_qhat_lin = Q1_fft_linear = Q2_fft_linear = Q3_fft_linear = nullptr;
+#endif
     free_rows(C1, g_prev_M);
     free_rows(C2, g_prev_M);
     free(Utmp); Utmp = nullptr;
@@ -49,6 +61,19 @@ static void release_all() {
 
 // defined in MarginalCreation.cpp:35 without a declaration in its header
 double f_marg2D_x1v1(std::vector<double> &U_vals0, int i1, int j1, double x1, double v1);
+
+#ifdef FullandLinear
+// The two-species RK4 is defined with a double* state (collisionRoutines_1.cpp:637)
+// while its header and main call a vector<double>& version; the forwarder
+// below supplies that symbol so the library loads.
+void RK4(double *f, int l, fftw_complex *qHat, double **conv_weights, fftw_complex *qHat_linear,
+         double **conv_weights_linear, double *U, double *dU);
+void RK4(double *f, int l, fftw_complex *qHat, double **conv_weights, fftw_complex *qHat_linear,
+         double **conv_weights_linear, std::vector<double> &U_vals, double *dU) {
+    RK4(f, l, qHat, conv_weights, qHat_linear, conv_weights_linear, U_vals.data(), dU);
+}
+void generate_conv_weights_linear(double **conv_weights_linear);
+#endif
 
 extern "C" {
 
@@ -97,6 +122,10 @@ int ref_setup(int nx, int nv, int n_spec, double lv, double lx, double nu_, doub
     if (with_weights) {
         g_conv = (double **)malloc(size_ft * sizeof(double *));
         for (int i = 0; i < size_ft; ++i) g_conv[i] = (double *)malloc(size_ft * sizeof(double));
+#ifdef FullandLinear
+        g_conv_lin = (double **)malloc(size_ft * sizeof(double *));
+        for (int i = 0; i < size_ft; ++i) g_conv_lin[i] = (double *)malloc(size_ft * sizeof(double));
+#endif
         g_prev_ft = size_ft;
     } else {
         g_prev_ft = 0;
@@ -117,6 +146,12 @@ int ref_setup(int nx, int nv, int n_spec, double lv, double lx, double nu_, doub
     Q3_fft = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
     fftOut = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
     fftIn = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
+#ifdef FullandLinear
+    g_qhat_lin = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
+    Q1_fft_linear = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
+    Q2_fft_linear = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
+    Q3_fft_linear = (fftw_complex *)fftw_malloc(size_ft * sizeof(fftw_complex));
+#endif
 
     scale = 1.0 / sqrt(2.0 * M_PI);
     scale3 = pow(scale, 3.0);
@@ -131,6 +166,9 @@ int ref_setup(int nx, int nv, int n_spec, double lv, double lx, double nu_, doub
     trapezoidalRule(N, wtN);
     createCCtAndPivot();
     if (with_weights) generate_conv_weights(g_conv);
+#ifdef FullandLinear
+    if (with_weights) generate_conv_weights_linear(g_conv_lin);
+#endif
 
     // Poisson set-up.  coef_pois writes only the band entries of the static
     // poisab array, so clear the region transmat reads before re-assembling.
@@ -193,6 +231,7 @@ void ref_fs(const double *in, double *out) {
     memcpy(out, fftOut, sizeof(fftw_complex) * size_ft);
 }
 
+#ifndef FullandLinear
 int ref_compute_q(const double *f, double *qhat) {
     if (!g_have_weights) return 1;
     std::vector<double> fcopy(f, f + size_ft);
@@ -219,6 +258,47 @@ int ref_rk4(const double *f, int l, const double *qhat, const double *U, double 
     memcpy(dU_cell, Utmp_coll + (size_t)l_local * size_v * 5, sizeof(double) * 5 * size_v);
     return 0;
 }
+#else
+// Two-species variant (collisionRoutines_1.cpp:551-737, conservationRoutines.cpp:63-98).
+int ref_compute_q_lin(const double *f, double *qhat, double *qhat_lin) {
+    if (!g_have_weights) return 1;
+    std::vector<double> fcopy(f, f + size_ft);
+    ComputeQ(fcopy.data(), g_qhat, g_conv, g_qhat_lin, g_conv_lin);
+    memcpy(qhat, g_qhat, sizeof(fftw_complex) * size_ft);
+    memcpy(qhat_lin, g_qhat_lin, sizeof(fftw_complex) * size_ft);
+    return 0;
+}
+
+void ref_conserve_lin(double *qhat, double *qhat_lin) {
+    memcpy(g_qhat, qhat, sizeof(fftw_complex) * size_ft);
+    memcpy(g_qhat_lin, qhat_lin, sizeof(fftw_complex) * size_ft);
+    conserveAllMoments(g_qhat, g_qhat_lin);
+    memcpy(qhat, g_qhat, sizeof(fftw_complex) * size_ft);
+    memcpy(qhat_lin, g_qhat_lin, sizeof(fftw_complex) * size_ft);
+}
+
+void ref_get_cct_lin(double *cct_lin) { memcpy(cct_lin, CCt_linear, sizeof(double) * 4); }
+
+// Rows [r0, r1) of the linear weight table.
+int ref_get_weights_lin(int r0, int r1, double *out) {
+    if (!g_have_weights) return 1;
+    for (int r = r0; r < r1; ++r) memcpy(out + (size_t)(r - r0) * size_ft, g_conv_lin[r], sizeof(double) * size_ft);
+    return 0;
+}
+
+int ref_rk4_lin(const double *f, int l, const double *qhat, const double *qhat_lin, const double *U,
+                double *dU_cell) {
+    if (!g_have_weights) return 1;
+    std::vector<double> fcopy(f, f + size_ft);
+    memcpy(g_qhat, qhat, sizeof(fftw_complex) * size_ft);
+    memcpy(g_qhat_lin, qhat_lin, sizeof(fftw_complex) * size_ft);
+    memcpy(g_U.data(), U, sizeof(double) * 7 * (size_t)size);
+    RK4(fcopy.data(), l, g_qhat, g_conv, g_qhat_lin, g_conv_lin, g_U.data(), Utmp_coll);
+    int l_local = l % chunk_Nx;
+    memcpy(dU_cell, Utmp_coll + (size_t)l_local * size_v * 5, sizeof(double) * 5 * size_v);
+    return 0;
+}
+#endif
 
 void ref_intmodes(int k1, int k2, int k3, int j1, int j2, int j3, double *out10) {
     IntModes(k1, k2, k3, j1, j2, j3, out10);
@@ -275,6 +355,7 @@ void ref_rk3(double *U, double *potc, double *phix, double *phiy) {
 // The collision sequence of main for spatial cells [l0, l1) (source/
 // LP_ompi_1.cpp:502-516): setInit_spectral, then per cell ComputeQ,
 // conserveAllMoments, RK4.  dU_out receives (l1-l0)*size_v*5 doubles.
+#ifndef FullandLinear
 int ref_collision_cells(const double *U, int l0, int l1, double *dU_out) {
     if (!g_have_weights) return 1;
     memcpy(g_U.data(), U, sizeof(double) * 7 * (size_t)size);
@@ -289,6 +370,7 @@ int ref_collision_cells(const double *U, int l0, int l1, double *dU_out) {
     }
     return 0;
 }
+#endif
 
 // Moments of the reference: out = {mass, p1, p2, p3, KiE, EleE(phix, phiy)}.
 void ref_moments(const double *U, const double *phix, const double *phiy, double *out) {

@@ -9,6 +9,11 @@ FS, SetInit_LD, setInit_spectral, ComputeQ, conserveAllMoments, IntModes,
 RK4 (zero state, so the stride defect F1 does not enter), pois2d, the band
 factors, one RK3 step, the verbatim collision driver and the moments.
 
+The two-species fixture (ref_lin_n8) comes from the reference compiled with
+its FullandLinear switch: the linear weight rows, CCt_linear, ComputeQ with
+its linear part, the two conservations and RK4 (state with equal stride-6 and
+stride-7 slots, so the slot defect F1 reads the same values either way).
+
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -82,11 +87,46 @@ def make(name, case, rng):
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
 
 
+LIN_CASE = ("ref_lin_n8", Case(nx1=2, nx2=2, nv=4, n=8, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01,
+                                a_amp=0.2, k_wave=0.5, linear_ei=1))
+
+
+def make_lin(name, case, rng):
+    R = Reference(case, with_weights=True)
+    n3 = case.n ** 3
+    out = {"case": np.array([case.nx1, case.nx2, case.nv, case.n], np.int64),
+           "case_f": np.array([case.lv, case.lx, case.nu, case.dt, case.a_amp, case.k_wave])}
+    rows = np.sort(rng.choice(n3, 6, replace=False))
+    out.update(wl_rows=rows, wl_vals=np.stack([R.weights_lin(int(r), int(r) + 1)[0] for r in rows]))
+    out.update(cct_lin=R.cct_lin())
+    U = R.set_init_ld()
+    U2 = U.copy().reshape(-1, 7)
+    U2[:, 2] = U2[:, 3]
+    U2 = U2.ravel()
+    f = R.set_init_spectral(U2)[1].copy()
+    q, ql = R.compute_q_lin(f)
+    qc, qlc = R.conserve_lin(q, ql)
+    out.update(f_cell=f, qhat=q, qhat_lin=ql, qhat_cons=qc, qlin_cons=qlc)
+    # a state whose stride-6 reads of cell 1 see the stride-7 slots {0,3,4,5,6}
+    nv3 = case.nv ** 3
+    Us = np.zeros_like(U)
+    src = U.reshape(-1, 7)[nv3:2 * nv3]
+    for kt in range(nv3):
+        k = nv3 + kt
+        Us[6 * k + 0], Us[6 * k + 2], Us[6 * k + 3] = src[kt, 0], src[kt, 3], src[kt, 4]
+        Us[6 * k + 4], Us[6 * k + 5] = src[kt, 5], src[kt, 6]
+    out.update(rk4_state=Us, rk4_cell_state=src.ravel(), rk4_du=R.rk4_lin(f, 1, qc, qlc, Us))
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
+
+
 def main():
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
     rng = np.random.default_rng(SEED)
     for name, case in CASES:
         make(name, case, rng)
+    make_lin(*LIN_CASE, np.random.default_rng(SEED + 1))
 
 
 if __name__ == "__main__":
