@@ -74,6 +74,9 @@ typedef struct {
     double a_amp, k_wave; /* initial perturbation (1 + a cos(k x1)) */
     unsigned fixes;   /* LP_FIX_* bits */
     int precision;    /* LP_PREC_* */
+    int linear_ei;    /* 1: add the linear electron-ion operator of the reference's
+                         two-species variant (its FullandLinear switch,
+                         collisionRoutines_1.cpp:551-737, conservationRoutines.cpp:63-98) */
 } lp_params;
 
 typedef struct lp_ctx lp_ctx;
@@ -103,6 +106,13 @@ lp_status lp_set_init(lp_ctx *ctx, int kind, double u);
 lp_status lp_fft3d(lp_ctx *ctx, const double *in, double *out);
 lp_status lp_fs(lp_ctx *ctx, const double *in, double *out);
 lp_status lp_compute_q(lp_ctx *ctx, const double *f, double *qhat);
+/* Two-species contexts (linear_ei = 1): ComputeQ's qHat (Q(f,f) plus the
+ * linear term) and qHat_linear (the linear term alone), conserveAllMoments
+ * of both (5 and 2 constraints), and RK4 from the conserved pair. */
+lp_status lp_compute_q_lin(lp_ctx *ctx, const double *f, double *qhat, double *qhat_lin);
+lp_status lp_conserve_lin(lp_ctx *ctx, double *qhat, double *qhat_lin);
+lp_status lp_rk4_cell_lin(lp_ctx *ctx, const double *f, int cell, const double *qhat, const double *qhat_lin,
+                          double *dU);
 lp_status lp_conserve(lp_ctx *ctx, double *qhat);
 /* RK4 of spatial cell `cell` from node values f and conserved qhat, reading
  * that cell's records of the resident state; dU receives nv^3*5 doubles. */

@@ -34,6 +34,12 @@ struct lp_ctx {
     void *P = nullptr;                                       // R precision
     unsigned *PI = nullptr;
     float *LW = nullptr;            // line-tiled weight table (mixed path)
+    // two-species variant: linear weight table (R precision), window offsets,
+    // the linear term's workspace and CCt_linear embedded in a 5x5 matrix
+    void *WLin = nullptr;
+    long long *win_off = nullptr;
+    double2 *qlin = nullptr;
+    double *cct_lin5 = nullptr;
     cudaStream_t side = nullptr;    // second stream of the line-tiled contraction
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long *line_off = nullptr;
@@ -207,6 +213,18 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
                                  std::is_same<R, double>::value ? (double *)P : nullptr,
                                  std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
     }
+    if (T.prm.linear_ei) {
+        LP_TRY(upload(c, &c->win_off, T.win_off.data(), T.win_off.size()));
+        LP_TRY(upload(c, &c->cct_lin5, T.cct_lin5, 25));
+        const size_t nw = (size_t)T.win_off[T.n3];
+        R *W = nullptr;
+        LP_TRY(dalloc(c, &W, nw));
+        c->WLin = W;
+        LP_CUDA(lp::launch_lin_weights(c->eta, c->shat, c->cw, c->win_off, T.n, T.scale3,
+                                       std::is_same<R, double>::value ? (double *)W : nullptr,
+                                       std::is_same<R, float>::value ? (float *)W : nullptr, c->stream));
+        LP_TRY(dalloc(c, &c->qlin, (size_t)T.n3 * c->Bcap));
+    }
     return alloc_workspace<R>(c);
 }
 
@@ -361,6 +379,28 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
     return LP_OK;
 }
 
+// The conserved mode array of one stage from the transformed node values F:
+// ComputeQ's contraction and conserveAllMoments; in the two-species variant
+// the linear term is added before, conserved with its own two constraints,
+// and added again after (C:551-635, K:63-98, C:656-698).
+template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q) {
+    using C = typename V2<R>::t;
+    const lp::Tables &T = c->T;
+    LP_TRY(contract<R>(c, Bp, q));
+    if (c->WLin) {
+        const long long tot = (long long)T.n3 * Bp;
+        LP_CUDA(lp::launch_qlin<R>((const C *)c->F, (const R *)c->WLin, c->win_off, T.n, Bp, c->qlin, c->stream));
+        LP_CUDA(lp::launch_qadd(q, c->qlin, tot, c->stream));
+        LP_CUDA(lp::launch_conserve(q, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+        LP_CUDA(lp::launch_conserve(c->qlin, c->c1, c->c2, c->cct_lin5, T.n3, Bp, c->cpart, c->nchunk, c->lam,
+                                    c->stream));
+        LP_CUDA(lp::launch_qadd(q, c->qlin, tot, c->stream));
+        return LP_OK;
+    }
+    LP_CUDA(lp::launch_conserve(q, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    return LP_OK;
+}
+
 // RK4 stages 1-3 (C:831-865) from node values f and conserved q[0].
 lp::Rates rates_at(const lp_ctx *c, int c0) {
     lp::Rates r;
@@ -376,9 +416,7 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp) {
         LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
                                        (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0)));
         LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
-        LP_TRY(contract<R>(c, Bp, c->q[s + 1]));
-        LP_CUDA(lp::launch_conserve(c->q[s + 1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam,
-                                    c->stream));
+        LP_TRY(stage_q<R>(c, Bp, c->q[s + 1]));
     }
     return LP_OK;
 }
@@ -424,8 +462,7 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
-    LP_TRY(contract<R>(c, Bp, c->q[0]));
-    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_TRY(stage_q<R>(c, Bp, c->q[0]));
     LP_TRY(rk4_stages<R>(c, c0, Bp));
     LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
@@ -441,8 +478,7 @@ template <typename R> lp_status collide_batch_prefix(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
-    LP_TRY(contract<R>(c, Bp, c->q[0]));
-    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_TRY(stage_q<R>(c, Bp, c->q[0]));
     LP_TRY(rk4_stages<R>(c, c0, Bp));
     return LP_OK;
 }
@@ -516,12 +552,19 @@ template <typename R> lp_status do_fft3d(lp_ctx *c, const double *in, double *ou
     return get_cplx_column<R>(c, out, (const C *)c->F, T.n3);
 }
 
-template <typename R> lp_status do_compute_q(lp_ctx *c, const double *f, double *qhat) {
+// ComputeQ of one cell; in the two-species variant qhat is Q(f,f) plus the
+// linear term and qhat_lin (optional) the linear term alone.
+template <typename R> lp_status do_compute_q(lp_ctx *c, const double *f, double *qhat, double *qhat_lin = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     LP_TRY(put_real_column<R>(c, (R *)c->f, f, T.n3));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, 32, c->stream));
     LP_TRY(contract<R>(c, 32, c->q[0]));
+    if (c->WLin) {
+        LP_CUDA(lp::launch_qlin<R>((const C *)c->F, (const R *)c->WLin, c->win_off, T.n, 32, c->qlin, c->stream));
+        LP_CUDA(lp::launch_qadd(c->q[0], c->qlin, (long long)T.n3 * 32, c->stream));
+        if (qhat_lin) LP_TRY(get_cplx_column<double>(c, qhat_lin, c->qlin, T.n3));
+    }
     return get_cplx_column<double>(c, qhat, c->q[0], T.n3);
 }
 
@@ -685,6 +728,7 @@ lp_status adj_setup(lp_ctx *c) {
     if (A.ready) return LP_OK;
     const lp::Tables &T = c->T;
     if (c->mixed || !c->collide_on || !c->advect_on) return fail(c, LP_ERR_INVALID, "the adjoint needs an FP64 context");
+    if (c->WLin) return fail(c, LP_ERR_INVALID, "the adjoint covers the one-species operator");
     if ((T.prm.fixes & (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3)) != (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3))
         return fail(c, LP_ERR_INVALID, "the adjoint needs LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3");
     if (T.pois.ndim > 4096) return fail(c, LP_ERR_INVALID, "the adjoint needs a Poisson matrix of order <= 4096");
@@ -988,6 +1032,37 @@ lp_status lp_rk4_cell(lp_ctx *c, const double *f, int cell, const double *qhat, 
     if (!c || !f || !qhat || !dU || cell < 0 || cell >= c->T.ncell) return fail(c, LP_ERR_INVALID, "bad argument");
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
     return c->mixed ? do_rk4_cell<float>(c, f, cell, qhat, dU) : do_rk4_cell<double>(c, f, cell, qhat, dU);
+}
+
+lp_status lp_compute_q_lin(lp_ctx *c, const double *f, double *qhat, double *qhat_lin) {
+    if (!c || !f || !qhat || !qhat_lin) return LP_ERR_INVALID;
+    if (!c->WLin) return fail(c, LP_ERR_INVALID, "not a two-species context");
+    return c->mixed ? do_compute_q<float>(c, f, qhat, qhat_lin) : do_compute_q<double>(c, f, qhat, qhat_lin);
+}
+
+lp_status lp_conserve_lin(lp_ctx *c, double *qhat, double *qhat_lin) {
+    if (!c || !qhat || !qhat_lin) return LP_ERR_INVALID;
+    if (!c->WLin) return fail(c, LP_ERR_INVALID, "not a two-species context");
+    const lp::Tables &T = c->T;
+    LP_TRY(put_cplx_column<double>(c, c->q[0], qhat, T.n3));
+    LP_TRY(put_cplx_column<double>(c, c->qlin, qhat_lin, T.n3));
+    LP_CUDA(lp::launch_conserve(c->q[0], c->c1, c->c2, c->cct, T.n3, 32, c->cpart, c->nchunk, c->lam, c->stream));
+    LP_CUDA(lp::launch_conserve(c->qlin, c->c1, c->c2, c->cct_lin5, T.n3, 32, c->cpart, c->nchunk, c->lam,
+                                c->stream));
+    LP_TRY(get_cplx_column<double>(c, qhat, c->q[0], T.n3));
+    return get_cplx_column<double>(c, qhat_lin, c->qlin, T.n3);
+}
+
+lp_status lp_rk4_cell_lin(lp_ctx *c, const double *f, int cell, const double *qhat, const double *qhat_lin,
+                          double *dU) {
+    if (!c || !f || !qhat || !qhat_lin || !dU || cell < 0 || cell >= c->T.ncell)
+        return fail(c, LP_ERR_INVALID, "bad argument");
+    if (!c->WLin) return fail(c, LP_ERR_INVALID, "not a two-species context");
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    // the two-species RK4 starts from qHat + qHat_linear (C:644-648)
+    std::vector<double> q0(2 * (size_t)c->T.n3);
+    for (size_t i = 0; i < q0.size(); ++i) q0[i] = qhat[i] + qhat_lin[i];
+    return c->mixed ? do_rk4_cell<float>(c, f, cell, q0.data(), dU) : do_rk4_cell<double>(c, f, cell, q0.data(), dU);
 }
 
 lp_status lp_nodes(lp_ctx *c, double *f) {
@@ -1414,7 +1489,8 @@ lp_status lp_batch_create(const lp_params *ps, int count, lp_batch **out) {
     const unsigned fixes = ps[0].fixes;
     const int prec = ps[0].precision;
     for (int r = 0; r < count; ++r) {
-        if (ps[r].fixes != fixes || ps[r].precision != prec) return LP_ERR_INVALID;  // shared fixes and precision
+        if (ps[r].fixes != fixes || ps[r].precision != prec || ps[r].linear_ei != ps[0].linear_ei)
+            return LP_ERR_INVALID;  // shared fixes, precision and operator
         const int ncell = ps[r].nx1 * ps[r].nx2;
         const int ncollide = (fixes & LP_FIX_F3) ? ncell : std::min(ps[r].nx1, ncell);
         if (ncollide != ncell) return LP_ERR_INVALID;  // 2-D runs need LP_FIX_F3

@@ -72,6 +72,98 @@ __global__ void k_pairs(const double *__restrict__ eta, const double *__restrict
     }
 }
 
+// ---------------------------------------------------------------- two-species linear term
+// gHat3_linear(eta_xi, eta_omega) = -sum_ij Shat_ij(omega) xi_i (xi_j - omega_j)
+// (C:71-96) in the reference's (i, j) order, without FMA.
+__device__ double weight_lin_dev(const double *eta, const double *shat, int n, int i, int j, int k, int o) {
+    const int l = o / (n * n), m = (o / n) % n, q = o % n;
+    const double *s = shat + 6 * (long long)o;
+    const double S[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
+    const double z[3] = {eta[i], eta[j], eta[k]}, w[3] = {eta[l], eta[m], eta[q]};
+    double r = 0.;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) r = __dadd_rn(r, __dmul_rn(__dmul_rn(S[a][b], z[a]), __dsub_rn(z[b], w[b])));
+    return -r;
+}
+
+// Linear weight table: for every xi, all window entries L (row-major over the
+// window box) hold cw(omega) scale3 gHat3_linear(eta_xi, eta_omega), the
+// factor of F(xi + n/2 - omega) in ComputeQ's linear term (C:614-621).
+__global__ void k_lin_weights(const double *__restrict__ eta, const double *__restrict__ shat,
+                              const double *__restrict__ cw, const long long *__restrict__ win_off, int n,
+                              double scale3, double *__restrict__ W64, float *__restrict__ W32) {
+    const int xi = blockIdx.x, h = n / 2;
+    const int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
+    const int si = i < h ? 0 : i - h + 1, sj = j < h ? 0 : j - h + 1, sk = k < h ? 0 : k - h + 1;
+    const int nj = j < h ? j + h + 1 : 3 * h - 1 - j, nk = k < h ? k + h + 1 : 3 * h - 1 - k;
+    const long long off = win_off[xi], cnt = win_off[xi + 1] - off;
+    for (long long L = threadIdx.x; L < cnt; L += blockDim.x) {
+        const int l = si + (int)(L / (nj * nk)), m = sj + (int)((L / nk) % nj), q = sk + (int)(L % nk);
+        const int o = (l * n + m) * n + q;
+        const double w = __dmul_rn(__dmul_rn(cw[o], scale3), weight_lin_dev(eta, shat, n, i, j, k, o));
+        if (W64) W64[off + L] = w;
+        if (W32) W32[off + L] = (float)w;
+    }
+}
+
+// ql(xi) = sum over the window of Wl F(xi + n/2 - omega), one thread per (xi,
+// cell), cell-minor.  FP64: one sequential sum in the window's order with
+// _rn operations; FP32: each window line summed in FP32 and the lines added
+// to a Kahan-compensated FP32 sum.
+template <typename R>
+__global__ void k_qlin(const typename V2<R>::t *__restrict__ F, const R *__restrict__ Wl,
+                       const long long *__restrict__ win_off, int n, int Bp, double2 *__restrict__ ql) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int n3 = n * n * n, h = n / 2;
+    if (tid >= (long long)n3 * Bp) return;
+    const int c = (int)(tid % Bp), xi = (int)(tid / Bp);
+    const int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
+    const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
+    const int sj = j < h ? 0 : j - h + 1, nj = j < h ? j + h + 1 : 3 * h - 1 - j;
+    const int sk = k < h ? 0 : k - h + 1, nk = k < h ? k + h + 1 : 3 * h - 1 - k;
+    const R *w = Wl + win_off[xi];
+    if constexpr (std::is_same<R, double>::value) {
+        double sr = 0., sim = 0.;
+        for (int a = 0; a < ni; ++a)
+            for (int b = 0; b < nj; ++b) {
+                const int x = i + h - (si + a), y = j + h - (sj + b);
+                const double2 *Fl = F + ((long long)(x * n + y) * n) * Bp + c;
+                const double *wl = w + (a * nj + b) * nk;
+                for (int e = 0; e < nk; ++e) {
+                    const double2 f = Fl[(long long)(k + h - (sk + e)) * Bp];
+                    sr = __dadd_rn(sr, __dmul_rn(wl[e], f.x));
+                    sim = __dadd_rn(sim, __dmul_rn(wl[e], f.y));
+                }
+            }
+        ql[tid] = make_double2(sr, sim);
+    } else {
+        float sr = 0.f, sim = 0.f, cr = 0.f, ci = 0.f;
+        for (int a = 0; a < ni; ++a)
+            for (int b = 0; b < nj; ++b) {
+                const int x = i + h - (si + a), y = j + h - (sj + b);
+                const float2 *Fl = F + ((long long)(x * n + y) * n) * Bp + c;
+                const float *wl = w + (a * nj + b) * nk;
+                float pr = 0.f, pim = 0.f;
+                for (int e = 0; e < nk; ++e) {
+                    const float2 f = Fl[(long long)(k + h - (sk + e)) * Bp];
+                    pr = fmaf(wl[e], f.x, pr);
+                    pim = fmaf(wl[e], f.y, pim);
+                }
+                float yr = pr - cr, tr = sr + yr;
+                cr = (tr - sr) - yr; sr = tr;
+                float yi = pim - ci, ti = sim + yi;
+                ci = (ti - sim) - yi; sim = ti;
+            }
+        ql[tid] = make_double2((double)sr - (double)cr, (double)sim - (double)ci);
+    }
+}
+
+// q += ql (the two-species stage's mode array, C:656-698)
+__global__ void k_qadd(double2 *__restrict__ q, const double2 *__restrict__ ql, long long total) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < total) { const double2 a = q[t], b = ql[t]; q[t] = make_double2(a.x + b.x, a.y + b.y); }
+}
+
 // ---------------------------------------------------------------- nodes
 // setInit_spectral for a batch of cells, cell-minor output.
 template <typename R>
@@ -1554,6 +1646,28 @@ __global__ void k_moments(const double *__restrict__ U, long long size, long lon
 }  // namespace
 
 // =============================================================== launchers
+cudaError_t launch_lin_weights(const double *eta, const double *shat, const double *cw, const long long *win_off, int n,
+                               double scale3, double *W64, float *W32, cudaStream_t st) {
+    k_lin_weights<<<n * n * n, 256, 0, st>>>(eta, shat, cw, win_off, n, scale3, W64, W32);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_qlin(const typename V2<R>::t *F, const R *Wl, const long long *win_off, int n, int Bp, double2 *ql,
+                        cudaStream_t st) {
+    k_qlin<R><<<grid1((long long)n * n * n * Bp, 128), 128, 0, st>>>(F, Wl, win_off, n, Bp, ql);
+    return cudaGetLastError();
+}
+template cudaError_t launch_qlin<double>(const double2 *, const double *, const long long *, int, int, double2 *,
+                                         cudaStream_t);
+template cudaError_t launch_qlin<float>(const float2 *, const float *, const long long *, int, int, double2 *,
+                                        cudaStream_t);
+
+cudaError_t launch_qadd(double2 *q, const double2 *ql, long long total, cudaStream_t st) {
+    k_qadd<<<grid1(total, 256), 256, 0, st>>>(q, ql, total);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pairs(const double *eta, const double *shat, const double *ahat, const unsigned char *rzero,
                          const double *cw, const int *pair_off, int n, double *P64, float *P32, unsigned *PI,
                          cudaStream_t st) {

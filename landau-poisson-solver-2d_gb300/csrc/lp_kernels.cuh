@@ -65,6 +65,15 @@ template <typename R>
 cudaError_t launch_computeq(const typename V2<R>::t *F, const R *P, const unsigned *PI,
                             const int *pair_off, int n3, int Bp, double2 *q, cudaStream_t st);
 
+// Two-species variant: the linear weight table (per xi, every window entry),
+// its contraction ql(xi) = sum Wl F(xi + n/2 - omega), and q += ql.
+cudaError_t launch_lin_weights(const double *eta, const double *shat, const double *cw, const long long *win_off, int n,
+                               double scale3, double *W64, float *W32, cudaStream_t st);
+template <typename R>
+cudaError_t launch_qlin(const typename V2<R>::t *F, const R *Wl, const long long *win_off, int n, int Bp, double2 *ql,
+                        cudaStream_t st);
+cudaError_t launch_qadd(double2 *q, const double2 *ql, long long total, cudaStream_t st);
+
 // Line-tiled FP32 contraction (mixed path, n in {8, 16, 24, 32}): one warp
 // per (output line (i, j), k-tile, 32 cells); the symmetric plane pairs
 // {(l, m), (i+n/2-l, j+n/2-m)} of the window keep both F lines in registers

@@ -538,6 +538,31 @@ static lp_status build_collision_tables(const lp_params &p, Tables &t, std::stri
         int cnt = ni * nj * nk;
         t.pair_off[xi + 1] = t.pair_off[xi] + (cnt + 1) / 2;
     }
+    if (p.linear_ei) {
+        t.win_off.assign(t.n3 + 1, 0);
+        for (int xi = 0; xi < t.n3; ++xi) {
+            int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
+            long long cnt = (long long)(i < h ? i + h + 1 : 3 * h - 1 - i) * (j < h ? j + h + 1 : 3 * h - 1 - j) *
+                            (k < h ? k + h + 1 : 3 * h - 1 - k);
+            t.win_off[xi + 1] = t.win_off[xi] + cnt;
+        }
+        // CCt_linear (K:190-199): Gram matrix of rows C1[0], C1[4], inverted
+        double g[4] = {0, 0, 0, 0};
+        for (int k = 0; k < t.n3; ++k) {
+            g[0] += t.c1[0 * (size_t)t.n3 + k] * t.c1[0 * (size_t)t.n3 + k] + t.c2[0 * (size_t)t.n3 + k] * t.c2[0 * (size_t)t.n3 + k];
+            g[1] += t.c1[0 * (size_t)t.n3 + k] * t.c1[4 * (size_t)t.n3 + k] + t.c2[0 * (size_t)t.n3 + k] * t.c2[4 * (size_t)t.n3 + k];
+            g[3] += t.c1[4 * (size_t)t.n3 + k] * t.c1[4 * (size_t)t.n3 + k] + t.c2[4 * (size_t)t.n3 + k] * t.c2[4 * (size_t)t.n3 + k];
+        }
+        g[2] = g[1];
+        int piv2[2];
+        if (dgetf2(2, 2, g, 2, piv2) != 0 || dgetri(2, g, 2, piv2) != 0) {
+            err = "two-species Gram matrix is singular";
+            return LP_ERR_INVALID;
+        }
+        std::fill(t.cct_lin5, t.cct_lin5 + 25, 0.);
+        t.cct_lin5[0 * 5 + 0] = g[0]; t.cct_lin5[0 * 5 + 4] = g[1];
+        t.cct_lin5[4 * 5 + 0] = g[2]; t.cct_lin5[4 * 5 + 4] = g[3];
+    }
 
     return LP_OK;
 }

@@ -45,6 +45,11 @@ struct Tables {
     std::vector<double> mfwd;    // n x n complex, out index major
     std::vector<double> minv;    // n x n complex, out index major
     std::vector<int> pair_off;   // n3 + 1 prefix offsets of the pair table
+    // two-species variant: n3 + 1 prefix offsets of the window entries (the
+    // linear weight table) and CCt_linear's inverse embedded in rows/columns
+    // {0, 4} of a 5x5 matrix (zero elsewhere)
+    std::vector<long long> win_off;
+    double cct_lin5[25] = {0};
     // Moment reconciliation of the mixed path: the 5 DG moments (mass, three
     // momenta, kinetic energy) of a cell's collision increment equal
     // dt*kfac*Re sum_k gmom[m][k] Qc(k) exactly; gm_inv is the inverse of

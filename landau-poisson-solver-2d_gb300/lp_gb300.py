@@ -41,7 +41,7 @@ EXPORTS = [
     "lp_batch_step", "lp_batch_classes", "lp_batch_class_info", "lp_batch_autotune",
     "lp_field_energy", "lp_collision_vjp", "lp_advect_vjp", "lp_step_vjp", "lp_field_energy_gradient",
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
-    "lp_autotune",
+    "lp_autotune", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -56,7 +56,8 @@ class _Params(ctypes.Structure):
     _fields_ = [("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nv", ctypes.c_int),
                 ("n", ctypes.c_int), ("lv", ctypes.c_double), ("lx", ctypes.c_double),
                 ("nu", ctypes.c_double), ("dt", ctypes.c_double), ("a_amp", ctypes.c_double),
-                ("k_wave", ctypes.c_double), ("fixes", ctypes.c_uint), ("precision", ctypes.c_int)]
+                ("k_wave", ctypes.c_double), ("fixes", ctypes.c_uint), ("precision", ctypes.c_int),
+                ("linear_ei", ctypes.c_int)]
 
 
 @dataclass
@@ -73,6 +74,7 @@ class Params:
     k_wave: float = 0.5
     fixes: int = FIX_DEFAULT
     precision: int = PREC_FP64
+    linear_ei: int = 0
 
     @property
     def ncell(self):
@@ -84,7 +86,7 @@ class Params:
 
     def _c(self):
         return _Params(self.nx1, self.nx2, self.nv, self.n, self.lv, self.lx, self.nu, self.dt,
-                       self.a_amp, self.k_wave, self.fixes, self.precision)
+                       self.a_amp, self.k_wave, self.fixes, self.precision, self.linear_ei)
 
 
 _lib = None
@@ -149,6 +151,9 @@ def lib():
         L.lp_step_vjp.argtypes = [_vp, _vp, _vp, _dp]
         L.lp_field_energy_gradient.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp, _vp, _dp]
         L.lp_diagnostics.argtypes = [_vp, _dp]
+        L.lp_compute_q_lin.argtypes = [_vp, _dp, _dp, _dp]
+        L.lp_conserve_lin.argtypes = [_vp, _dp, _dp]
+        L.lp_rk4_cell_lin.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]
         L.lp_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int)]
         L.lp_diagnostics_append.argtypes = [_vp, ctypes.c_char_p, ctypes.c_char_p]
@@ -258,6 +263,28 @@ class Context:
         q = np.array(q, dtype=np.complex128).reshape(-1)
         self._chk(self.L.lp_conserve(self.h, _p(q.view(np.float64))))
         return q
+
+    def compute_q_lin(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        q = np.zeros(self.n3, np.complex128)
+        ql = np.zeros(self.n3, np.complex128)
+        self._chk(self.L.lp_compute_q_lin(self.h, _p(f), _p(q.view(np.float64)), _p(ql.view(np.float64))))
+        return q, ql
+
+    def conserve_lin(self, q, ql):
+        q = np.array(q, dtype=np.complex128).reshape(-1)
+        ql = np.array(ql, dtype=np.complex128).reshape(-1)
+        self._chk(self.L.lp_conserve_lin(self.h, _p(q.view(np.float64)), _p(ql.view(np.float64))))
+        return q, ql
+
+    def rk4_cell_lin(self, f, cell, qhat, qlin):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(qhat, dtype=np.complex128).reshape(-1)
+        ql = np.ascontiguousarray(qlin, dtype=np.complex128).reshape(-1)
+        du = np.zeros(self.nv3 * 5)
+        self._chk(self.L.lp_rk4_cell_lin(self.h, _p(f), int(cell), _p(q.view(np.float64)),
+                                         _p(ql.view(np.float64)), _p(du)))
+        return du
 
     def rk4_cell(self, f, cell, qhat):
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
