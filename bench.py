@@ -36,15 +36,41 @@ WORKLOAD = dict(nx1=64, nx2=1, nv=24, n=24, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.
 METRIC = "collision+conserve cell-steps/s"
 UNIT = "cell-steps/s"
 L2_FLUSH_BYTES = 512 << 20
-# DRAM bytes of one contraction of this workload (both k-tiles of k_cq_lines,
-# dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
+# DRAM bytes of one contraction of this workload in the line-tiled form
+# (both k-tiles of k_cq_lines, dram__bytes_read.sum + dram__bytes_write.sum
+# from one ncu capture of
 # `bench.py --steps 2 --warmup 1 --no-cpu-baseline --fp64-steps 0`)
 CONTRACT_TRAFFIC_BYTES = 105.24e6 + 100.49e6
-# kernels of one mixed collision step at n = 24: nodes 1, forward transform
-# 3 x 4, contraction 2 tiles x 4, conservation 3 x 4, inverse transform 3 x 3,
-# DG projection 4, moment reconciliation 3 (its correction rides on the
-# scatter), scatter 1
-LAUNCHES_PER_STEP = 1 + 12 + 8 + 12 + 9 + 4 + 3 + 1
+# the same for the kernels of the convolution form (filled from ncu; None
+# where not captured)
+FQ_TRAFFIC_BYTES = {}
+
+
+def launches_per_step(line_warps):
+    """Kernels of one mixed collision step at n = 24 (64 cells, one pass):
+    nodes 1, forward transform 3 x 4, contraction x 4 (5 kernels in the
+    convolution form, 2 k-tiles in the line-tiled form), conservation 3 x 4,
+    inverse transform 3 x 3, DG projection 4, moment reconciliation 2 (its
+    target is zero; the correction rides on the scatter), scatter 1."""
+    return 1 + 12 + 4 * (5 if line_warps == 0 else 2) + 12 + 9 + 4 + 2 + 1
+
+
+def fq_kernel_model(n, cells):
+    """Algorithmic DRAM bytes and FP32 flops per launch of the five kernels of
+    the convolution form (complex FP32 intermediates of 8 bytes, q in FP64):
+    each kernel reads its input arrays once and writes its outputs once."""
+    M, h = 3 * n // 2, n // 2
+    c8 = 8 * cells
+    t3, x, g, hh = 10 * n * n * M, 13 * n * M * M, n * M * M, n * n * M
+    # valid (i, l) pairs of the direct axis-1 sum: 0 <= i + h - l < n
+    pairs = sum(1 for i in range(n) for l in range(n) if 0 <= i + h - l < n)
+    return {
+        "k_fq_x1": (n ** 3 * c8 + 7 * n ** 3 * 4 + t3 * c8, None),
+        "k_fq_x2": (t3 * c8 + x * c8, None),
+        "k_fq_y": (x * c8 + g * c8, 7 * pairs * 8.0 * M * M * cells),
+        "k_fq_z1": (g * c8 + hh * c8, None),
+        "k_fq_z2": (hh * c8 + n ** 3 * 16 * cells, None),
+    }
 
 
 def _config(extra=None):
@@ -367,11 +393,17 @@ def main():
     e2e_value = ws * cells * max(2, args.steps // 2) / t_e2e
 
     # Dominant kernel: the weighted contraction of ComputeQ for the 64 cells,
-    # timed alone with CUDA events on the context's stream.
+    # timed alone with CUDA events on the context's stream; in the
+    # convolution form each of its five kernels is timed alone too.
     extra = {}
     with torch.cuda.stream(stream):
         flush.zero_()
         t_contract_ms = ctx.time_kernel(0, reps=max(5, args.steps))
+        fq_ms = {}
+        if schedule[1] == 0:
+            for i, name in enumerate(["k_fq_x1", "k_fq_x2", "k_fq_y", "k_fq_z1", "k_fq_z2"]):
+                flush.zero_()
+                fq_ms[name] = ctx.time_kernel(4 + i, reps=max(5, args.steps))
     n = WORKLOAD["n"]
     h = n // 2
     win = [i + h + 1 if i < h else 3 * h - 1 - i for i in range(n)]
@@ -411,8 +443,40 @@ def main():
             v, secs = cpu_baseline(1)
             cb = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                   "sample": f"1 spatial cell of the 64-cell step ({secs:.1f} s of CPU work)"}
-        achieved = contract_bytes / (t_contract_ms * 1e-3) / 1e9
-        contract_tflops = contract_flops / (t_contract_ms * 1e-3) / 1e12
+        if fq_ms:
+            model = fq_kernel_model(n, cells)
+            kern = []
+            for name, ms in fq_ms.items():
+                b, fl = model[name]
+                kern.append({"kernel": name, "ms_per_launch": ms, "algorithmic_bytes": b,
+                             "gbs": b / (ms * 1e-3) / 1e9,
+                             "tflops": (fl / (ms * 1e-3) / 1e12) if fl else None})
+            extra["contraction_kernels"] = kern
+            dom = max(kern, key=lambda k: k["ms_per_launch"])
+            hbm_frac = dom["gbs"] / peak
+            roof = {"bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s", "frac": hbm_frac,
+                    "traffic": FQ_TRAFFIC_BYTES.get(dom["kernel"]),
+                    "algorithmic_bytes": dom["algorithmic_bytes"], "peak_kind": peak_kind,
+                    "kernel": dom["kernel"] + " (the largest of the five kernels of the convolution form)",
+                    "ms_per_launch": dom["ms_per_launch"]}
+            comp = {"pipe": "fp32 FMA (packed f32x2, CUDA cores)", "kernel": dom["kernel"],
+                    "achieved_tflops": dom["tflops"], "peak_tflops": fp32_peak,
+                    "frac": (dom["tflops"] / fp32_peak) if (dom["tflops"] and fp32_peak) else None,
+                    "peak_kind": "measured (FMA-chain microbenchmark)", "fp64_peak_tflops": fp64_peak}
+        else:
+            achieved = contract_bytes / (t_contract_ms * 1e-3) / 1e9
+            contract_tflops = contract_flops / (t_contract_ms * 1e-3) / 1e12
+            roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": CONTRACT_TRAFFIC_BYTES if args.precision == "mixed" else None,
+                    "algorithmic_bytes": contract_bytes, "peak_kind": peak_kind,
+                    "kernel": "k_cq_lines (weighted contraction of ComputeQ, all tiles)",
+                    "ms_per_launch": t_contract_ms,
+                    "note": "the contraction is bound by the FP32 FMA pipe, see compute_roofline"}
+            comp = {"pipe": "fp32 FMA (packed f32x2, CUDA cores)",
+                    "achieved_tflops": contract_tflops, "peak_tflops": fp32_peak,
+                    "frac": contract_tflops / fp32_peak if fp32_peak else None,
+                    "peak_kind": "measured (FMA-chain microbenchmark)", "fp64_peak_tflops": fp64_peak}
+        extra["contraction_ms"] = t_contract_ms
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -421,20 +485,9 @@ def main():
                 "config": _config({"precision": args.precision}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                         "d2h_bytes_per_step": nbytes},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak,
-                             "traffic": CONTRACT_TRAFFIC_BYTES if args.precision == "mixed" else None,
-                             "algorithmic_bytes": contract_bytes, "peak_kind": peak_kind,
-                             "kernel": "k_cq_lines (weighted contraction of ComputeQ, all tiles)",
-                             "ms_per_launch": t_contract_ms,
-                             "note": "the contraction is bound by the FP32 FMA pipe, see compute_roofline"},
-                "compute_roofline": {"pipe": "fp32 FMA (packed f32x2, CUDA cores)",
-                                     "achieved_tflops": contract_tflops, "peak_tflops": fp32_peak,
-                                     "frac": contract_tflops / fp32_peak if fp32_peak else None,
-                                     "peak_kind": "measured (FMA-chain microbenchmark)",
-                                     "fp64_peak_tflops": fp64_peak},
+                "roofline": roof, "compute_roofline": comp,
                 "cpu_baseline": cb, "clocks": clk.summary(),
-                "gpu_launches": LAUNCHES_PER_STEP * args.steps}
+                "gpu_launches": launches_per_step(schedule[1]) * args.steps}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -147,22 +147,37 @@ lp_status lp_step(lp_ctx *ctx, int nsteps);
 lp_status lp_moments(lp_ctx *ctx, double *out6);
 
 /* ---- schedule autotuner (no reference counterpart) ----------------------- */
+/* A collision schedule is (cells per pass, contraction form).  The mixed
+ * path has two forms of ComputeQ's weighted sum for n in {8, 16, 24, 32}:
+ * line_warps 2 or 4 -- the line-tiled weighted sum with that many warps per
+ * block -- and line_warps 0 -- the convolution form (the weight split into
+ * seven omega factors, 3n/2-point DFTs along two axes and a direct sum along
+ * the third).  The FP64 path has one form (line_warps 2). */
+
 /* Times one collision step of the resident state (best of `reps` after a
  * warm-up, CUDA events, the state restored before each run) for every
  * candidate schedule -- cells per pass 64, 128, ... up to the workspace's
- * capacity, and 2 or 4 warps per block of the line-tiled contraction -- and
- * keeps the fastest; with cache_path, a schedule recorded there for the same
- * key (n, nv, lv, cells, precision, device) is reused and new ones appended.
- * The chosen schedule is returned in pass_cells and line_warps (optional).
- * Leaves the state as it was. */
+ * capacity, times the contraction forms above -- and keeps the fastest;
+ * with cache_path, a schedule recorded there for the same key (n, nv, lv,
+ * cells, precision, device) is reused and new ones appended.  The chosen
+ * schedule is returned in pass_cells and line_warps (optional).  Leaves the
+ * state as it was. */
 lp_status lp_autotune(lp_ctx *ctx, int reps, const char *cache_path, int *pass_cells, int *line_warps);
+
+/* Sets the schedule directly: pass_cells a multiple of 32 up to the
+ * workspace capacity (lp_autotune's largest candidate), line_warps one of
+ * the forms above.  LP_ERR_INVALID for a schedule the context cannot run. */
+lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
 
 /* ---- measurement helpers (no reference counterpart) --------------------- */
 /* Average device time in ms of one launch of a hot-path stage on the
  * context's stream, over `reps` launches after one warm-up, timed with CUDA
  * events: which = 0 the weighted contraction of ComputeQ for every collided
  * cell, 1 the forward transform, 2 the moment-conserving projection, 3 the
- * DG projection of the RK4 combination.  Needs the resident state. */
+ * DG projection of the RK4 combination; 4..8 the five kernels of the
+ * convolution form (axis-3 DFTs, axis-2 DFTs, axis-1 sums, inverse axis-2
+ * and axis-3 DFTs) for the first convolution chunk of cells, each alone,
+ * when that form is the schedule.  Needs the resident state. */
 lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
 /* Dense FMA throughput of the current device measured with dependent-chain
  * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */

@@ -57,7 +57,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     cu_flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                        "-I", INCLUDE, "-I", CSRC]
-    for name in ("lp_kernels.cu", "lp_api.cu", "lp_noalloc.cu", "lp_adjoint.cu"):
+    for name in ("lp_kernels.cu", "lp_api.cu", "lp_noalloc.cu", "lp_adjoint.cu", "lp_fftq.cu"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OUT, name.replace(".cu", ".o"))
         objs.append(obj)
@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs.append(obj)
     if force or _stale(obj, [src] + hdrs):
         jobs.append([CXX] + cxx_flags + ["-c", src, "-o", obj])
-    with ThreadPoolExecutor(max_workers=4) as ex:
+    with ThreadPoolExecutor(max_workers=6) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout, r.stderr)

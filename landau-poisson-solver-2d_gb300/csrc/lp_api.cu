@@ -34,6 +34,12 @@ struct lp_ctx {
     void *P = nullptr;                                       // R precision
     unsigned *PI = nullptr;
     float *LW = nullptr;            // line-tiled weight table (mixed path)
+    // convolution form of the mixed contraction: omega factors C[7][n^3],
+    // twiddles and the scratch of fq_bs cells
+    float *FQC = nullptr;
+    float2 *fscr = nullptr;
+    int fq_bs = 0;
+    lp::FftTw ftw{};
     // two-species variant: linear weight table (R precision), window offsets,
     // the linear term's workspace and CCt_linear embedded in a 5x5 matrix
     void *WLin = nullptr;
@@ -203,6 +209,20 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
         LP_TRY(dalloc(c, &c->LW, (size_t)nw));
         LP_CUDA(lp::launch_lines_table(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->line_off, T.n, c->LW,
                                        c->stream));
+        if (lp::fftq_supported(T.n)) {
+            std::vector<float> C;
+            lp::fftq_coefficients(T.shat.data(), T.ahat.data(), T.cw.data(), T.h_eta, T.n, C);
+            LP_TRY(upload(c, &c->FQC, C.data(), C.size()));
+            // chunk of cells of one convolution pass: 64, or more while the
+            // scratch stays within 512 MB
+            const size_t per_cell = lp::fftq_scratch_elems(T.n, 1) * sizeof(float2);
+            const int fit = (int)std::min<size_t>((size_t)c->Bcap, (512ull << 20) / per_cell) / 32 * 32;
+            c->fq_bs = std::min(c->Bcap, std::max(64, fit));
+            LP_TRY(dalloc(c, &c->fscr, lp::fftq_scratch_elems(T.n, c->fq_bs)));
+            c->ftw = lp::fftq_twiddles(T.n);
+            // the convolution form is the faster one from n = 16 up
+            if (T.n >= 16) c->line_warps = 0;
+        }
     } else {
         const size_t npair = (size_t)T.pair_off[T.n3];
         R *P = nullptr;
@@ -357,9 +377,17 @@ lp_status advect(lp_ctx *c) {
 }
 
 // The weighted contraction of ComputeQ on the transformed node values F.
+// Mixed path: line_warps 0 selects the convolution form, 2 or 4 the
+// line-tiled weighted sum with that many warps per line.
 template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
+    if (c->FQC && c->line_warps == 0) {
+        for (int c0 = 0; c0 < Bp; c0 += c->fq_bs)
+            LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, c0,
+                                            std::min(c->fq_bs, Bp - c0), c->fscr, c->fq_bs, q, c->stream));
+        return LP_OK;
+    }
     if (c->LW) {
         // the k-tiles run on two streams so that the short lines at the end
         // of one tile overlap the next tile
@@ -421,16 +449,24 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp) {
     return LP_OK;
 }
 
-// defer_fix: the mixed path's moment correction is left to the scatter
+// defer_fix: the mixed path's moment correction is left to the scatter.
+// The DG moments of the increment are linear functionals of the RK4
+// combination of q0..q3; every q_s leaves conserveAllMoments with zero mass,
+// momentum and energy integrals, and the DG projection keeps those integrals
+// (1, v and |v|^2 lie in the span of each cell's basis), so the FP64 target
+// of the one-species operator is zero and the correction only removes the
+// FP32 projection's moment error.  The two-species operator conserves only
+// mass and energy of its linear term: its target is summed from q0..q3.
 template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool defer_fix = false) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     static const int fixed_slots[5] = {0, 3, 4, 5, 6}, ref_slots[5] = {0, 2, 3, 4, 5};
     const bool f1 = (T.prm.fixes & LP_FIX_F1) != 0;
     const bool fix = c->mixed && f1;
+    const bool target = fix && c->WLin;
     // the FP64 target moments need only q0..q3: on the side stream, beside the projection
-    cudaStream_t tst = (fix && c->side) ? c->side : c->stream;
-    if (fix) {
+    cudaStream_t tst = (target && c->side) ? c->side : c->stream;
+    if (target) {
         if (tst != c->stream) {
             LP_CUDA(cudaEventRecord(c->ev_fork, c->stream));
             LP_CUDA(cudaStreamWaitEvent(tst, c->ev_fork, 0));
@@ -446,9 +482,9 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool d
     if (fix) {
         if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
-        LP_CUDA(lp::launch_moment_finish(c->mtpart, c->nchunk, c->U, T.nv, T.dv, T.prm.lv, c0, B, Bp, c->nrc,
-                                         c->mapart, c->gm_inv, T.prm.dt * kfac, kfac, c->mlam, c->dU, c->stream,
-                                         rates_at(c, c0), !defer_fix));
+        LP_CUDA(lp::launch_moment_finish(target ? c->mtpart : nullptr, c->nchunk, c->U, T.nv, T.dv, T.prm.lv, c0, B,
+                                         Bp, c->nrc, c->mapart, c->gm_inv, T.prm.dt * kfac, kfac, c->mlam, c->dU,
+                                         c->stream, rates_at(c, c0), !defer_fix));
     }
     return LP_OK;
 }
@@ -1159,13 +1195,16 @@ lp_status lp_step(lp_ctx *c, int nsteps) {
 }
 
 lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
-    if (!c || !ms || reps < 1 || which < 0 || which > 3) return fail(c, LP_ERR_INVALID, "bad argument");
+    if (!c || !ms || reps < 1 || which < 0 || which > 8) return fail(c, LP_ERR_INVALID, "bad argument");
+    if (which >= 4 && !(c->FQC && c->line_warps == 0))
+        return fail(c, LP_ERR_INVALID, "the convolution form is not this context's schedule");
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
     const lp::Tables &T = c->T;
     const int B = std::min(c->Bcap, T.ncollide), Bp = round32(B);
     // inputs of every stage: node values, transform, one conserved mode array
     lp_status s = c->mixed ? collide_batch_prefix<float>(c, 0, B) : collide_batch_prefix<double>(c, 0, B);
     if (s != LP_OK) return s;
+    if (which >= 4) LP_TRY(contract<float>(c, Bp, c->q[1]));  // fills the convolution scratch
     auto run = [&]() -> lp_status {
         switch (which) {
         case 0: return c->mixed ? contract<float>(c, Bp, c->q[1]) : contract<double>(c, Bp, c->q[1]);
@@ -1176,7 +1215,11 @@ lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
         case 2:
             LP_CUDA(lp::launch_conserve(c->q[1], c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
             return LP_OK;
-        default: return c->mixed ? project<float>(c, 0, B, Bp) : project<double>(c, 0, B, Bp);
+        case 3: return c->mixed ? project<float>(c, 0, B, Bp) : project<double>(c, 0, B, Bp);
+        default:
+            LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, 0, std::min(c->fq_bs, Bp),
+                                            c->fscr, c->fq_bs, c->q[1], c->stream, which - 4));
+            return LP_OK;
         }
     };
     LP_TRY(run());
@@ -1409,7 +1452,7 @@ bool tune_lookup(const std::vector<std::string> &lines, const std::string &key, 
         int bp = 0, lw = 0;
         double t = 0.;
         if (sscanf(l.c_str(), "%511s %d %d %lf", kbuf, &bp, &lw, &t) == 4 && key == kbuf && bp >= 32 &&
-            bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4 || !e->LW)) {
+            bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4 || (lw == 0 && e->FQC) || !e->LW)) {
             e->Bpass = bp;
             e->line_warps = e->LW ? lw : 2;
             *ms = t;
@@ -1460,6 +1503,7 @@ lp_status tune_engine(lp_ctx *e, int ncell, cudaStream_t st, int reps, double *b
     passes.push_back(e->Bcap);
     std::vector<int> warps = {2};
     if (e->LW) warps.push_back(4);
+    if (e->FQC) warps.push_back(0);
     LP_CUDA(cudaMemcpyAsync(e->U1, e->U, bytes, cudaMemcpyDeviceToDevice, st));
     double best = 1e300;
     int bbp = e->Bcap, blw = 2;
@@ -1904,6 +1948,20 @@ lp_status lp_autotune(lp_ctx *c, int reps, const char *cache_path, int *pass_cel
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }  // recapture with the new schedule
     if (pass_cells) *pass_cells = c->Bpass;
     if (line_warps) *line_warps = c->line_warps;
+    return LP_OK;
+}
+
+lp_status lp_set_schedule(lp_ctx *c, int pass_cells, int line_warps) {
+    if (!c) return LP_ERR_INVALID;
+    if (!c->collide_on) return fail(c, LP_ERR_INVALID, "no collision tables in this context");
+    if (pass_cells < 32 || pass_cells % 32 || pass_cells > c->Bcap)
+        return fail(c, LP_ERR_INVALID, "pass_cells must be a multiple of 32 up to the workspace capacity");
+    const bool ok = (line_warps == 2) || (line_warps == 4 && c->LW) || (line_warps == 0 && c->FQC);
+    if (!ok) return fail(c, LP_ERR_INVALID, "contraction form not available in this context");
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    c->Bpass = pass_cells;
+    c->line_warps = line_warps;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
     return LP_OK;
 }
 

@@ -1,0 +1,443 @@
+// ComputeQ of the mixed path as a sum of seven windowed convolutions.
+//
+// The reference's weight (source/collisionRoutines_1.cpp:30-69, used at
+// C:739-822) is gHat3(xi, omega) = ahat(omega) - d^T Shat(omega) d with
+// d = eta(xi) - eta(omega).  On the uniform eta grid d = (u - h) h_eta where
+// u = xi + h - omega is the index of the second factor F(u), so every term
+// of the windowed sum
+//
+//     Qhat(xi) = sum_omega cw(omega) gHat3(xi, omega) F(omega) F(u)
+//
+// splits into a function of omega times a function of u:
+//
+//     Qhat = sum_p (a_p * b_p)(xi + h),   p = 0..6,
+//     a_0 = cw ahat F,                    b_0 = F,
+//     a_ij = -c_ij h_eta^2 cw Shat_ij F,  b_ij = (u_i - h)(u_j - h) F,
+//
+// with c_ii = 1, c_ij = 2 (i < j) and * the linear convolution on the n^3
+// grid.  The output window xi + h in [h, n + h) of a linear convolution of
+// two length-n sequences is free of wrap-around on a cyclic grid of
+// M = 3n/2 points, so along axes 2 and 3 the convolutions are products of
+// M-point DFTs of the zero-padded arrays, and along axis 1 they are summed
+// directly (the direct sum along one axis costs less than a third of the
+// forward and inverse transforms it replaces):
+//
+//   X1  axis-3 DFT of the 7 a-arrays and of F (u3-h)^e, e = 0, 1, 2;
+//   X2  axis-2 DFT of the 7 a-arrays and of the 6 (e2, e3) b-combinations;
+//   Y   per (k2, k3): sum_p sum_l a_p(l) (u1-h)^e1 b_p(u1), u1 = i + h - l;
+//   Z1  inverse axis-2 DFT, only the n outputs xi2 + h;
+//   Z2  inverse axis-3 DFT, only the n outputs xi3 + h, written as FP64.
+//
+// The shift by h of the output window is the factor exp(2 pi i k h / M) =
+// exp(2 pi i k / 3) on the a-side spectra.  The M-point DFTs factor as
+// M = 6 S (S = n/4): S six-point DFTs of the 4 non-zero inputs, twiddles,
+// six S-point DFTs; the inverse is the conjugate transpose with only 4 of
+// the 6 outputs of its last stage kept.  A thread transforms one pencil of
+// one cell; the 32 lanes of a warp are 32 cells, so every load and store is
+// coalesced on the cell-minor arrays.  Arithmetic is FP32.
+#include "lp_kernels.cuh"
+#include "lp_f32x2.cuh"
+
+#include <cmath>
+
+namespace lp {
+namespace {
+
+constexpr float kC3 = 0.866025403784438646763723170752936183f;  // sqrt(3)/2
+constexpr float kR2 = 0.707106781186547524400844362104849039f;  // 1/sqrt(2)
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// -i z (forward) or +i z (inverse)
+template <bool INV> __device__ __forceinline__ float2 rot(float2 z) {
+    return INV ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x);
+}
+
+// Three-point DFT, sign of the exponent negative (forward) or positive.
+template <bool INV> __device__ __forceinline__ void dft3(float2 a, float2 b, float2 c, float2 &X0, float2 &X1,
+                                                         float2 &X2) {
+    const float2 s = cadd(b, c), d = csub(b, c);
+    X0 = cadd(a, s);
+    const float2 t = make_float2(a.x - 0.5f * s.x, a.y - 0.5f * s.y);
+    const float2 e = cscale(rot<INV>(d), kC3);
+    X1 = cadd(t, e);
+    X2 = csub(t, e);
+}
+// the same with c = 0
+template <bool INV> __device__ __forceinline__ void dft3_2(float2 a, float2 b, float2 &X0, float2 &X1, float2 &X2) {
+    X0 = cadd(a, b);
+    const float2 t = make_float2(a.x - 0.5f * b.x, a.y - 0.5f * b.y);
+    const float2 e = cscale(rot<INV>(b), kC3);
+    X1 = cadd(t, e);
+    X2 = csub(t, e);
+}
+
+// Six-point DFT as two three-point DFTs (even / odd inputs).  NIN = 4: the
+// inputs x4, x5 are zero.  NOUT = 4: only X0..X3 are formed.
+template <bool INV, int NIN, int NOUT> __device__ __forceinline__ void dft6(const float2 (&x)[6], float2 (&X)[6]) {
+    float2 E0, E1, E2, O0, O1, O2;
+    if (NIN == 4) {
+        dft3_2<INV>(x[0], x[2], E0, E1, E2);
+        dft3_2<INV>(x[1], x[3], O0, O1, O2);
+    } else {
+        dft3<INV>(x[0], x[2], x[4], E0, E1, E2);
+        dft3<INV>(x[1], x[3], x[5], O0, O1, O2);
+    }
+    const float2 w1 = make_float2(0.5f, INV ? kC3 : -kC3), w2 = make_float2(-0.5f, INV ? kC3 : -kC3);
+    const float2 p1 = cmul(O1, w1), p2 = cmul(O2, w2);
+    X[0] = cadd(E0, O0);
+    X[1] = cadd(E1, p1);
+    X[2] = cadd(E2, p2);
+    X[3] = csub(E0, O0);
+    if (NOUT == 6) {
+        X[4] = csub(E1, p1);
+        X[5] = csub(E2, p2);
+    }
+}
+
+template <bool INV> __device__ __forceinline__ void dft4(float2 a, float2 b, float2 c, float2 d, float2 &X0,
+                                                         float2 &X1, float2 &X2, float2 &X3) {
+    const float2 s0 = cadd(a, c), d0 = csub(a, c), s1 = cadd(b, d), e = rot<INV>(csub(b, d));
+    X0 = cadd(s0, s1);
+    X2 = csub(s0, s1);
+    X1 = cadd(d0, e);
+    X3 = csub(d0, e);
+}
+
+// In-place S-point DFT, S in {2, 4, 6, 8}.
+template <int S, bool INV> __device__ __forceinline__ void dftS(float2 (&x)[S]) {
+    if constexpr (S == 2) {
+        const float2 a = x[0], b = x[1];
+        x[0] = cadd(a, b);
+        x[1] = csub(a, b);
+    } else if constexpr (S == 4) {
+        float2 X0, X1, X2, X3;
+        dft4<INV>(x[0], x[1], x[2], x[3], X0, X1, X2, X3);
+        x[0] = X0; x[1] = X1; x[2] = X2; x[3] = X3;
+    } else if constexpr (S == 6) {
+        float2 X[6];
+        dft6<INV, 6, 6>(x, X);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] = X[k];
+    } else {
+        static_assert(S == 8, "S-point DFT for S in {2, 4, 6, 8}");
+        float2 E[4], O[4];
+        dft4<INV>(x[0], x[2], x[4], x[6], E[0], E[1], E[2], E[3]);
+        dft4<INV>(x[1], x[3], x[5], x[7], O[0], O[1], O[2], O[3]);
+        const float2 w1 = make_float2(kR2, INV ? kR2 : -kR2), w3 = make_float2(-kR2, INV ? kR2 : -kR2);
+        const float2 p[4] = {O[0], cmul(O[1], w1), rot<INV>(O[2]), cmul(O[3], w3)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            x[k] = cadd(E[k], p[k]);
+            x[k + 4] = csub(E[k], p[k]);
+        }
+    }
+}
+
+// Forward M-point DFT (M = 3n/2 = 6S) of n inputs zero-padded to M:
+// X[k1 + 6 k2] = sum_q2 exp(-2 pi i q2 k2 / S) tw[q2][k1]
+//                sum_q1 x[S q1 + q2] exp(-2 pi i q1 k1 / 6).
+// tw is exp(-2 pi i q2 k1 / M), times exp(2 pi i k1 / 3) on the a-side.
+template <int N, bool PHASE> __device__ __forceinline__ void fwd_pencil(const float2 (&x)[N],
+                                                                        float2 (&X)[3 * N / 2],
+                                                                        const float2 *tw) {
+    constexpr int S = N / 4;
+    float2 Y[S][6];
+#pragma unroll
+    for (int q2 = 0; q2 < S; ++q2) {
+        const float2 in[6] = {x[q2], x[S + q2], x[2 * S + q2], x[3 * S + q2], make_float2(0.f, 0.f),
+                              make_float2(0.f, 0.f)};
+        dft6<false, 4, 6>(in, Y[q2]);
+    }
+#pragma unroll
+    for (int q2 = 0; q2 < S; ++q2)
+#pragma unroll
+        for (int k1 = 1; k1 < 6; ++k1)
+            if (PHASE || q2 > 0) Y[q2][k1] = cmul(Y[q2][k1], tw[q2 * 6 + k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < 6; ++k1) {
+        float2 col[S];
+#pragma unroll
+        for (int q2 = 0; q2 < S; ++q2) col[q2] = Y[q2][k1];
+        dftS<S, false>(col);
+#pragma unroll
+        for (int k2 = 0; k2 < S; ++k2) X[k1 + 6 * k2] = col[k2];
+    }
+}
+
+// Inverse: x[s] = sum_k G[k] exp(2 pi i k s / M) / M for s in [0, n), the
+// conjugate transpose of fwd_pencil without the phase; iv holds
+// conj(tw[q2][k1]) / M.
+template <int N> __device__ __forceinline__ void inv_pencil(const float2 (&G)[3 * N / 2], float2 (&x)[N],
+                                                            const float2 *iv) {
+    constexpr int S = N / 4;
+    float2 Z[6][S];
+#pragma unroll
+    for (int k1 = 0; k1 < 6; ++k1) {
+#pragma unroll
+        for (int k2 = 0; k2 < S; ++k2) Z[k1][k2] = G[k1 + 6 * k2];
+        dftS<S, true>(Z[k1]);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 6; ++k1)
+#pragma unroll
+        for (int q2 = 0; q2 < S; ++q2) Z[k1][q2] = cmul(Z[k1][q2], iv[q2 * 6 + k1]);
+#pragma unroll
+    for (int q2 = 0; q2 < S; ++q2) {
+        const float2 in[6] = {Z[0][q2], Z[1][q2], Z[2][q2], Z[3][q2], Z[4][q2], Z[5][q2]};
+        float2 out[6];
+        dft6<true, 6, 4>(in, out);
+#pragma unroll
+        for (int q1 = 0; q1 < 4; ++q1) x[S * q1 + q2] = out[q1];
+    }
+}
+
+// (u - h)^e for e in {0, 1, 2}
+__device__ __forceinline__ float poww(int u, int h, int e) {
+    const float d = (float)(u - h);
+    return e == 0 ? 1.f : (e == 1 ? d : d * d);
+}
+
+constexpr int kPY = 4;  // pencils per block (blockDim.y); blockDim.x = 32 cells
+
+// X1: axis-3 DFT of the (l, m) pencils.  Arrays 0..6: C_p F (a-side, with
+// the phase); 7..9: (u3 - h)^e F.  T3 is [10][n][n][M][Bs].
+template <int N>
+__global__ void __launch_bounds__(32 * kPY) k_fq_x1(const float2 *__restrict__ F, const float *__restrict__ C,
+                                                    int Bp, int c0, float2 *__restrict__ T3, int Bs, FftTw tw) {
+    constexpr int n = N, h = N / 2, M = 3 * N / 2;
+    const int pen = blockIdx.x * kPY + threadIdx.y;
+    if (pen >= n * n) return;
+    const int cell = blockIdx.y * 32 + threadIdx.x, arr = blockIdx.z;
+    const float2 *src = F + (size_t)pen * n * Bp + c0 + cell;
+    float2 x[N], X[M];
+    if (arr < 7) {
+        const float *cp = C + (size_t)arr * n * n * n + (size_t)pen * n;
+#pragma unroll
+        for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], __ldg(cp + q));
+        fwd_pencil<N, true>(x, X, tw.fa);
+    } else {
+        const int e = arr - 7;
+#pragma unroll
+        for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], poww(q, h, e));
+        fwd_pencil<N, false>(x, X, tw.fw);
+    }
+    float2 *dst = T3 + ((size_t)arr * n * n + pen) * M * Bs + cell;
+#pragma unroll
+    for (int k = 0; k < M; ++k) dst[(size_t)k * Bs] = X[k];
+}
+
+// X2: axis-2 DFT of the (l, k3) pencils.  Arrays 0..6 the a-side; 7..12
+// the b-side combinations (e2, e3) = (0,0) (2,0) (0,2) (1,0) (0,1) (1,1),
+// from the X1 arrays 7 + e3 weighted by (u2 - h)^e2.  X is [13][n][M][M][Bs].
+template <int N>
+__global__ void __launch_bounds__(32 * kPY) k_fq_x2(const float2 *__restrict__ T3, int Bs,
+                                                    float2 *__restrict__ X, FftTw tw) {
+    constexpr int n = N, h = N / 2, M = 3 * N / 2;
+    const int pen = blockIdx.x * kPY + threadIdx.y;
+    if (pen >= n * M) return;
+    const int l = pen / M, k3 = pen - l * M;
+    const int cell = blockIdx.y * 32 + threadIdx.x, arr = blockIdx.z;
+    int sa = arr, e2 = 0;
+    if (arr >= 7) {
+        const int j = arr - 7;
+        sa = 7 + (j == 2 ? 2 : (j >= 4 ? 1 : 0));
+        e2 = (j == 1) ? 2 : ((j == 3 || j == 5) ? 1 : 0);
+    }
+    const float2 *src = T3 + (((size_t)sa * n + l) * n * M + k3) * Bs + cell;
+    float2 x[N], Xo[M];
+#pragma unroll
+    for (int m = 0; m < n; ++m) x[m] = src[(size_t)m * M * Bs];
+    if (arr < 7) {
+        fwd_pencil<N, true>(x, Xo, tw.fa);
+    } else {
+        if (e2) {
+#pragma unroll
+            for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2));
+        }
+        fwd_pencil<N, false>(x, Xo, tw.fw);
+    }
+    float2 *dst = X + (((size_t)arr * n + l) * M * M + k3) * Bs + cell;
+#pragma unroll
+    for (int k = 0; k < M; ++k) dst[(size_t)k * M * Bs] = Xo[k];
+}
+
+// Y: the direct convolution along axis 1 for the outputs i in
+// [I0, I0 + NI) of one (k2, k3) pencil, summed over the seven pairs.
+// Pair p takes the b-array Y00 (p = 0, 1), Y20, Y02, Y10, Y01, Y11 (p = 2..6)
+// weighted by (u1 - h)^e1, e1 = 2 for p = 1, 1 for p = 4, 5, else 0.
+// Complex products use packed FMAs with split accumulators:
+// A += Re(a) b, B += Im(a) b, a b = (A.x - B.y, A.y + B.x).
+template <int N, int NI, int I0>
+__device__ __forceinline__ void y_part(const float2 *__restrict__ base, size_t ps, float2 *__restrict__ dst,
+                                       size_t os) {
+    constexpr int n = N, h = N / 2;
+    unsigned long long A[NI], B[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) A[i] = B[i] = 0ull;
+#pragma unroll 1
+    for (int p = 0; p < 7; ++p) {
+        const int sy = (p == 0 || p == 1) ? 7 : p + 6;
+        const int e1 = (p == 1) ? 2 : ((p == 4 || p == 5) ? 1 : 0);
+        unsigned long long yb[N];
+#pragma unroll
+        for (int u = 0; u < n; ++u) {
+            const float2 v = cscale(base[((size_t)sy * n + u) * ps], poww(u, h, e1));
+            yb[u] = pk2(v.x, v.y);
+        }
+        const float2 *ap = base + (size_t)p * n * ps;
+#pragma unroll
+        for (int l = 0; l < n; ++l) {
+            // outputs i with u = i + h - l in [0, n)
+            if (l - h >= I0 + NI || l + h <= I0) continue;
+            const float2 a = ap[(size_t)l * ps];
+            const unsigned long long ar = pk2(a.x, a.x), ai = pk2(a.y, a.y);
+#pragma unroll
+            for (int ii = 0; ii < NI; ++ii) {
+                const int u = I0 + ii + h - l;
+                if (u >= 0 && u < n) {
+                    A[ii] = fma2(ar, yb[u], A[ii]);
+                    B[ii] = fma2(ai, yb[u], B[ii]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < NI; ++ii) {
+        const float2 a = up2(A[ii]), b = up2(B[ii]);
+        dst[(size_t)ii * os] = make_float2(a.x - b.y, a.y + b.x);
+    }
+}
+
+// blockIdx.z selects the output half when NI = N / 2.  G is [n][M][M][Bs].
+template <int N, int NI>
+__global__ void __launch_bounds__(32 * kPY) k_fq_y(const float2 *__restrict__ X, int Bs, float2 *__restrict__ G) {
+    constexpr int M = 3 * N / 2;
+    const int pen = blockIdx.x * kPY + threadIdx.y;
+    if (pen >= M * M) return;
+    const int cell = blockIdx.y * 32 + threadIdx.x;
+    const size_t ps = (size_t)M * M * Bs;  // stride of the axis-1 index
+    const float2 *base = X + (size_t)pen * Bs + cell;
+    float2 *dst = G + (size_t)pen * Bs + cell;
+    if (NI == N || blockIdx.z == 0) {
+        y_part<N, NI, 0>(base, ps, dst, ps);
+    } else {
+        y_part<N, NI, (NI < N ? NI : 0)>(base, ps, dst + (size_t)NI * ps, ps);
+    }
+}
+
+// Z1: inverse axis-2 DFT of the (i, k3) pencils, outputs xi2 in [0, n).
+// H is [n][n][M][Bs].
+template <int N>
+__global__ void __launch_bounds__(32 * kPY) k_fq_z1(const float2 *__restrict__ G, int Bs, float2 *__restrict__ H,
+                                                    FftTw tw) {
+    constexpr int n = N, M = 3 * N / 2;
+    const int pen = blockIdx.x * kPY + threadIdx.y;
+    if (pen >= n * M) return;
+    const int i = pen / M, k3 = pen - i * M;
+    const int cell = blockIdx.y * 32 + threadIdx.x;
+    const float2 *src = G + ((size_t)i * M * M + k3) * Bs + cell;
+    float2 g[M], x[N];
+#pragma unroll
+    for (int k = 0; k < M; ++k) g[k] = src[(size_t)k * M * Bs];
+    inv_pencil<N>(g, x, tw.iv);
+    float2 *dst = H + ((size_t)i * n * M + k3) * Bs + cell;
+#pragma unroll
+    for (int j = 0; j < n; ++j) dst[(size_t)j * M * Bs] = x[j];
+}
+
+// Z2: inverse axis-3 DFT of the (i, j) pencils into q (FP64, stride Bp).
+template <int N>
+__global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H, int Bs, double2 *__restrict__ q,
+                                                    int Bp, int c0, FftTw tw) {
+    constexpr int n = N, M = 3 * N / 2;
+    const int pen = blockIdx.x * kPY + threadIdx.y;
+    if (pen >= n * n) return;
+    const int cell = blockIdx.y * 32 + threadIdx.x;
+    const float2 *src = H + (size_t)pen * M * Bs + cell;
+    float2 g[M], x[N];
+#pragma unroll
+    for (int k = 0; k < M; ++k) g[k] = src[(size_t)k * Bs];
+    inv_pencil<N>(g, x, tw.iv);
+    double2 *dst = q + (size_t)pen * n * Bp + c0 + cell;
+#pragma unroll
+    for (int k = 0; k < n; ++k) dst[(size_t)k * Bp] = make_double2((double)x[k].x, (double)x[k].y);
+}
+
+template <int N>
+cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc, float2 *scratch,
+                      int Bs, double2 *q, cudaStream_t st, int stage) {
+    constexpr int n = N, M = 3 * N / 2;
+    constexpr int NI = (N >= 32) ? N / 2 : N;  // outputs per thread in Y
+    float2 *T3 = scratch, *X = scratch + fftq_t3_elems(n, Bs);
+    float2 *G = T3, *H = T3 + (size_t)n * M * M * Bs;  // T3 is dead after X2
+    const dim3 blk(32, kPY);
+    const int gc = Bc / 32;
+    if (stage < 0 || stage == 0)
+        k_fq_x1<N><<<dim3((n * n + kPY - 1) / kPY, gc, 10), blk, 0, st>>>(F, C, Bp, c0, T3, Bs, tw);
+    if (stage < 0 || stage == 1) k_fq_x2<N><<<dim3((n * M + kPY - 1) / kPY, gc, 13), blk, 0, st>>>(T3, Bs, X, tw);
+    if (stage < 0 || stage == 2) k_fq_y<N, NI><<<dim3((M * M + kPY - 1) / kPY, gc, N / NI), blk, 0, st>>>(X, Bs, G);
+    if (stage < 0 || stage == 3) k_fq_z1<N><<<dim3((n * M + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(G, Bs, H, tw);
+    if (stage < 0 || stage == 4)
+        k_fq_z2<N><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q, Bp, c0, tw);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool fftq_supported(int n) { return n == 8 || n == 16 || n == 24 || n == 32; }
+
+size_t fftq_t3_elems(int n, int Bs) { return (size_t)10 * n * n * (3 * n / 2) * Bs; }
+
+size_t fftq_scratch_elems(int n, int Bs) {
+    const size_t M = 3 * (size_t)n / 2;
+    return fftq_t3_elems(n, Bs) + (size_t)13 * n * M * M * Bs;
+}
+
+FftTw fftq_twiddles(int n) {
+    FftTw t{};
+    const int M = 3 * n / 2, S = n / 4;
+    const double PI = std::acos(-1.0);
+    for (int q2 = 0; q2 < S; ++q2)
+        for (int k1 = 0; k1 < 6; ++k1) {
+            const double a = -2. * PI * q2 * k1 / M, ph = 2. * PI * k1 / 3.;
+            t.fw[q2 * 6 + k1] = make_float2((float)std::cos(a), (float)std::sin(a));
+            t.fa[q2 * 6 + k1] = make_float2((float)std::cos(a + ph), (float)std::sin(a + ph));
+            t.iv[q2 * 6 + k1] = make_float2((float)(std::cos(a) / M), (float)(-std::sin(a) / M));
+        }
+    return t;
+}
+
+void fftq_coefficients(const double *shat, const double *ahat, const double *cw, double h_eta, int n,
+                       std::vector<float> &C) {
+    const size_t n3 = (size_t)n * n * n;
+    C.assign(7 * n3, 0.f);
+    const double h2 = h_eta * h_eta;
+    // pairs: (ahat, 1), (S00, u1^2), (S11, u2^2), (S22, u3^2), (S01, u1 u2), (S02, u1 u3), (S12, u2 u3);
+    // shat per omega: S00, S01, S02, S11, S12, S22
+    static const int sidx[6] = {0, 3, 5, 1, 2, 4};
+    static const double mult[6] = {1., 1., 1., 2., 2., 2.};
+    for (size_t o = 0; o < n3; ++o) {
+        C[o] = (float)(cw[o] * ahat[o]);
+        for (int p = 0; p < 6; ++p) C[(p + 1) * n3 + o] = (float)(-mult[p] * h2 * cw[o] * shat[6 * o + sidx[p]]);
+    }
+}
+
+cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
+                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage) {
+    if (Bc <= 0 || Bc % 32 || Bc > Bs || c0 % 32 || c0 + Bc > Bp || stage < -1 || stage > 4)
+        return cudaErrorInvalidValue;
+    switch (n) {
+    case 8: return launch_fq<8>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
+    case 16: return launch_fq<16>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
+    case 24: return launch_fq<24>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
+    case 32: return launch_fq<32>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace lp

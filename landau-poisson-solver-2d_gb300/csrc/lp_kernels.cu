@@ -4,6 +4,7 @@
 //   A = source/advection_1.cpp           P = source/PoissonFunctions.cpp
 //   S = source/SetInit_1.cpp             MC = source/MomentCalculations.cpp
 #include "lp_kernels.cuh"
+#include "lp_f32x2.cuh"
 
 #include <algorithm>
 #include <cstdint>
@@ -348,28 +349,6 @@ template <> struct LinesCfg<24> { static constexpr int KT = 12; };
 template <> struct LinesCfg<32> { static constexpr int KT = 8; };
 
 __device__ __forceinline__ float pick4(const float4 &v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w)); }
-
-// Packed FP32x2 helpers (Blackwell f32x2 arithmetic on 64-bit register pairs).
-__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float2 up2(unsigned long long v) {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-    return make_float2(lo, hi);
-}
-__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -872,8 +851,9 @@ __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const
     if (c >= B) return;
     if (cdt) scale = cdt[c] * kfac;
     double tg[5] = {0, 0, 0, 0, 0}, ac[5] = {0, 0, 0, 0, 0};
-    for (int k = lane; k < nchunk; k += 32)
-        for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
+    if (tpart)  // nullptr: the target moments are zero
+        for (int k = lane; k < nchunk; k += 32)
+            for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
     for (int k = lane; k < nrc; k += 32)
         for (int m = 0; m < 5; ++m) ac[m] += apart[((long long)c * nrc + k) * 5 + m];
     for (int off = 16; off > 0; off >>= 1)

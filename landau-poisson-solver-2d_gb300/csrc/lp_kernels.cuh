@@ -91,6 +91,27 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
                                   int Bp, double2 *q, cudaStream_t st, int warps = 2,
                                   cudaStream_t st_odd = nullptr);
 
+// Mixed path, convolution form of the same contraction (lp_fftq.cu): the
+// weight splits into seven omega-factors C[7][n^3] times polynomials in u,
+// so q is a sum of seven windowed convolutions, evaluated with M = 3n/2
+// point DFTs along axes 2 and 3 and summed directly along axis 1.
+struct FftTw {
+    float2 fw[48];  // exp(-2 pi i q2 k1 / M) at q2 * 6 + k1
+    float2 fa[48];  // fw exp(2 pi i k1 / 3): the a-side, output shift n/2
+    float2 iv[48];  // conj(fw) / M
+};
+bool fftq_supported(int n);
+FftTw fftq_twiddles(int n);
+void fftq_coefficients(const double *shat, const double *ahat, const double *cw, double h_eta, int n,
+                       std::vector<float> &C);
+size_t fftq_t3_elems(int n, int Bs);
+size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
+// Cells [c0, c0 + Bc) of F and q (stride Bp); Bc and c0 multiples of 32,
+// Bc <= Bs, the cells of the scratch.  stage -1 runs the five kernels;
+// 0..4 only one of them (X1, X2, Y, Z1, Z2), on the scratch a full run left.
+cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
+                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1);
+
 // Moment-conserving projection of q in place (FP64).
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
                             int n3, int Bp, double *part, int nchunk, double *lam,
@@ -110,7 +131,8 @@ cudaError_t launch_project(const double2 *q0, const double2 *q1, const double2 *
 // FP64 values from the mode array (minimal-norm 5x5 Lagrange correction), in
 // two parts: the FP64 target moments from q0..q3 (independent of the DG
 // projection, so they can run beside it) and, once dU exists, its actual
-// moments, the multipliers and (apply) the correction of dU.
+// moments, the multipliers and (apply) the correction of dU.  tpart nullptr
+// in launch_moment_finish: the target moments are zero.
 cudaError_t launch_moment_target(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3,
                                  double nu, const double *gmom, int n3, int Bp, int nchunk, double *tpart,
                                  cudaStream_t st, Rates rates = Rates{});

@@ -41,7 +41,7 @@ EXPORTS = [
     "lp_batch_step", "lp_batch_classes", "lp_batch_class_info", "lp_batch_autotune",
     "lp_field_energy", "lp_collision_vjp", "lp_advect_vjp", "lp_step_vjp", "lp_field_energy_gradient",
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
-    "lp_autotune", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
+    "lp_autotune", "lp_set_schedule", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -156,6 +156,7 @@ def lib():
         L.lp_rk4_cell_lin.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]
         L.lp_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int)]
+        L.lp_set_schedule.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
         L.lp_diagnostics_append.argtypes = [_vp, ctypes.c_char_p, ctypes.c_char_p]
         L.lp_marginal_x1v1.argtypes = [_vp, _dp]
         L.lp_state_append.argtypes = [_vp, ctypes.c_char_p]
@@ -332,7 +333,8 @@ class Context:
 
     def time_kernel(self, which=0, reps=10):
         """Average ms per launch of a stage (0 contraction, 1 forward transform,
-        2 conservation, 3 DG projection), CUDA events on the context's stream."""
+        2 conservation, 3 DG projection, 4..8 the five kernels of the convolution
+        form), CUDA events on the context's stream."""
         ms = ctypes.c_double()
         self._chk(self.L.lp_time_kernel(self.h, int(which), int(reps), ctypes.byref(ms)))
         return ms.value
@@ -343,11 +345,17 @@ class Context:
         return out
 
     def autotune(self, reps=3, cache_path=None):
-        """Pick the fastest collision schedule; returns (cells per pass, warps per line block)."""
+        """Pick the fastest collision schedule; returns (cells per pass, contraction form):
+        the form is 0 for the convolution form, 2 or 4 for the line-tiled sum with that
+        many warps per line block."""
         bp, lw = ctypes.c_int(), ctypes.c_int()
         self._chk(self.L.lp_autotune(self.h, int(reps), cache_path.encode() if cache_path else None,
                                      ctypes.byref(bp), ctypes.byref(lw)))
         return bp.value, lw.value
+
+    def set_schedule(self, pass_cells, line_warps):
+        """Set the collision schedule (see autotune for the forms)."""
+        self._chk(self.L.lp_set_schedule(self.h, int(pass_cells), int(line_warps)))
 
     def diagnostics(self):
         """{mass, p1, p2, p3, KiE, EleE, sqrt EleE, log sqrt EleE, KiE + EleE, entropy}"""
