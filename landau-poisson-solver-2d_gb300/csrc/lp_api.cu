@@ -77,6 +77,7 @@ struct lp_ctx {
     double *cpart = nullptr, *lam = nullptr, *dU = nullptr;
     // moment reconciliation (mixed path)
     double *gmom = nullptr, *gm_inv = nullptr, *mtpart = nullptr, *mapart = nullptr, *mlam = nullptr;
+    double *incpart = nullptr;  // per-block DG moment partials of the fused projection
     int nrc = 16;
     // adjoint workspace (FP64 contexts, allocated by the first adjoint call)
     struct Adj {
@@ -182,6 +183,7 @@ template <typename R> lp_status alloc_workspace(lp_ctx *c) {
         LP_TRY(dalloc(c, &c->mtpart, (size_t)c->nchunk * 5 * Bp));
         LP_TRY(dalloc(c, &c->mapart, (size_t)c->nrc * 5 * Bp));
         LP_TRY(dalloc(c, &c->mlam, 5 * Bp));
+        LP_TRY(dalloc(c, &c->incpart, (size_t)lp::project_inc_blocks(T.nv) * 5 * Bp));
     }
     return LP_OK;
 }
@@ -489,6 +491,34 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool d
     return LP_OK;
 }
 
+// The mixed path with LP_FIX_F1 fixed: the DG projection writes the
+// coefficient increments and the partial sums of their moments, and the
+// multipliers of the moment correction follow; the scatter adds both to U.
+bool fused_tail(const lp_ctx *c) { return c->mixed && (c->T.prm.fixes & LP_FIX_F1); }
+
+lp_status project_fused(lp_ctx *c, int c0, int B, int Bp) {
+    const lp::Tables &T = c->T;
+    const bool target = c->WLin != nullptr;
+    cudaStream_t tst = (target && c->side) ? c->side : c->stream;
+    if (target) {
+        if (tst != c->stream) {
+            LP_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+            LP_CUDA(cudaStreamWaitEvent(tst, c->ev_fork, 0));
+        }
+        LP_CUDA(lp::launch_moment_target(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, c->gmom, T.n3, Bp, c->nchunk,
+                                         c->mtpart, tst, rates_at(c, c0)));
+        if (tst != c->stream) LP_CUDA(cudaEventRecord(c->ev_join, tst));
+    }
+    LP_CUDA(lp::launch_project_inc(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const float *)c->tfac, T.n, T.nv,
+                                   Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
+                                   (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0)));
+    if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
+    LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.nv, B, Bp, c->gm_inv,
+                                  T.prm.dt * kfac, kfac, c->mlam, c->stream, rates_at(c, c0)));
+    return LP_OK;
+}
+
 // Collision step of cells [c0, c0+B), B <= Bcap (LP_ompi_1.cpp:502-532).
 template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     using C = typename V2<R>::t;
@@ -500,6 +530,7 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
     LP_TRY(stage_q<R>(c, Bp, c->q[0]));
     LP_TRY(rk4_stages<R>(c, c0, Bp));
+    if (fused_tail(c)) return project_fused(c, c0, B, Bp);
     LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
 }
@@ -531,9 +562,12 @@ lp_status collide(lp_ctx *c, int c0, int c1) {
         if (total > pass && !(c->T.prm.fixes & LP_FIX_F1))
             return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one batch");
         LP_TRY(c->mixed ? collide_batch<float>(c, b0, B) : collide_batch<double>(c, b0, B));
-        const bool fix = c->mixed && (c->T.prm.fixes & LP_FIX_F1);
-        LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream, fix ? c->mlam : nullptr, c->T.nv, c->T.dv,
-                                   c->T.prm.lv));
+        if (fused_tail(c))
+            LP_CUDA(lp::launch_scatter_inc(c->dU, round32(B), B, c->T.nv, b0, c->U, c->mlam, c->T.dv, c->T.prm.lv,
+                                           c->stream));
+        else
+            LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream, nullptr, c->T.nv, c->T.dv,
+                                       c->T.prm.lv));
     }
     return LP_OK;
 }

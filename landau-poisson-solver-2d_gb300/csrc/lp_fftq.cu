@@ -36,7 +36,7 @@
 // one cell; the 32 lanes of a warp are 32 cells, so every load and store is
 // coalesced on the cell-minor arrays.  Arithmetic is FP32.
 #include "lp_kernels.cuh"
-#include "lp_f32x2.cuh"
+#include "lp_dev.cuh"
 
 #include <cmath>
 
@@ -270,31 +270,51 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_x2(const float2 *__restrict__ T
 // [I0, I0 + NI) of one (k2, k3) pencil, summed over the seven pairs.
 // Pair p takes the b-array Y00 (p = 0, 1), Y20, Y02, Y10, Y01, Y11 (p = 2..6)
 // weighted by (u1 - h)^e1, e1 = 2 for p = 1, 1 for p = 4, 5, else 0.
+// The 2n values of a pair (b-array along u1, a-array along l) are copied
+// into shared memory with cp.async, two pairs in flight: the copies of pair
+// p + 1 run while pair p is summed.  Every thread copies and reads only its
+// own column (sm + v * threads), so no block barrier is needed.
 // Complex products use packed FMAs with split accumulators:
 // A += Re(a) b, B += Im(a) b, a b = (A.x - B.y, A.y + B.x).
+template <int N>
+__device__ __forceinline__ void y_issue(const float2 *__restrict__ base, size_t ps, int p, float2 *sm, int nt) {
+    const int sy = (p == 0 || p == 1) ? 7 : p + 6;
+#pragma unroll
+    for (int u = 0; u < N; ++u) cp_async8(sm + u * nt, base + ((size_t)sy * N + u) * ps);
+#pragma unroll
+    for (int l = 0; l < N; ++l) cp_async8(sm + (N + l) * nt, base + ((size_t)p * N + l) * ps);
+    cp_async_commit();
+}
+
 template <int N, int NI, int I0>
 __device__ __forceinline__ void y_part(const float2 *__restrict__ base, size_t ps, float2 *__restrict__ dst,
-                                       size_t os) {
+                                       size_t os, float2 *sm, int nt) {
     constexpr int n = N, h = N / 2;
     unsigned long long A[NI], B[NI];
 #pragma unroll
     for (int i = 0; i < NI; ++i) A[i] = B[i] = 0ull;
+    y_issue<N>(base, ps, 0, sm, nt);
 #pragma unroll 1
     for (int p = 0; p < 7; ++p) {
-        const int sy = (p == 0 || p == 1) ? 7 : p + 6;
+        float2 *cur = sm + (p & 1) * 2 * N * nt;
+        if (p + 1 < 7) {
+            y_issue<N>(base, ps, p + 1, sm + ((p + 1) & 1) * 2 * N * nt, nt);
+            cp_async_wait1();
+        } else {
+            cp_async_wait0();
+        }
         const int e1 = (p == 1) ? 2 : ((p == 4 || p == 5) ? 1 : 0);
         unsigned long long yb[N];
 #pragma unroll
         for (int u = 0; u < n; ++u) {
-            const float2 v = cscale(base[((size_t)sy * n + u) * ps], poww(u, h, e1));
+            const float2 v = cscale(cur[u * nt], poww(u, h, e1));
             yb[u] = pk2(v.x, v.y);
         }
-        const float2 *ap = base + (size_t)p * n * ps;
 #pragma unroll
         for (int l = 0; l < n; ++l) {
             // outputs i with u = i + h - l in [0, n)
             if (l - h >= I0 + NI || l + h <= I0) continue;
-            const float2 a = ap[(size_t)l * ps];
+            const float2 a = cur[(N + l) * nt];
             const unsigned long long ar = pk2(a.x, a.x), ai = pk2(a.y, a.y);
 #pragma unroll
             for (int ii = 0; ii < NI; ++ii) {
@@ -314,19 +334,23 @@ __device__ __forceinline__ void y_part(const float2 *__restrict__ base, size_t p
 }
 
 // blockIdx.z selects the output half when NI = N / 2.  G is [n][M][M][Bs].
-template <int N, int NI>
-__global__ void __launch_bounds__(32 * kPY) k_fq_y(const float2 *__restrict__ X, int Bs, float2 *__restrict__ G) {
+// Dynamic shared memory: 2 stages x 2N values x blockDim threads.
+template <int N, int NI, int PY>
+__global__ void __launch_bounds__(32 * PY) k_fq_y(const float2 *__restrict__ X, int Bs, float2 *__restrict__ G) {
     constexpr int M = 3 * N / 2;
-    const int pen = blockIdx.x * kPY + threadIdx.y;
+    extern __shared__ float2 ysm[];
+    const int pen = blockIdx.x * PY + threadIdx.y;
     if (pen >= M * M) return;
     const int cell = blockIdx.y * 32 + threadIdx.x;
     const size_t ps = (size_t)M * M * Bs;  // stride of the axis-1 index
     const float2 *base = X + (size_t)pen * Bs + cell;
     float2 *dst = G + (size_t)pen * Bs + cell;
+    float2 *sm = ysm + threadIdx.y * 32 + threadIdx.x;
+    constexpr int nt = 32 * PY;
     if (NI == N || blockIdx.z == 0) {
-        y_part<N, NI, 0>(base, ps, dst, ps);
+        y_part<N, NI, 0>(base, ps, dst, ps, sm, nt);
     } else {
-        y_part<N, NI, (NI < N ? NI : 0)>(base, ps, dst + (size_t)NI * ps, ps);
+        y_part<N, NI, (NI < N ? NI : 0)>(base, ps, dst + (size_t)NI * ps, ps, sm, nt);
     }
 }
 
@@ -380,7 +404,15 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
     if (stage < 0 || stage == 0)
         k_fq_x1<N><<<dim3((n * n + kPY - 1) / kPY, gc, 10), blk, 0, st>>>(F, C, Bp, c0, T3, Bs, tw);
     if (stage < 0 || stage == 1) k_fq_x2<N><<<dim3((n * M + kPY - 1) / kPY, gc, 13), blk, 0, st>>>(T3, Bs, X, tw);
-    if (stage < 0 || stage == 2) k_fq_y<N, NI><<<dim3((M * M + kPY - 1) / kPY, gc, N / NI), blk, 0, st>>>(X, Bs, G);
+    if (stage < 0 || stage == 2) {
+        constexpr int PY = (N >= 32) ? 2 : 4;
+        const size_t smem = sizeof(float2) * 2 * 2 * N * 32 * PY;
+        // opt-in above 48 KB of dynamic shared memory (per device, so on every call)
+        const cudaError_t e = cudaFuncSetAttribute(k_fq_y<N, NI, PY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+        k_fq_y<N, NI, PY><<<dim3((M * M + PY - 1) / PY, gc, N / NI), dim3(32, PY), smem, st>>>(X, Bs, G);
+    }
     if (stage < 0 || stage == 3) k_fq_z1<N><<<dim3((n * M + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(G, Bs, H, tw);
     if (stage < 0 || stage == 4)
         k_fq_z2<N><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q, Bp, c0, tw);

@@ -4,7 +4,7 @@
 //   A = source/advection_1.cpp           P = source/PoissonFunctions.cpp
 //   S = source/SetInit_1.cpp             MC = source/MomentCalculations.cpp
 #include "lp_kernels.cuh"
-#include "lp_f32x2.cuh"
+#include "lp_dev.cuh"
 
 #include <algorithm>
 #include <cstdint>
@@ -350,16 +350,6 @@ template <> struct LinesCfg<32> { static constexpr int KT = 8; };
 
 __device__ __forceinline__ float pick4(const float4 &v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w)); }
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // One k-tile of output lines.  The LW warps of a block take the
 // plane pairs of the same (line, tile, 32 cells) in turn; each warp stages
@@ -844,9 +834,12 @@ __global__ void k_mom_actual(const double *__restrict__ dU, const double *__rest
     if (t < 5) part[((long long)cc * nrc + blockIdx.x) * 5 + t] = red[t][0];
 }
 
+// The multipliers of each cell: lambda = Gm^-1 (scale target - actual), the
+// actual moments summed from nk partials at apart[c sc + k sk + m sm].
 __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const double *__restrict__ apart,
-                             int nrc, const double *__restrict__ gm_inv, double scale, double kfac,
-                             const double *__restrict__ cdt, int B, int Bp, double *__restrict__ lam) {
+                             int nk, long long sc, long long sk, long long sm, const double *__restrict__ gm_inv,
+                             double scale, double kfac, const double *__restrict__ cdt, int B, int Bp,
+                             double *__restrict__ lam) {
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
     if (cdt) scale = cdt[c] * kfac;
@@ -854,8 +847,8 @@ __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const
     if (tpart)  // nullptr: the target moments are zero
         for (int k = lane; k < nchunk; k += 32)
             for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
-    for (int k = lane; k < nrc; k += 32)
-        for (int m = 0; m < 5; ++m) ac[m] += apart[((long long)c * nrc + k) * 5 + m];
+    for (int k = lane; k < nk; k += 32)
+        for (int m = 0; m < 5; ++m) ac[m] += apart[c * sc + k * sk + m * sm];
     for (int off = 16; off > 0; off >>= 1)
         for (int m = 0; m < 5; ++m) {
             tg[m] += __shfl_down_sync(FULL, tg[m], off);
@@ -910,6 +903,122 @@ __global__ void k_scatter(const double *__restrict__ dU, long long nrec, long lo
     }
     double *u = U + 7 * (r0 + r);
     u[0] = d[0]; u[6] = d[4]; u[3] = d[1]; u[4] = d[2]; u[5] = d[3];
+}
+
+// ---------------------------------------------------------------- mixed tail
+// Mixed path with LP_FIX_F1 fixed.  The mass-matrix inverse of the last
+// projection step maps the old coefficients to themselves (its u-terms
+// cancel), so the increment of the 5 collided coefficients of a record is
+// dt kfac (19/4 tp0 - 15 tp5, 12 tp2, 12 tp3, 12 tp4, 60 tp5 - 15 tp0) and
+// needs no state.  k_proj1_inc writes it cell-minor, Inc[kt][5][Bp], with
+// per-block partial sums of its 5 DG moments (part[blk][5][Bp]);
+// k_scatter_inc adds increment and moment correction to U through a
+// shared-memory transpose, so both sides of the copy are coalesced.
+constexpr int kIncWarps = 8;
+
+__global__ void __launch_bounds__(32 * kIncWarps)
+    k_proj1_inc(const float2 *__restrict__ Z, const float *__restrict__ tf, int n, int nv, int Bp, int B, double dt,
+                double kfac, const double *__restrict__ cdt, double dv, double lv, MomRow mr,
+                double *__restrict__ Inc, double *__restrict__ part) {
+    __shared__ double red[kIncWarps][5][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + lane;
+    const int nch = (nv + JB - 1) / JB, W = nv * nv * nch;
+    const int it = blockIdx.x * kIncWarps + w;
+    double m[5] = {0, 0, 0, 0, 0};
+    if (it < W && c < B) {
+        const int j3 = it % nv, j2 = (it / nv) % nv, ch = it / (nv * nv);
+        const int j0 = ch * JB;
+        const double s = (cdt ? cdt[c] : dt) * kfac;
+        float a[7][JB];
+#pragma unroll
+        for (int e = 0; e < 7; ++e)
+#pragma unroll
+            for (int jj = 0; jj < JB; ++jj) a[e][jj] = 0.f;
+        const long long zs = (long long)n * nv * nv * Bp;
+        for (int k1 = 0; k1 < n; ++k1) {
+            const long long zb = (((long long)k1 * nv + j2) * nv + j3) * Bp + c;
+            const float2 z0 = Z[zb], z1 = Z[zb + zs], z2 = Z[zb + 2 * zs], z3 = Z[zb + 3 * zs], z4 = Z[zb + 4 * zs];
+#pragma unroll
+            for (int jj = 0; jj < JB; ++jj) {
+                if (j0 + jj < nv) {
+                    const int j1 = j0 + jj;
+                    const float *t0 = tf + 2 * ((0 * n + k1) * nv + j1);
+                    const float *t1 = tf + 2 * ((1 * n + k1) * nv + j1);
+                    const float *t2 = tf + 2 * ((2 * n + k1) * nv + j1);
+                    a[0][jj] += t0[0] * z0.x - t0[1] * z0.y;
+                    a[1][jj] += t1[0] * z0.x - t1[1] * z0.y;
+                    a[2][jj] += t0[0] * z1.x - t0[1] * z1.y;
+                    a[3][jj] += t0[0] * z3.x - t0[1] * z3.y;
+                    a[4][jj] += t2[0] * z0.x - t2[1] * z0.y;
+                    a[5][jj] += t0[0] * z2.x - t0[1] * z2.y;
+                    a[6][jj] += t0[0] * z4.x - t0[1] * z4.y;
+                }
+            }
+        }
+        const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
+#pragma unroll
+        for (int jj = 0; jj < JB; ++jj) {
+            if (j0 + jj >= nv) continue;
+            const int j1 = j0 + jj;
+            const long long kt = ((long long)j1 * nv + j2) * nv + j3;
+            const double tp0 = a[0][jj], tp2 = a[1][jj], tp3 = a[2][jj], tp4 = a[3][jj];
+            const double tp5 = (double)a[4][jj] + (double)a[5][jj] + (double)a[6][jj];
+            const double d0 = s * (4.75 * tp0 - 15. * tp5), d4 = s * (60. * tp5 - 15. * tp0);
+            const double d1 = 12. * s * tp2, d2 = 12. * s * tp3, d3 = 12. * s * tp4;
+            double *o = Inc + kt * 5 * Bp + c;
+            o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
+            const double G1 = -lv + (j1 + 0.5) * dv, g2 = G1 * G1 + G2 * G2 + G3 * G3;
+            m[0] += d0 + 0.25 * d4;
+            m[1] += G1 * d0 + mr.dv12 * d1 + 0.25 * G1 * d4;
+            m[2] += G2 * d0 + mr.dv12 * d2 + 0.25 * G2 * d4;
+            m[3] += G3 * d0 + mr.dv12 * d3 + 0.25 * G3 * d4;
+            m[4] += (g2 + mr.dv2q) * d0 + mr.dv6 * (G1 * d1 + G2 * d2 + G3 * d3) + (mr.c19 + 0.25 * g2) * d4;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) red[w][q][lane] = m[q];
+    __syncthreads();
+    if (w == 0 && c < Bp) {
+        for (int q = 0; q < 5; ++q) {
+            double t = 0.;
+            for (int v = 0; v < kIncWarps; ++v) t += red[v][q][lane];
+            part[((long long)blockIdx.x * 5 + q) * Bp + c] = t;
+        }
+    }
+}
+
+constexpr int kScatRec = 32;  // records per tile (x 32 cells)
+__global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ Inc, int Bp, int B, int nv, int c0,
+                                                     double *__restrict__ U, const double *__restrict__ lam,
+                                                     double dv, double lv, MomRow mr) {
+    __shared__ double S[kScatRec][5][33];
+    __shared__ double L[32][5];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const long long nv3 = (long long)nv * nv * nv;
+    const long long kt0 = (long long)blockIdx.x * kScatRec;
+    const int cb = blockIdx.y * 32;
+    // rows (record, coefficient) of 32 cells: coalesced along the cells
+    for (int row = w; row < kScatRec * 5; row += 8) {
+        const int r = row / 5, q = row - r * 5;
+        const long long kt = kt0 + r;
+        S[r][q][lane] = (kt < nv3 && cb + lane < B) ? Inc[(kt * 5 + q) * Bp + cb + lane] : 0.;
+    }
+    if (t < 160) {
+        const int cc = t / 5, q = t - cc * 5;
+        L[cc][q] = (lam && cb + cc < B) ? lam[5 * (cb + cc) + q] : 0.;
+    }
+    __syncthreads();
+    // one cell per warp pass, lanes along the records: coalesced on U
+    const long long kt = kt0 + lane;
+    if (kt >= nv3) return;
+    for (int cc = w; cc < 32; cc += 8) {
+        if (cb + cc >= B) break;
+        double a[5] = {S[lane][0][cc], S[lane][1][cc], S[lane][2][cc], S[lane][3][cc], S[lane][4][cc]};
+        if (lam) mom_correct(a, L[cc], dv, lv, nv, kt, mr);
+        double *u = U + 7 * ((long long)(c0 + cb + cc) * nv3 + kt);
+        u[0] += a[0]; u[3] += a[1]; u[4] += a[2]; u[5] += a[3]; u[6] += a[4];
+    }
 }
 
 // ---------------------------------------------------------------- Poisson
@@ -1841,11 +1950,45 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
                                  double kfac, double *lam, double *dU, cudaStream_t st, Rates rates, bool apply) {
     const MomRow mr = mom_row(dv);
     k_mom_actual<<<dim3(nrc, B), 256, 0, st>>>(dU, U, nv, dv, lv, mr, c0, nrc, apart);
-    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, gm_inv, scale, kfac, rates.dt, B, Bp, lam);
+    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, apart, nrc, (long long)nrc * 5, 5, 1, gm_inv, scale,
+                                              kfac, rates.dt, B, Bp, lam);
     if (apply) {
         const long long nrec = (long long)B * nv * nv * nv;
         k_mom_apply<<<grid1(nrec, 256), 256, 0, st>>>(dU, lam, nv, dv, lv, mr, nrec);
     }
+    return cudaGetLastError();
+}
+
+int project_inc_blocks(int nv) { return (nv * nv * ((nv + JB - 1) / JB) + kIncWarps - 1) / kIncWarps; }
+
+cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
+                               const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
+                               double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
+                               double *part, double lv, double dv, cudaStream_t st, Rates rates) {
+    const long long n3 = (long long)n * n * n;
+    k_qcomb<float><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Bp, rates.nu, Qc);
+    const int nch = (nv + JB - 1) / JB;
+    k_proj3<float><<<grid1((long long)n * n * nch * Bp, 128), 128, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
+    k_proj2<float><<<grid1((long long)n * nv * nch * Bp, 128), 128, 0, st>>>(Y, tfac, n, nv, Bp, Z);
+    const double kfac = 1. / scalev / scaleL / scale3;
+    k_proj1_inc<<<dim3(project_inc_blocks(nv), Bp / 32), 32 * kIncWarps, 0, st>>>(
+        Z, tfac, n, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int nv, int B, int Bp,
+                              const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
+                              Rates rates) {
+    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, part, project_inc_blocks(nv), 1, 5LL * Bp, Bp, gm_inv,
+                                              scale, kfac, rates.dt, B, Bp, lam);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_inc(const double *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
+                               double dv, double lv, cudaStream_t st) {
+    const long long nv3 = (long long)nv * nv * nv;
+    k_scatter_inc<<<dim3((unsigned)((nv3 + kScatRec - 1) / kScatRec), Bp / 32), 256, 0, st>>>(
+        Inc, Bp, B, nv, c0, U, lam, dv, lv, mom_row(dv));
     return cudaGetLastError();
 }
 
