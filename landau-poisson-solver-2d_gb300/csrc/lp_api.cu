@@ -173,7 +173,7 @@ template <typename R> lp_status alloc_workspace(lp_ctx *c) {
     LP_TRY(dalloc(c, &Z, 5 * n * nv * nv * Bp));
     c->f = f; c->f1 = f1; c->qn = qn; c->F = F; c->t1 = t1; c->t2 = t2; c->Qc = Qc; c->Y = Y; c->Z = Z;
     for (int i = 0; i < 4; ++i) LP_TRY(dalloc(c, &c->q[i], n3 * Bp));
-    c->nchunk = 64;
+    c->nchunk = 256;  // point chunks of the FP64 moment sums (parallel partials)
     LP_TRY(dalloc(c, &c->cpart, (size_t)c->nchunk * 5 * Bp));
     LP_TRY(dalloc(c, &c->lam, 5 * Bp));
     LP_TRY(dalloc(c, &c->dU, (size_t)T.nv3 * 5 * Bp));
@@ -183,7 +183,7 @@ template <typename R> lp_status alloc_workspace(lp_ctx *c) {
         LP_TRY(dalloc(c, &c->mtpart, (size_t)c->nchunk * 5 * Bp));
         LP_TRY(dalloc(c, &c->mapart, (size_t)c->nrc * 5 * Bp));
         LP_TRY(dalloc(c, &c->mlam, 5 * Bp));
-        LP_TRY(dalloc(c, &c->incpart, (size_t)lp::project_inc_blocks(T.nv) * 5 * Bp));
+        LP_TRY(dalloc(c, &c->incpart, (size_t)lp::project_inc_blocks(T.n, T.nv) * 5 * Bp));
     }
     return LP_OK;
 }
@@ -514,7 +514,7 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp) {
                                    (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0)));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
-    LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.nv, B, Bp, c->gm_inv,
+    LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.n, T.nv, B, Bp, c->gm_inv,
                                   T.prm.dt * kfac, kfac, c->mlam, c->stream, rates_at(c, c0)));
     return LP_OK;
 }

@@ -252,10 +252,89 @@ __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict_
     }
 }
 
+// The same pass for n in {8, 16, 24, 32}: OG threads per (pencil, cell),
+// each holding the pencil's n inputs in registers and forming n / OG of the
+// outputs (in pairs) from M in shared memory (broadcast reads); the pass
+// needs one block barrier (after staging M) instead of one per pencil.
+template <typename R, typename TIn, int OUT, int N, int PY, int OG>
+__global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ in, typename V2<R>::t *__restrict__ out,
+                                                       const R *__restrict__ M, int ax, int Bp, int stage, R dt,
+                                                       R nu, const R *__restrict__ f, R *__restrict__ qn,
+                                                       R *__restrict__ f1, const double *__restrict__ cnu,
+                                                       const double *__restrict__ cdt) {
+    using C = typename V2<R>::t;
+    constexpr int NO = N / OG;  // outputs per thread
+    __shared__ C Ms[N * N];
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < N * N; t += 32 * PY * OG) Ms[t] = mk2<R>(M[2 * t], M[2 * t + 1]);
+    __syncthreads();
+    const int pid = blockIdx.x * PY + threadIdx.y / OG, og = threadIdx.y % OG;
+    if (pid >= N * N) return;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    long long base, stride;
+    if (ax == 2) { base = (long long)pid * N * Bp; stride = Bp; }
+    else if (ax == 1) { const int i0 = pid / N, i2 = pid % N; base = ((long long)i0 * N * N + i2) * Bp; stride = (long long)N * Bp; }
+    else { base = (long long)pid * Bp; stride = (long long)N * N * Bp; }
+    base += c;
+    C x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if constexpr (std::is_same<TIn, double2>::value) x[i] = ld2c<R>(in + base + i * stride);
+        else x[i] = ld2<R>(in + base + i * stride);
+    }
+    R dtc = dt, nuc = nu;
+    if (OUT == 1 && cnu) { nuc = (R)cnu[c]; dtc = (R)cdt[c]; }
+#pragma unroll
+    for (int aa = 0; aa < NO; aa += 2) {
+        const int a = og * NO + aa;
+        R sr0 = R(0), si0 = R(0), sr1 = R(0), si1 = R(0);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const C m0 = Ms[a * N + i], m1 = Ms[(a + 1) * N + i];
+            sr0 += m0.x * x[i].x - m0.y * x[i].y;
+            si0 += m0.x * x[i].y + m0.y * x[i].x;
+            sr1 += m1.x * x[i].x - m1.y * x[i].y;
+            si1 += m1.x * x[i].y + m1.y * x[i].x;
+        }
+        const long long o0 = base + a * stride, o1 = o0 + stride;
+        if constexpr (OUT == 0) {
+            out[o0] = mk2<R>(sr0, si0);
+            out[o1] = mk2<R>(sr1, si1);
+        } else {
+            // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
+            if (stage == 0) {
+                qn[o0] = sr0;
+                f1[o0] = f[o0] + dtc * sr0 * nuc;
+                qn[o1] = sr1;
+                f1[o1] = f[o1] + dtc * sr1 * nuc;
+            } else {
+                f1[o0] = f[o0] + R(0.5) * dtc * qn[o0] * nuc + R(0.5) * dtc * sr0 * nuc;
+                f1[o1] = f[o1] + R(0.5) * dtc * qn[o1] * nuc + R(0.5) * dtc * sr1 * nuc;
+            }
+        }
+    }
+}
+
+template <typename R, typename TIn, int OUT, int N>
+cudaError_t dftp_launch(const TIn *in, typename V2<R>::t *out, const R *M, int ax, int Bp, int stage, double dt,
+                        double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates) {
+    constexpr int PY = 2, OG = 4;
+    dim3 grid((N * N + PY - 1) / PY, Bp / 32), block(32, PY * OG);
+    k_dftp<R, TIn, OUT, N, PY, OG><<<grid, block, 0, st>>>(in, out, M, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1,
+                                                           rates.nu, rates.dt);
+    return cudaGetLastError();
+}
+
 template <typename R, typename TIn, int OUT>
 cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
                      double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{}) {
     using C = typename V2<R>::t;
+    switch (n) {
+    case 8: return dftp_launch<R, TIn, OUT, 8>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    case 16: return dftp_launch<R, TIn, OUT, 16>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    case 24: return dftp_launch<R, TIn, OUT, 24>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    case 32: return dftp_launch<R, TIn, OUT, 32>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    default: break;
+    }
     const size_t smem = sizeof(C) * (size_t)(n * n + 2 * 32 * n);
     dim3 grid((n * n + kDftPencils - 1) / kDftPencils, Bp / 32), block(32, n);
     k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1, rates.nu,
@@ -536,6 +615,7 @@ __global__ void k_cons_partial(const double2 *__restrict__ q, const double *__re
     const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
     const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
     double t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+#pragma unroll 4
     for (int pt = p0 + y; pt < p1; pt += 8) {
         const double2 v = q[(long long)pt * Bp + c];
         t0 += v.x * c1[pt];
@@ -911,10 +991,10 @@ __global__ void k_scatter(const double *__restrict__ dU, long long nrec, long lo
 // cancel), so the increment of the 5 collided coefficients of a record is
 // dt kfac (19/4 tp0 - 15 tp5, 12 tp2, 12 tp3, 12 tp4, 60 tp5 - 15 tp0) and
 // needs no state.  k_proj1_inc writes it cell-minor, Inc[kt][5][Bp], with
-// per-block partial sums of its 5 DG moments (part[blk][5][Bp]);
+// per-block partial sums of its 5 DG moments (part[cell][5][blk]);
 // k_scatter_inc adds increment and moment correction to U through a
 // shared-memory transpose, so both sides of the copy are coalesced.
-constexpr int kIncWarps = 8;
+constexpr int kIncWarps = 4, JBI = 4;
 
 __global__ void __launch_bounds__(32 * kIncWarps)
     k_proj1_inc(const float2 *__restrict__ Z, const float *__restrict__ tf, int n, int nv, int Bp, int B, double dt,
@@ -923,24 +1003,24 @@ __global__ void __launch_bounds__(32 * kIncWarps)
     __shared__ double red[kIncWarps][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c = blockIdx.y * 32 + lane;
-    const int nch = (nv + JB - 1) / JB, W = nv * nv * nch;
+    const int nch = (nv + JBI - 1) / JBI, W = nv * nv * nch;
     const int it = blockIdx.x * kIncWarps + w;
     double m[5] = {0, 0, 0, 0, 0};
     if (it < W && c < B) {
         const int j3 = it % nv, j2 = (it / nv) % nv, ch = it / (nv * nv);
-        const int j0 = ch * JB;
+        const int j0 = ch * JBI;
         const double s = (cdt ? cdt[c] : dt) * kfac;
-        float a[7][JB];
+        float a[7][JBI];
 #pragma unroll
         for (int e = 0; e < 7; ++e)
 #pragma unroll
-            for (int jj = 0; jj < JB; ++jj) a[e][jj] = 0.f;
+            for (int jj = 0; jj < JBI; ++jj) a[e][jj] = 0.f;
         const long long zs = (long long)n * nv * nv * Bp;
         for (int k1 = 0; k1 < n; ++k1) {
             const long long zb = (((long long)k1 * nv + j2) * nv + j3) * Bp + c;
             const float2 z0 = Z[zb], z1 = Z[zb + zs], z2 = Z[zb + 2 * zs], z3 = Z[zb + 3 * zs], z4 = Z[zb + 4 * zs];
 #pragma unroll
-            for (int jj = 0; jj < JB; ++jj) {
+            for (int jj = 0; jj < JBI; ++jj) {
                 if (j0 + jj < nv) {
                     const int j1 = j0 + jj;
                     const float *t0 = tf + 2 * ((0 * n + k1) * nv + j1);
@@ -958,7 +1038,7 @@ __global__ void __launch_bounds__(32 * kIncWarps)
         }
         const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
 #pragma unroll
-        for (int jj = 0; jj < JB; ++jj) {
+        for (int jj = 0; jj < JBI; ++jj) {
             if (j0 + jj >= nv) continue;
             const int j1 = j0 + jj;
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
@@ -983,41 +1063,294 @@ __global__ void __launch_bounds__(32 * kIncWarps)
         for (int q = 0; q < 5; ++q) {
             double t = 0.;
             for (int v = 0; v < kIncWarps; ++v) t += red[v][q][lane];
-            part[((long long)blockIdx.x * 5 + q) * Bp + c] = t;
+            part[((long long)c * 5 + q) * gridDim.x + blockIdx.x] = t;
         }
     }
 }
 
+// The same projection for n in {8, 16, 24, 32}, one thread per (pencil,
+// cell) with the pencil's n inputs in registers and the per-axis factors
+// T0, T1, T2 ([3][n][nv] complex) in shared memory (broadcast reads):
+//   k_pj3  RK4 combination of q0..q3 (FP64 in, FP32 out) and the axis-3 pass,
+//   k_pj2  the axis-2 pass into the five combinations Z0..Z4,
+//   k_pj1  the axis-1 pass into the increments and their moment partials.
+template <int N>
+__global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
+                                             const double2 *__restrict__ q2, const double2 *__restrict__ q3,
+                                             double nu, const double *__restrict__ cnu, const float *__restrict__ tf,
+                                             int nv, int Bp, float2 *__restrict__ Y) {
+    extern __shared__ float2 Ts[];
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < 3 * N * nv; t += 128) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
+    __syncthreads();
+    const int pid = blockIdx.x * 4 + threadIdx.y;  // (k1, k2)
+    if (pid >= N * N) return;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    if (cnu) nu = cnu[c];
+    float2 x[N];
+    const long long b = (long long)pid * N * Bp + c;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const long long o = b + (long long)k * Bp;
+        const double2 a = q0[o], e = q1[o], d = q2[o], g = q3[o];
+        x[k] = make_float2((float)(nu * (0.5 * a.x + (e.x + d.x + g.x) * (1. / 6.))),
+                           (float)(nu * (0.5 * a.y + (e.y + d.y + g.y) * (1. / 6.))));
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < nv; ++j) {
+            const float2 *t = Ts + a * N * nv + j;
+            float sr = 0.f, si = 0.f;
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const float2 m = t[k * nv];
+                sr += m.x * x[k].x - m.y * x[k].y;
+                si += m.x * x[k].y + m.y * x[k].x;
+            }
+            Y[(((long long)a * N * N + pid) * nv + j) * Bp + c] = make_float2(sr, si);
+        }
+}
+
+// Z[p][k1][j2][j3] with (axis-3, axis-2 factor) = (0,0) (0,1) (0,2) (1,0) (2,0)
+template <int N>
+__global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const float *__restrict__ tf, int nv,
+                                             int Bp, float2 *__restrict__ Z) {
+    extern __shared__ float2 Ts[];
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < 3 * N * nv; t += 128) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
+    __syncthreads();
+    const int pid = blockIdx.x * 4 + threadIdx.y;  // (k1, j3)
+    if (pid >= N * nv) return;
+    const int k1 = pid / nv, j3 = pid - k1 * nv;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    const long long ys = (long long)N * N * nv * Bp, zs = (long long)N * nv * nv * Bp;
+    for (int a = 0; a < 3; ++a) {
+        float2 x[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) x[k] = Y[a * ys + (((long long)k1 * N + k) * nv + j3) * Bp + c];
+        const int nf = a == 0 ? 3 : 1;
+        for (int f = 0; f < nf; ++f) {
+            const int p = a == 0 ? f : 2 + a;
+            for (int j = 0; j < nv; ++j) {
+                const float2 *t = Ts + f * N * nv + j;
+                float sr = 0.f, si = 0.f;
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    const float2 m = t[k * nv];
+                    sr += m.x * x[k].x - m.y * x[k].y;
+                    si += m.x * x[k].y + m.y * x[k].x;
+                }
+                Z[p * zs + (((long long)k1 * nv + j) * nv + j3) * Bp + c] = make_float2(sr, si);
+            }
+        }
+    }
+}
+
+// Per (j2, j3, cell): the pencils Z0..Z4 along k1 are staged in shared
+// memory (kPj1Pen pencils x 32 cells per block); the warps split the j1
+// outputs of a pencil.  The 7 real sums of each j1 give
+// the increment (see k_proj1_inc), written cell-minor, and the block's
+// moment partials.
+constexpr int kPj1Warps = 8, kPj1Pen = 1;
+template <int N>
+__global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
+                                                        int nv, int Bp, int B, double dt, double kfac,
+                                                        const double *__restrict__ cdt, double dv, double lv,
+                                                        MomRow mr, double *__restrict__ Inc, double *__restrict__ part) {
+    extern __shared__ float2 Ts[];
+    __shared__ double red[kPj1Warps][5][32];
+    constexpr int nq = kPj1Warps / kPj1Pen;  // j1 groups per pencil
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int t = threadIdx.x; t < 3 * N * nv; t += 32 * kPj1Warps) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
+    float2 *zs_all = Ts + 3 * N * nv;  // [pencil][5 N][32 cells]
+    const int c = blockIdx.y * 32 + lane;
+    const long long zs = (long long)N * nv * nv * Bp;
+    // stage both pencils: rows (pencil, p, k) of 32 cells, coalesced
+    for (int row = w; row < kPj1Pen * 5 * N; row += kPj1Warps) {
+        const int pp = row / (5 * N), rem = row - pp * 5 * N, p = rem / N, k = rem - p * N;
+        const int pid = blockIdx.x * kPj1Pen + pp;
+        float2 v = make_float2(0.f, 0.f);
+        if (pid < nv * nv && c < B) {
+            const int j2 = pid / nv, j3 = pid - j2 * nv;
+            v = Z[p * zs + (((long long)k * nv + j2) * nv + j3) * Bp + c];
+        }
+        zs_all[row * 32 + lane] = v;
+    }
+    __syncthreads();
+    const int pp = w / nq, g = w - pp * nq;
+    const int pid = blockIdx.x * kPj1Pen + pp;
+    double m[5] = {0, 0, 0, 0, 0};
+    if (pid < nv * nv && c < B) {
+        const int j2 = pid / nv, j3 = pid - j2 * nv;
+        const float2 *zc = zs_all + pp * 5 * N * 32 + lane;
+        const double s = (cdt ? cdt[c] : dt) * kfac;
+        const float2 *T0 = Ts, *T1 = Ts + N * nv, *T2 = Ts + 2 * N * nv;
+        const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
+        for (int j1 = g; j1 < nv; j1 += nq) {
+            float a[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+            for (int k = 0; k < N; ++k) {
+                const float2 t0 = T0[k * nv + j1], t1 = T1[k * nv + j1], t2 = T2[k * nv + j1];
+                const float2 z0 = zc[(0 * N + k) * 32], z1 = zc[(1 * N + k) * 32], z2 = zc[(2 * N + k) * 32],
+                             z3 = zc[(3 * N + k) * 32], z4 = zc[(4 * N + k) * 32];
+                a[0] += t0.x * z0.x - t0.y * z0.y;
+                a[1] += t1.x * z0.x - t1.y * z0.y;
+                a[2] += t0.x * z1.x - t0.y * z1.y;
+                a[3] += t0.x * z3.x - t0.y * z3.y;
+                a[4] += t2.x * z0.x - t2.y * z0.y;
+                a[5] += t0.x * z2.x - t0.y * z2.y;
+                a[6] += t0.x * z4.x - t0.y * z4.y;
+            }
+            const long long kt = ((long long)j1 * nv + j2) * nv + j3;
+            const double tp0 = a[0], tp2 = a[1], tp3 = a[2], tp4 = a[3];
+            const double tp5 = (double)a[4] + (double)a[5] + (double)a[6];
+            const double d0 = s * (4.75 * tp0 - 15. * tp5), d4 = s * (60. * tp5 - 15. * tp0);
+            const double d1 = 12. * s * tp2, d2 = 12. * s * tp3, d3 = 12. * s * tp4;
+            double *o = Inc + kt * 5 * Bp + c;
+            o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
+            const double G1 = -lv + (j1 + 0.5) * dv, g2 = G1 * G1 + G2 * G2 + G3 * G3;
+            m[0] += d0 + 0.25 * d4;
+            m[1] += G1 * d0 + mr.dv12 * d1 + 0.25 * G1 * d4;
+            m[2] += G2 * d0 + mr.dv12 * d2 + 0.25 * G2 * d4;
+            m[3] += G3 * d0 + mr.dv12 * d3 + 0.25 * G3 * d4;
+            m[4] += (g2 + mr.dv2q) * d0 + mr.dv6 * (G1 * d1 + G2 * d2 + G3 * d3) + (mr.c19 + 0.25 * g2) * d4;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) red[w][q][lane] = m[q];
+    __syncthreads();
+    if (w == 0 && c < Bp)
+        for (int q = 0; q < 5; ++q) {
+            double t = 0.;
+            for (int v = 0; v < kPj1Warps; ++v) t += red[v][q][lane];
+            part[((long long)c * 5 + q) * gridDim.x + blockIdx.x] = t;
+        }
+}
+
+template <int N>
+cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
+                      const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
+                      double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates) {
+    const size_t ts = sizeof(float2) * 3 * N * nv, zsm = sizeof(float2) * kPj1Pen * 5 * N * 32;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_pj3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj1<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ts + zsm)))) return e;
+    k_pj3<N><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac, nv, Bp, Y);
+    k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
+    k_pj1<N><<<dim3((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32), 32 * kPj1Warps, ts + zsm, st>>>(
+        Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
+    return cudaGetLastError();
+}
+
 constexpr int kScatRec = 32;  // records per tile (x 32 cells)
+constexpr size_t kScatSmem = sizeof(double) * (kScatRec * 5 * 33 + 32 * 5 + 8 * 7 * kScatRec);
 __global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ Inc, int Bp, int B, int nv, int c0,
                                                      double *__restrict__ U, const double *__restrict__ lam,
                                                      double dv, double lv, MomRow mr) {
-    __shared__ double S[kScatRec][5][33];
-    __shared__ double L[32][5];
+    extern __shared__ double ssm[];
+    double(*S)[5][33] = reinterpret_cast<double(*)[5][33]>(ssm);  // [record][coefficient][cell]
+    double(*L)[5] = reinterpret_cast<double(*)[5]>(ssm + kScatRec * 5 * 33);
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const long long nv3 = (long long)nv * nv * nv;
-    const long long kt0 = (long long)blockIdx.x * kScatRec;
+    double *ut = ssm + kScatRec * 5 * 33 + 32 * 5 + w * 7 * kScatRec;  // this warp's records of U
+    const int nv3 = nv * nv * nv;
+    const int kt0 = blockIdx.x * kScatRec;
+    const int nrec = min(kScatRec, nv3 - kt0);
     const int cb = blockIdx.y * 32;
-    // rows (record, coefficient) of 32 cells: coalesced along the cells
-    for (int row = w; row < kScatRec * 5; row += 8) {
-        const int r = row / 5, q = row - r * 5;
-        const long long kt = kt0 + r;
-        S[r][q][lane] = (kt < nv3 && cb + lane < B) ? Inc[(kt * 5 + q) * Bp + cb + lane] : 0.;
+    // rows (record, coefficient) of 32 cells: coalesced along the cells; all
+    // loads of a thread are issued before the first shared-memory store
+    double v[kScatRec * 5 / 8];
+#pragma unroll
+    for (int j = 0; j < kScatRec * 5 / 8; ++j) {
+        const int row = w + 8 * j, r = row / 5, q = row - r * 5;
+        v[j] = (r < nrec && cb + lane < B) ? Inc[((long long)(kt0 + r) * 5 + q) * Bp + cb + lane] : 0.;
+    }
+#pragma unroll
+    for (int j = 0; j < kScatRec * 5 / 8; ++j) {
+        const int row = w + 8 * j, r = row / 5, q = row - r * 5;
+        S[r][q][lane] = v[j];
     }
     if (t < 160) {
         const int cc = t / 5, q = t - cc * 5;
         L[cc][q] = (lam && cb + cc < B) ? lam[5 * (cb + cc) + q] : 0.;
     }
     __syncthreads();
-    // one cell per warp pass, lanes along the records: coalesced on U
-    const long long kt = kt0 + lane;
-    if (kt >= nv3) return;
-    for (int cc = w; cc < 32; cc += 8) {
-        if (cb + cc >= B) break;
-        double a[5] = {S[lane][0][cc], S[lane][1][cc], S[lane][2][cc], S[lane][3][cc], S[lane][4][cc]};
-        if (lam) mom_correct(a, L[cc], dv, lv, nv, kt, mr);
-        double *u = U + 7 * ((long long)(c0 + cb + cc) * nv3 + kt);
-        u[0] += a[0]; u[3] += a[1]; u[4] += a[2]; u[5] += a[3]; u[6] += a[4];
+    const int kt = kt0 + lane, j3 = kt % nv, j2 = (kt / nv) % nv, j1 = kt / (nv * nv);
+    const double G[3] = {-lv + (j1 + 0.5) * dv, -lv + (j2 + 0.5) * dv, -lv + (j3 + 0.5) * dv};
+    const double g2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+    // one cell per warp pass: its nrec records are 7 nrec contiguous doubles of U
+    for (int cc = w; cc < 32 && cb + cc < B; cc += 8) {
+        double *ug = U + 7 * ((long long)(c0 + cb + cc) * nv3 + kt0);
+        if (nrec == kScatRec) {
+            double x[7];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) x[j] = ug[lane + 32 * j];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) ut[lane + 32 * j] = x[j];
+        } else {
+            for (int k = lane; k < 7 * nrec; k += 32) ut[k] = ug[k];
+        }
+        __syncwarp();
+        if (lane < nrec) {
+            double a[5] = {S[lane][0][cc], S[lane][1][cc], S[lane][2][cc], S[lane][3][cc], S[lane][4][cc]};
+            if (lam) {  // Phi^T lambda (mom_correct with the cell centre of this lane's record)
+                const double *l = L[cc];
+                a[0] += l[0] + G[0] * l[1] + G[1] * l[2] + G[2] * l[3] + (g2 + mr.dv2q) * l[4];
+                a[1] += mr.dv12 * l[1] + mr.dv6 * G[0] * l[4];
+                a[2] += mr.dv12 * l[2] + mr.dv6 * G[1] * l[4];
+                a[3] += mr.dv12 * l[3] + mr.dv6 * G[2] * l[4];
+                a[4] += 0.25 * l[0] + 0.25 * (G[0] * l[1] + G[1] * l[2] + G[2] * l[3]) + (mr.c19 + 0.25 * g2) * l[4];
+            }
+            double *u = ut + 7 * lane;
+            u[0] += a[0]; u[3] += a[1]; u[4] += a[2]; u[5] += a[3]; u[6] += a[4];
+        }
+        __syncwarp();
+        if (nrec == kScatRec) {
+#pragma unroll
+            for (int j = 0; j < 7; ++j) ug[lane + 32 * j] = ut[lane + 32 * j];
+        } else {
+            for (int k = lane; k < 7 * nrec; k += 32) ug[k] = ut[k];
+        }
+        __syncwarp();
+    }
+}
+
+// The multipliers of one cell per block from the partials part[c][5][nk]
+// (coalesced) and, when given, the target partials tpart[nchunk][5][Bp].
+__global__ void __launch_bounds__(256) k_lambda_inc(const double *__restrict__ tpart, int nchunk,
+                                                    const double *__restrict__ part, int nk,
+                                                    const double *__restrict__ gm_inv, double scale, double kfac,
+                                                    const double *__restrict__ cdt, int Bp,
+                                                    double *__restrict__ lam) {
+    __shared__ double red[2][5][256];
+    const int c = blockIdx.x, t = threadIdx.x;
+    double tg[5] = {0, 0, 0, 0, 0}, ac[5] = {0, 0, 0, 0, 0};
+    const double *pc = part + (long long)c * 5 * nk;
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+        for (int k = t; k < nk; k += 256) ac[m] += pc[m * nk + k];
+    if (tpart)
+        for (int k = t; k < nchunk; k += 256)
+            for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
+    for (int m = 0; m < 5; ++m) {
+        red[0][m][t] = tg[m];
+        red[1][m][t] = ac[m];
+    }
+    __syncthreads();
+    for (int wd = 128; wd > 0; wd >>= 1) {
+        if (t < wd)
+            for (int m = 0; m < 5; ++m) {
+                red[0][m][t] += red[0][m][t + wd];
+                red[1][m][t] += red[1][m][t + wd];
+            }
+        __syncthreads();
+    }
+    if (t == 0) {
+        if (cdt) scale = cdt[c] * kfac;
+        double r[5];
+        for (int m = 0; m < 5; ++m) r[m] = scale * red[0][m][0] - red[1][m][0];
+        for (int i = 0; i < 5; ++i) {
+            double sum = 0;
+            for (int j = 0; j < 5; ++j) sum += gm_inv[i * 5 + j] * r[j];
+            lam[5 * c + i] = sum;
+        }
     }
 }
 
@@ -1959,35 +2292,48 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
     return cudaGetLastError();
 }
 
-int project_inc_blocks(int nv) { return (nv * nv * ((nv + JB - 1) / JB) + kIncWarps - 1) / kIncWarps; }
+int project_inc_blocks(int n, int nv) {
+    if (n == 8 || n == 16 || n == 24 || n == 32) return (nv * nv + kPj1Pen - 1) / kPj1Pen;  // k_pj1
+    return (nv * nv * ((nv + JBI - 1) / JBI) + kIncWarps - 1) / kIncWarps;
+}
 
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates) {
+    const double kfac = 1. / scalev / scaleL / scale3;
+    switch (n) {
+    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
+    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
+    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
+    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
+    default: break;
+    }
     const long long n3 = (long long)n * n * n;
     k_qcomb<float><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Bp, rates.nu, Qc);
     const int nch = (nv + JB - 1) / JB;
     k_proj3<float><<<grid1((long long)n * n * nch * Bp, 128), 128, 0, st>>>(Qc, tfac, n, nv, Bp, Y);
     k_proj2<float><<<grid1((long long)n * nv * nch * Bp, 128), 128, 0, st>>>(Y, tfac, n, nv, Bp, Z);
-    const double kfac = 1. / scalev / scaleL / scale3;
-    k_proj1_inc<<<dim3(project_inc_blocks(nv), Bp / 32), 32 * kIncWarps, 0, st>>>(
+    k_proj1_inc<<<dim3(project_inc_blocks(n, nv), Bp / 32), 32 * kIncWarps, 0, st>>>(
         Z, tfac, n, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
     return cudaGetLastError();
 }
 
-cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int nv, int B, int Bp,
+cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates) {
-    k_mom_lambda<<<(B + 3) / 4, 128, 0, st>>>(tpart, nchunk, part, project_inc_blocks(nv), 1, 5LL * Bp, Bp, gm_inv,
-                                              scale, kfac, rates.dt, B, Bp, lam);
+    k_lambda_inc<<<B, 256, 0, st>>>(tpart, nchunk, part, project_inc_blocks(n, nv), gm_inv, scale, kfac, rates.dt, Bp,
+                                    lam);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_inc(const double *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
                                double dv, double lv, cudaStream_t st) {
     const long long nv3 = (long long)nv * nv * nv;
-    k_scatter_inc<<<dim3((unsigned)((nv3 + kScatRec - 1) / kScatRec), Bp / 32), 256, 0, st>>>(
+    const cudaError_t e = cudaFuncSetAttribute(k_scatter_inc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kScatSmem);
+    if (e != cudaSuccess) return e;
+    k_scatter_inc<<<dim3((unsigned)((nv3 + kScatRec - 1) / kScatRec), Bp / 32), 256, kScatSmem, st>>>(
         Inc, Bp, B, nv, c0, U, lam, dv, lv, mom_row(dv));
     return cudaGetLastError();
 }

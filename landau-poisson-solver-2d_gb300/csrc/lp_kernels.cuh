@@ -146,12 +146,12 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
 // per-block partial sums of their DG moments, part[blocks][5][Bp]; the
 // multipliers from those partials (tpart as in launch_moment_finish); and
 // U slots {0,3,4,5,6} += increment + moment correction.
-int project_inc_blocks(int nv);
+int project_inc_blocks(int n, int nv);
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{});
-cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int nv, int B, int Bp,
+cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
 cudaError_t launch_scatter_inc(const double *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
