@@ -41,9 +41,10 @@ L2_FLUSH_BYTES = 512 << 20
 # from one ncu capture of
 # `bench.py --steps 2 --warmup 1 --no-cpu-baseline --fp64-steps 0`)
 CONTRACT_TRAFFIC_BYTES = 105.24e6 + 100.49e6
-# the same for the kernels of the convolution form (filled from ncu; None
+# the same for the kernels of the convolution form, per launch, from one
+# `ncu --set full -k regex:"k_fq_y|k_fq_x2"` capture of that command (None
 # where not captured)
-FQ_TRAFFIC_BYTES = {}
+FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x2": 107.26e6 + 147.53e6}
 
 
 def launches_per_step(line_warps):
@@ -432,6 +433,26 @@ def main():
             ctx64 = make("fp64")
             t64 = timed(ctx64, lambda: ctx64.collision_step(), args.fp64_steps, 1)
             t_fp64 = cells * args.fp64_steps / t64
+            # per-step error of full time steps against the FP64 path from the
+            # same initial state, and the conservation drift of the mixed path
+            ref, mix = make("fp64"), make("mixed")
+            mix.set_schedule(*schedule)
+            ref.set_init(1)
+            mix.set_init(1)
+            m0 = mix.moments()
+            errs, drift = [], []
+            for _ in range(args.fp64_steps):
+                ref.step(1)
+                mix.step(1)
+                Ur, Um = ref.get_state(), mix.get_state()
+                errs.append(float(np.linalg.norm(Um - Ur) / np.linalg.norm(Ur)))
+                m1 = mix.moments()
+                drift.append(float(abs(m1[0] - m0[0]) / abs(m0[0])))
+            extra["rel_err_vs_fp64_per_step"] = errs
+            extra["mass_drift_per_step"] = drift
+            extra["finite"] = bool(np.isfinite(Um).all())
+            ref.close()
+            mix.close()
             ctx64.close()
         extra["fp64_value"] = t_fp64
         extra["mixed_over_fp64"] = (value / ws / t_fp64) if t_fp64 else None
