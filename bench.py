@@ -313,6 +313,10 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="landau64", choices=["landau64", "batch", "twostream"])
+    ap.add_argument("--schedule", default=None,
+                    help="cells_per_pass,line_warps for the collision (skips the autotuner)")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only run this many collision steps of the workload (for ncu launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -361,7 +365,20 @@ def main():
     ctx = make(args.precision)
     cells = WORKLOAD["nx1"] * WORKLOAD["nx2"]
     # the library's autotuner picks the collision schedule (outside the timed region)
-    schedule = ctx.autotune(reps=2)
+    if args.schedule:
+        schedule = tuple(int(x) for x in args.schedule.split(","))
+        ctx.set_schedule(*schedule)
+    else:
+        schedule = ctx.autotune(reps=2)
+    if args.profile_steps > 0:
+        with torch.cuda.stream(stream):
+            for _ in range(args.profile_steps):
+                ctx.collision_step()
+            torch.cuda.synchronize()
+        U = ctx.get_state()
+        print(json.dumps({"profile_steps": args.profile_steps, "schedule": schedule,
+                          "finite": bool(np.isfinite(U).all())}), flush=True)
+        return 0
     with ClockSampler(local) as clk:
         t = timed(ctx, lambda: ctx.collision_step(), args.steps, args.warmup)
     t_max = t
