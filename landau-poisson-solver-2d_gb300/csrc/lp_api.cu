@@ -78,6 +78,11 @@ struct lp_ctx {
     // moment reconciliation (mixed path)
     double *gmom = nullptr, *gm_inv = nullptr, *mtpart = nullptr, *mapart = nullptr, *mlam = nullptr;
     double *incpart = nullptr;  // per-block DG moment partials of the fused projection
+    // lazy conservation of the mixed one-species path: the nonzero constraint
+    // rows in FP32 (C1[0], C2[1..3], C1[4]) and the multipliers of the four
+    // stages, lam4[4][5][Bcap]
+    float *cf = nullptr;
+    double *lam4 = nullptr;
     int nrc = 16;
     // adjoint workspace (FP64 contexts, allocated by the first adjoint call)
     struct Adj {
@@ -184,6 +189,16 @@ template <typename R> lp_status alloc_workspace(lp_ctx *c) {
         LP_TRY(dalloc(c, &c->mapart, (size_t)c->nrc * 5 * Bp));
         LP_TRY(dalloc(c, &c->mlam, 5 * Bp));
         LP_TRY(dalloc(c, &c->incpart, (size_t)lp::project_inc_blocks(T.n, T.nv) * 5 * Bp));
+        if (lp::fftq_supported(T.n)) {
+            std::vector<float> cf(5 * n3);
+            for (size_t k = 0; k < n3; ++k) {
+                cf[k] = (float)T.c1[k];
+                for (int r = 1; r < 4; ++r) cf[r * n3 + k] = (float)T.c2[r * n3 + k];
+                cf[4 * n3 + k] = (float)T.c1[4 * n3 + k];
+            }
+            LP_TRY(upload(c, &c->cf, cf.data(), cf.size()));
+            LP_TRY(dalloc(c, &c->lam4, 4 * 5 * Bp));
+        }
     }
     return LP_OK;
 }
@@ -413,7 +428,9 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
 // ComputeQ's contraction and conserveAllMoments; in the two-species variant
 // the linear term is added before, conserved with its own two constraints,
 // and added again after (C:551-635, K:63-98, C:656-698).
-template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q) {
+// slot >= 0 (lazy conservation): only the multipliers of stage `slot` are
+// computed, into lam4; the consumers of q apply the correction on load.
+template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q, int slot = -1) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     LP_TRY(contract<R>(c, Bp, q));
@@ -427,6 +444,11 @@ template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q) {
         LP_CUDA(lp::launch_qadd(q, c->qlin, tot, c->stream));
         return LP_OK;
     }
+    if (slot >= 0) {
+        LP_CUDA(lp::launch_conserve(q, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam4 + slot * 5 * Bp,
+                                    c->stream, false));
+        return LP_OK;
+    }
     LP_CUDA(lp::launch_conserve(q, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
     return LP_OK;
 }
@@ -438,15 +460,18 @@ lp::Rates rates_at(const lp_ctx *c, int c0) {
     return r;
 }
 
-template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp) {
+// lazy: the stages' conservation corrections are applied by the consumers
+// (the next FS pass and the first DG projection pass).
+template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp, bool lazy = false) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     const R *M = (const R *)c->mfwd, *Mi = (const R *)c->minv;
     for (int s = 0; s < 3; ++s) {
         LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
-                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0)));
+                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0),
+                                       lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr));
         LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
-        LP_TRY(stage_q<R>(c, Bp, c->q[s + 1]));
+        LP_TRY(stage_q<R>(c, Bp, c->q[s + 1], lazy ? s + 1 : -1));
     }
     return LP_OK;
 }
@@ -496,7 +521,11 @@ template <typename R> lp_status project(lp_ctx *c, int c0, int B, int Bp, bool d
 // multipliers of the moment correction follow; the scatter adds both to U.
 bool fused_tail(const lp_ctx *c) { return c->mixed && (c->T.prm.fixes & LP_FIX_F1); }
 
-lp_status project_fused(lp_ctx *c, int c0, int B, int Bp) {
+// Lazy conservation: the one-species mixed path with the fused tail and the
+// register-pencil kernels (the two-species operator keeps its add-conserve-add order).
+bool lazy_cons(const lp_ctx *c) { return fused_tail(c) && !c->WLin && c->cf; }
+
+lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false) {
     const lp::Tables &T = c->T;
     const bool target = c->WLin != nullptr;
     cudaStream_t tst = (target && c->side) ? c->side : c->stream;
@@ -511,7 +540,8 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp) {
     }
     LP_CUDA(lp::launch_project_inc(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const float *)c->tfac, T.n, T.nv,
                                    Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
-                                   (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0)));
+                                   (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
+                                   lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
     LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.n, T.nv, B, Bp, c->gm_inv,
@@ -528,9 +558,10 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
-    LP_TRY(stage_q<R>(c, Bp, c->q[0]));
-    LP_TRY(rk4_stages<R>(c, c0, Bp));
-    if (fused_tail(c)) return project_fused(c, c0, B, Bp);
+    const bool lazy = lazy_cons(c);
+    LP_TRY(stage_q<R>(c, Bp, c->q[0], lazy ? 0 : -1));
+    LP_TRY(rk4_stages<R>(c, c0, Bp, lazy));
+    if (fused_tail(c)) return project_fused(c, c0, B, Bp, lazy);
     LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
 }

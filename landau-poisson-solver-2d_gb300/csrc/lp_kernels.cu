@@ -256,12 +256,16 @@ __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict_
 // each holding the pencil's n inputs in registers and forming n / OG of the
 // outputs (in pairs) from M in shared memory (broadcast reads); the pass
 // needs one block barrier (after staging M) instead of one per pencil.
+// cf/lamc (pencils along the last axis only): the input is a mode array whose
+// conservation projection was not applied; x -= C^T lambda is applied on load
+// in R precision (cf: the 5 nonzero constraint rows, lamc: [5][Bp]).
 template <typename R, typename TIn, int OUT, int N, int PY, int OG>
 __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ in, typename V2<R>::t *__restrict__ out,
                                                        const R *__restrict__ M, int ax, int Bp, int stage, R dt,
                                                        R nu, const R *__restrict__ f, R *__restrict__ qn,
                                                        R *__restrict__ f1, const double *__restrict__ cnu,
-                                                       const double *__restrict__ cdt) {
+                                                       const double *__restrict__ cdt, const float *__restrict__ cf,
+                                                       const double *__restrict__ lamc) {
     using C = typename V2<R>::t;
     constexpr int NO = N / OG;  // outputs per thread
     __shared__ C Ms[N * N];
@@ -280,6 +284,17 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
     for (int i = 0; i < N; ++i) {
         if constexpr (std::is_same<TIn, double2>::value) x[i] = ld2c<R>(in + base + i * stride);
         else x[i] = ld2<R>(in + base + i * stride);
+    }
+    if (cf) {
+        constexpr int n3 = N * N * N;
+        const R l0 = (R)lamc[c], l1 = (R)lamc[Bp + c], l2 = (R)lamc[2 * Bp + c], l3 = (R)lamc[3 * Bp + c],
+                l4 = (R)lamc[4 * Bp + c];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const int pt = pid * N + i;
+            x[i].x -= (R)cf[pt] * l0 + (R)cf[4 * n3 + pt] * l4;
+            x[i].y -= (R)cf[n3 + pt] * l1 + (R)cf[2 * n3 + pt] * l2 + (R)cf[3 * n3 + pt] * l3;
+        }
     }
     R dtc = dt, nuc = nu;
     if (OUT == 1 && cnu) { nuc = (R)cnu[c]; dtc = (R)cdt[c]; }
@@ -316,25 +331,29 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
 
 template <typename R, typename TIn, int OUT, int N>
 cudaError_t dftp_launch(const TIn *in, typename V2<R>::t *out, const R *M, int ax, int Bp, int stage, double dt,
-                        double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates) {
+                        double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates,
+                        const float *cf = nullptr, const double *lamc = nullptr) {
     constexpr int PY = 2, OG = 4;
+    if (cf && ax != 2) return cudaErrorInvalidValue;
     dim3 grid((N * N + PY - 1) / PY, Bp / 32), block(32, PY * OG);
     k_dftp<R, TIn, OUT, N, PY, OG><<<grid, block, 0, st>>>(in, out, M, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1,
-                                                           rates.nu, rates.dt);
+                                                           rates.nu, rates.dt, cf, lamc);
     return cudaGetLastError();
 }
 
 template <typename R, typename TIn, int OUT>
 cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
-                     double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{}) {
+                     double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{},
+                     const float *cf = nullptr, const double *lamc = nullptr) {
     using C = typename V2<R>::t;
     switch (n) {
-    case 8: return dftp_launch<R, TIn, OUT, 8>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
-    case 16: return dftp_launch<R, TIn, OUT, 16>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
-    case 24: return dftp_launch<R, TIn, OUT, 24>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
-    case 32: return dftp_launch<R, TIn, OUT, 32>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    case 8: return dftp_launch<R, TIn, OUT, 8>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+    case 16: return dftp_launch<R, TIn, OUT, 16>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+    case 24: return dftp_launch<R, TIn, OUT, 24>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+    case 32: return dftp_launch<R, TIn, OUT, 32>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
     default: break;
     }
+    if (cf) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil pass
     const size_t smem = sizeof(C) * (size_t)(n * n + 2 * 32 * n);
     dim3 grid((n * n + kDftPencils - 1) / kDftPencils, Bp / 32), block(32, n);
     k_dft<R, TIn, OUT><<<grid, block, smem, st>>>(in, out, M, n, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1, rates.nu,
@@ -1074,11 +1093,15 @@ __global__ void __launch_bounds__(32 * kIncWarps)
 //   k_pj3  RK4 combination of q0..q3 (FP64 in, FP32 out) and the axis-3 pass,
 //   k_pj2  the axis-2 pass into the five combinations Z0..Z4,
 //   k_pj1  the axis-1 pass into the increments and their moment partials.
+// cf/lam4: the q_s were not projected by conserveAllMoments; each gets its
+// correction q_s -= C^T lambda_s (lam4[s][5][Bp]) in FP32 on load, and the
+// combination is formed in FP32.
 template <int N>
 __global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
                                              const double2 *__restrict__ q2, const double2 *__restrict__ q3,
                                              double nu, const double *__restrict__ cnu, const float *__restrict__ tf,
-                                             int nv, int Bp, float2 *__restrict__ Y) {
+                                             int nv, int Bp, float2 *__restrict__ Y, const float *__restrict__ cf,
+                                             const double *__restrict__ lam4) {
     extern __shared__ float2 Ts[];
     for (int t = threadIdx.y * 32 + threadIdx.x; t < 3 * N * nv; t += 128) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
     __syncthreads();
@@ -1088,12 +1111,37 @@ __global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, con
     if (cnu) nu = cnu[c];
     float2 x[N];
     const long long b = (long long)pid * N * Bp + c;
+    if (cf) {
+        constexpr int n3 = N * N * N;
+        float l[4][5];
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const long long o = b + (long long)k * Bp;
-        const double2 a = q0[o], e = q1[o], d = q2[o], g = q3[o];
-        x[k] = make_float2((float)(nu * (0.5 * a.x + (e.x + d.x + g.x) * (1. / 6.))),
-                           (float)(nu * (0.5 * a.y + (e.y + d.y + g.y) * (1. / 6.))));
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+            for (int j = 0; j < 5; ++j) l[s][j] = (float)lam4[(s * 5 + j) * Bp + c];
+        const float nuf = (float)nu;
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const long long o = b + (long long)k * Bp;
+            const int pt = pid * N + k;
+            const float r0 = cf[pt], r1 = cf[n3 + pt], r2 = cf[2 * n3 + pt], r3 = cf[3 * n3 + pt], r4 = cf[4 * n3 + pt];
+            const double2 qs[4] = {q0[o], q1[o], q2[o], q3[o]};
+            float2 v[4];
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                v[s].x = (float)qs[s].x - (r0 * l[s][0] + r4 * l[s][4]);
+                v[s].y = (float)qs[s].y - (r1 * l[s][1] + r2 * l[s][2] + r3 * l[s][3]);
+            }
+            x[k] = make_float2(nuf * (0.5f * v[0].x + (v[1].x + v[2].x + v[3].x) * (1.f / 6.f)),
+                               nuf * (0.5f * v[0].y + (v[1].y + v[2].y + v[3].y) * (1.f / 6.f)));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const long long o = b + (long long)k * Bp;
+            const double2 a = q0[o], e = q1[o], d = q2[o], g = q3[o];
+            x[k] = make_float2((float)(nu * (0.5 * a.x + (e.x + d.x + g.x) * (1. / 6.))),
+                               (float)(nu * (0.5 * a.y + (e.y + d.y + g.y) * (1. / 6.))));
+        }
     }
     for (int a = 0; a < 3; ++a)
         for (int j = 0; j < nv; ++j) {
@@ -1227,13 +1275,15 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
 template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
-                      double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates) {
+                      double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
+                      const float *cf, const double *lam4) {
     const size_t ts = sizeof(float2) * 3 * N * nv, zsm = sizeof(float2) * kPj1Pen * 5 * N * 32;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_pj3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj1<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ts + zsm)))) return e;
-    k_pj3<N><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac, nv, Bp, Y);
+    k_pj3<N><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac, nv, Bp, Y,
+                                                                       cf, lam4);
     k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
     k_pj1<N><<<dim3((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32), 32 * kPj1Warps, ts + zsm, st>>>(
         Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
@@ -2128,10 +2178,11 @@ cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t
 template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2, const R *M, int n,
                             int Bp, int stage, double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st,
-                            Rates rates) {
+                            Rates rates, const float *cf, const double *lamc) {
     using C = typename V2<R>::t;
     cudaError_t e;
-    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf, lamc)))
+        return e;
     if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
     return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
 }
@@ -2245,10 +2296,10 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
 }
 
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
-                            double *part, int nchunk, double *lam, cudaStream_t st) {
+                            double *part, int nchunk, double *lam, cudaStream_t st, bool apply) {
     k_cons_partial<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
     k_cons_lambda<<<(Bp + 3) / 4, 128, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
-    k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
+    if (apply) k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
     return cudaGetLastError();
 }
 
@@ -2300,15 +2351,17 @@ int project_inc_blocks(int n, int nv) {
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
-                               double *part, double lv, double dv, cudaStream_t st, Rates rates) {
+                               double *part, double lv, double dv, cudaStream_t st, Rates rates, const float *cf,
+                               const double *lam4) {
     const double kfac = 1. / scalev / scaleL / scale3;
     switch (n) {
-    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
-    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
-    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
-    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates);
+    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
+    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
+    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
+    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
     default: break;
     }
+    if (cf) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil passes
     const long long n3 = (long long)n * n * n;
     k_qcomb<float><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Bp, rates.nu, Qc);
     const int nch = (nv + JB - 1) / JB;
@@ -2443,7 +2496,8 @@ cudaError_t launch_moments(const double *U, long long size, long long kend, int 
     template cudaError_t launch_fwd_complex<R>(const V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, int,   \
                                                cudaStream_t);                                                   \
     template cudaError_t launch_fs_stage<R>(const double2 *, V2<R>::t *, V2<R>::t *, const R *, int, int, int,  \
-                                            double, double, const R *, R *, R *, cudaStream_t, Rates);          \
+                                            double, double, const R *, R *, R *, cudaStream_t, Rates,           \
+                                            const float *, const double *);                                     \
     template cudaError_t launch_fs_full<R>(const double2 *, V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, \
                                            int, cudaStream_t);                                                  \
     template cudaError_t launch_computeq<R>(const V2<R>::t *, const R *, const unsigned *, const int *, int,    \

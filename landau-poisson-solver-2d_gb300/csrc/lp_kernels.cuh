@@ -45,10 +45,14 @@ struct Rates {
 // Inverse transform FS of q (FP64 complex), real part only, fused with the
 // RK4 stage update of the node values: stage 0 stores Q = Re FS(q) in qn and
 // writes f1 = f + dt Q nu; stages 1, 2 write f1 = f + dt/2 Q nu + dt/2 Re FS(q) nu.
+// cf/lamc (n in {8, 16, 24, 32}): q has not been projected by
+// conserveAllMoments; q -= C^T lambda is applied in R precision on load (cf:
+// the nonzero constraint rows C1[0], C2[1..3], C1[4] as FP32, lamc: [5][Bp]).
 template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
                             const R *M, int n, int Bp, int stage, double dt, double nu,
-                            const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{});
+                            const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{},
+                            const float *cf = nullptr, const double *lamc = nullptr);
 
 // Inverse transform FS of q, full complex output (for the reference-shaped FS).
 template <typename R>
@@ -113,9 +117,11 @@ cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw
                                 float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1);
 
 // Moment-conserving projection of q in place (FP64).
+// apply = false: only the multipliers lam[5][Bp] (the correction is left to
+// the consumers of q).
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
                             int n3, int Bp, double *part, int nchunk, double *lam,
-                            cudaStream_t st);
+                            cudaStream_t st, bool apply = true);
 
 // Final RK4 combination, DG projection and mass-matrix inverse: writes
 // dU[B][nv^3][5] for cells [c0, c0+B).  Qc, Y, Z are scratch.
@@ -147,10 +153,13 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
 // multipliers from those partials (tpart as in launch_moment_finish); and
 // U slots {0,3,4,5,6} += increment + moment correction.
 int project_inc_blocks(int n, int nv);
+// cf/lam4 (n in {8, 16, 24, 32}): the q_s were not projected; their
+// corrections with lam4[s][5][Bp] are applied in FP32 on load.
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
-                               double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{});
+                               double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{},
+                               const float *cf = nullptr, const double *lam4 = nullptr);
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
