@@ -1198,7 +1198,7 @@ __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const
 // moment partials.
 constexpr int kPj1Warps = 8, kPj1Pen = 1;
 template <int N>
-__global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
+__global__ void __launch_bounds__(32 * kPj1Warps, 2) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
                                                         int nv, int Bp, int B, double dt, double kfac,
                                                         const double *__restrict__ cdt, double dv, double lv,
                                                         MomRow mr, double *__restrict__ Inc, double *__restrict__ part) {
@@ -1228,9 +1228,12 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
     if (pid < nv * nv && c < B) {
         const int j2 = pid / nv, j3 = pid - j2 * nv;
         const float2 *zc = zs_all + pp * 5 * N * 32 + lane;
-        const double s = (cdt ? cdt[c] : dt) * kfac;
+        const float sf = (float)((cdt ? cdt[c] : dt) * kfac);
         const float2 *T0 = Ts, *T1 = Ts + N * nv, *T2 = Ts + 2 * N * nv;
         const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
+        // running sums over this thread's j1 of d_q, G1 d_0, G1 d_4, G1 d_1,
+        // G1^2 d_0, G1^2 d_4; the moments follow from them with G2, G3
+        double S[5] = {0, 0, 0, 0, 0}, A0 = 0, A4 = 0, A1 = 0, B0 = 0, B4 = 0;
         for (int j1 = g; j1 < nv; j1 += nq) {
             float a[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
@@ -1246,20 +1249,26 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
                 a[5] += t0.x * z2.x - t0.y * z2.y;
                 a[6] += t0.x * z4.x - t0.y * z4.y;
             }
+            // the increment in FP32 (its inputs are FP32 sums), stored and
+            // summed in FP64
+            const float tp5 = a[4] + a[5] + a[6];
+            const double d0 = sf * (4.75f * a[0] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0]);
+            const double d1 = 12.f * sf * a[1], d2 = 12.f * sf * a[2], d3 = 12.f * sf * a[3];
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
-            const double tp0 = a[0], tp2 = a[1], tp3 = a[2], tp4 = a[3];
-            const double tp5 = (double)a[4] + (double)a[5] + (double)a[6];
-            const double d0 = s * (4.75 * tp0 - 15. * tp5), d4 = s * (60. * tp5 - 15. * tp0);
-            const double d1 = 12. * s * tp2, d2 = 12. * s * tp3, d3 = 12. * s * tp4;
             double *o = Inc + kt * 5 * Bp + c;
             o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
-            const double G1 = -lv + (j1 + 0.5) * dv, g2 = G1 * G1 + G2 * G2 + G3 * G3;
-            m[0] += d0 + 0.25 * d4;
-            m[1] += G1 * d0 + mr.dv12 * d1 + 0.25 * G1 * d4;
-            m[2] += G2 * d0 + mr.dv12 * d2 + 0.25 * G2 * d4;
-            m[3] += G3 * d0 + mr.dv12 * d3 + 0.25 * G3 * d4;
-            m[4] += (g2 + mr.dv2q) * d0 + mr.dv6 * (G1 * d1 + G2 * d2 + G3 * d3) + (mr.c19 + 0.25 * g2) * d4;
+            const double G1 = -lv + (j1 + 0.5) * dv, G11 = G1 * G1;
+            S[0] += d0; S[1] += d1; S[2] += d2; S[3] += d3; S[4] += d4;
+            A0 += G1 * d0; A4 += G1 * d4; A1 += G1 * d1;
+            B0 += G11 * d0; B4 += G11 * d4;
         }
+        const double S04 = S[0] + 0.25 * S[4], G2233 = G2 * G2 + G3 * G3;
+        m[0] = S04;
+        m[1] = A0 + mr.dv12 * S[1] + 0.25 * A4;
+        m[2] = G2 * S04 + mr.dv12 * S[2];
+        m[3] = G3 * S04 + mr.dv12 * S[3];
+        m[4] = B0 + (G2233 + mr.dv2q) * S[0] + mr.dv6 * (A1 + G2 * S[2] + G3 * S[3]) + mr.c19 * S[4] + 0.25 * B4 +
+               0.25 * G2233 * S[4];
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) red[w][q][lane] = m[q];
