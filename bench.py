@@ -49,11 +49,11 @@ FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x2": 107.26e6 + 147.53e6}
 
 def launches_per_step(line_warps):
     """Kernels of one mixed collision step at n = 24 (64 cells, one pass):
-    nodes 1, forward transform 3 x 4, contraction x 4 (5 kernels in the
-    convolution form, 2 k-tiles in the line-tiled form), conservation 3 x 4,
-    inverse transform 3 x 3, DG projection 4, moment reconciliation 2 (its
-    target is zero; the correction rides on the scatter), scatter 1."""
-    return 1 + 12 + 4 * (5 if line_warps == 0 else 2) + 12 + 9 + 4 + 2 + 1
+    nodes 1, forward transform 3 x 4, contraction x 4 (4 kernels in the
+    convolution form at n <= 24, 2 k-tiles in the line-tiled form),
+    conservation 2 x 4 (its correction is applied by the next kernels),
+    inverse transform 3 x 3, DG projection 3, multipliers 1, scatter 1."""
+    return 1 + 12 + 4 * (4 if line_warps == 0 else 2) + 8 + 9 + 3 + 1 + 1
 
 
 def fq_kernel_model(n, cells):
@@ -65,13 +65,22 @@ def fq_kernel_model(n, cells):
     t3, x, g, hh = 10 * n * n * M, 13 * n * M * M, n * M * M, n * n * M
     # valid (i, l) pairs of the direct axis-1 sum: 0 <= i + h - l < n
     pairs = sum(1 for i in range(n) for l in range(n) if 0 <= i + h - l < n)
-    return {
+    model = {
         "k_fq_x1": (n ** 3 * c8 + 7 * n ** 3 * 4 + t3 * c8, None),
         "k_fq_x2": (t3 * c8 + x * c8, None),
+        # n <= 24: X1 and X2 fused, the X1 outputs stay in shared memory
+        "k_fq_x12": (n ** 3 * c8 + 7 * n ** 3 * 4 + x * c8, None),
         "k_fq_y": (x * c8 + g * c8, 7 * pairs * 8.0 * M * M * cells),
         "k_fq_z1": (g * c8 + hh * c8, None),
         "k_fq_z2": (hh * c8 + n ** 3 * 16 * cells, None),
     }
+    return model
+
+
+def fq_kernels(n):
+    """(name, lp_time_kernel code) of the convolution form's kernels."""
+    first = [("k_fq_x12", 4)] if n <= 24 else [("k_fq_x1", 4), ("k_fq_x2", 5)]
+    return first + [("k_fq_y", 6), ("k_fq_z1", 7), ("k_fq_z2", 8)]
 
 
 def _config(extra=None):
@@ -419,9 +428,9 @@ def main():
         t_contract_ms = ctx.time_kernel(0, reps=max(5, args.steps))
         fq_ms = {}
         if schedule[1] == 0:
-            for i, name in enumerate(["k_fq_x1", "k_fq_x2", "k_fq_y", "k_fq_z1", "k_fq_z2"]):
+            for name, code in fq_kernels(WORKLOAD["n"]):
                 flush.zero_()
-                fq_ms[name] = ctx.time_kernel(4 + i, reps=max(5, args.steps))
+                fq_ms[name] = ctx.time_kernel(code, reps=max(5, args.steps))
     n = WORKLOAD["n"]
     h = n // 2
     win = [i + h + 1 if i < h else 3 * h - 1 - i for i in range(n)]
@@ -495,7 +504,7 @@ def main():
             roof = {"bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s", "frac": hbm_frac,
                     "traffic": FQ_TRAFFIC_BYTES.get(dom["kernel"]),
                     "algorithmic_bytes": dom["algorithmic_bytes"], "peak_kind": peak_kind,
-                    "kernel": dom["kernel"] + " (the largest of the five kernels of the convolution form)",
+                    "kernel": dom["kernel"] + " (the largest kernel of the convolution form)",
                     "ms_per_launch": dom["ms_per_launch"]}
             comp = {"pipe": "fp32 FMA (packed f32x2, CUDA cores)", "kernel": dom["kernel"],
                     "achieved_tflops": dom["tflops"], "peak_tflops": fp32_peak,

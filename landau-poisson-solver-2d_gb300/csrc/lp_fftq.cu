@@ -169,6 +169,34 @@ template <int N, bool PHASE> __device__ __forceinline__ void fwd_pencil(const fl
     }
 }
 
+// The same transform handing each output to st(k, value) as soon as it is
+// formed (the outputs need no registers of their own).
+template <int N, bool PHASE, typename Store>
+__device__ __forceinline__ void fwd_pencil_st(const float2 (&x)[N], const float2 *tw, Store st) {
+    constexpr int S = N / 4;
+    float2 Y[S][6];
+#pragma unroll
+    for (int q2 = 0; q2 < S; ++q2) {
+        const float2 in[6] = {x[q2], x[S + q2], x[2 * S + q2], x[3 * S + q2], make_float2(0.f, 0.f),
+                              make_float2(0.f, 0.f)};
+        dft6<false, 4, 6>(in, Y[q2]);
+    }
+#pragma unroll
+    for (int q2 = 0; q2 < S; ++q2)
+#pragma unroll
+        for (int k1 = 1; k1 < 6; ++k1)
+            if (PHASE || q2 > 0) Y[q2][k1] = cmul(Y[q2][k1], tw[q2 * 6 + k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < 6; ++k1) {
+        float2 col[S];
+#pragma unroll
+        for (int q2 = 0; q2 < S; ++q2) col[q2] = Y[q2][k1];
+        dftS<S, false>(col);
+#pragma unroll
+        for (int k2 = 0; k2 < S; ++k2) st(k1 + 6 * k2, col[k2]);
+    }
+}
+
 // Inverse: x[s] = sum_k G[k] exp(2 pi i k s / M) / M for s in [0, n), the
 // conjugate transpose of fwd_pencil without the phase; iv holds
 // conj(tw[q2][k1]) / M.
@@ -214,21 +242,20 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_x1(const float2 *__restrict__ F
     if (pen >= n * n) return;
     const int cell = blockIdx.y * 32 + threadIdx.x, arr = blockIdx.z;
     const float2 *src = F + (size_t)pen * n * Bp + c0 + cell;
-    float2 x[N], X[M];
+    float2 x[N];
+    float2 *dst = T3 + ((size_t)arr * n * n + pen) * M * Bs + cell;
+    auto put = [&](int k, float2 v) { dst[(size_t)k * Bs] = v; };
     if (arr < 7) {
         const float *cp = C + (size_t)arr * n * n * n + (size_t)pen * n;
 #pragma unroll
         for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], __ldg(cp + q));
-        fwd_pencil<N, true>(x, X, tw.fa);
+        fwd_pencil_st<N, true>(x, tw.fa, put);
     } else {
         const int e = arr - 7;
 #pragma unroll
         for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], poww(q, h, e));
-        fwd_pencil<N, false>(x, X, tw.fw);
+        fwd_pencil_st<N, false>(x, tw.fw, put);
     }
-    float2 *dst = T3 + ((size_t)arr * n * n + pen) * M * Bs + cell;
-#pragma unroll
-    for (int k = 0; k < M; ++k) dst[(size_t)k * Bs] = X[k];
 }
 
 // X2: axis-2 DFT of the (l, k3) pencils.  Arrays 0..6 the a-side; 7..12
@@ -249,21 +276,80 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_x2(const float2 *__restrict__ T
         e2 = (j == 1) ? 2 : ((j == 3 || j == 5) ? 1 : 0);
     }
     const float2 *src = T3 + (((size_t)sa * n + l) * n * M + k3) * Bs + cell;
-    float2 x[N], Xo[M];
+    float2 x[N];
 #pragma unroll
     for (int m = 0; m < n; ++m) x[m] = src[(size_t)m * M * Bs];
+    float2 *dst = X + (((size_t)arr * n + l) * M * M + k3) * Bs + cell;
+    auto put = [&](int k, float2 v) { dst[(size_t)k * M * Bs] = v; };
     if (arr < 7) {
-        fwd_pencil<N, true>(x, Xo, tw.fa);
+        fwd_pencil_st<N, true>(x, tw.fa, put);
     } else {
         if (e2) {
 #pragma unroll
             for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2));
         }
-        fwd_pencil<N, false>(x, Xo, tw.fw);
+        fwd_pencil_st<N, false>(x, tw.fw, put);
     }
-    float2 *dst = X + (((size_t)arr * n + l) * M * M + k3) * Bs + cell;
+}
+
+// X1 and X2 fused per (axis-1 plane l, 16 cells, X1 array t = blockIdx.z):
+// the plane's axis-3 DFTs go to shared memory ([m][k3][16 cells]) and the
+// axis-2 DFTs read them from there, so the X1 outputs never reach DRAM.
+// blockDim = (16 cells, PY threads), each thread taking pencils ty,
+// ty + PY, ... of both phases.
+template <int N, int PY>
+__global__ void __launch_bounds__(16 * PY) k_fq_x12(const float2 *__restrict__ F, const float *__restrict__ C,
+                                                    int Bp, int c0, float2 *__restrict__ X, int Bs, FftTw tw) {
+    constexpr int n = N, h = N / 2, M = 3 * N / 2;
+    extern __shared__ float2 t3[];  // [m][k3][16]
+    const int tx = threadIdx.x, ty = threadIdx.y, l = blockIdx.x, t = blockIdx.z;
+    const int cell = blockIdx.y * 16 + tx;
+    const size_t as = (size_t)n * M * M * Bs, os = (size_t)M * Bs;  // array and k2 strides of X
+    {
+        // axis-3 DFTs of the (l, m) pencils of array t
+        for (int m = ty; m < n; m += PY) {
+            const float2 *src = F + ((size_t)l * n + m) * n * Bp + c0 + cell;
+            float2 x[N];
+            float2 *row = t3 + m * M * 16 + tx;
+            auto put = [&](int k, float2 v) { row[k * 16] = v; };
+            if (t < 7) {
+                const float *cp = C + (size_t)t * n * n * n + ((size_t)l * n + m) * n;
 #pragma unroll
-    for (int k = 0; k < M; ++k) dst[(size_t)k * M * Bs] = Xo[k];
+                for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], __ldg(cp + q));
+                fwd_pencil_st<N, true>(x, tw.fa, put);
+            } else {
+#pragma unroll
+                for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], poww(q, h, t - 7));
+                fwd_pencil_st<N, false>(x, tw.fw, put);
+            }
+        }
+        __syncthreads();
+        // axis-2 DFTs of the (l, k3) pencils into X
+        for (int k3 = ty; k3 < M; k3 += PY) {
+            float2 x[N];
+#pragma unroll
+            for (int m = 0; m < n; ++m) x[m] = t3[(m * M + k3) * 16 + tx];
+            float2 *dst = X + ((size_t)l * M * M + k3) * Bs + cell;
+            if (t < 7) {
+                float2 *d = dst + t * as;
+                fwd_pencil_st<N, true>(x, tw.fa, [&](int k, float2 v) { d[(size_t)k * os] = v; });
+            } else {
+                // b-side: the X1 array 7 + e3 gives the combinations (e2, e3)
+                // at arrays 7 (0,0), 8 (2,0), 10 (1,0) | 11 (0,1), 12 (1,1) | 9 (0,2)
+                const int e3 = t - 7;
+                const int no = e3 == 0 ? 3 : (e3 == 1 ? 2 : 1);
+                for (int o = 0; o < no; ++o) {
+                    const int e2 = e3 == 0 ? (o == 0 ? 0 : (o == 1 ? 2 : 1)) : (e3 == 1 ? o : 0);
+                    const int arr = e3 == 0 ? (o == 0 ? 7 : (o == 1 ? 8 : 10)) : (e3 == 1 ? 11 + o : 9);
+                    float2 xw[N];
+#pragma unroll
+                    for (int m = 0; m < n; ++m) xw[m] = e2 ? cscale(x[m], poww(m, h, e2)) : x[m];
+                    float2 *d = dst + arr * as;
+                    fwd_pencil_st<N, false>(xw, tw.fw, [&](int k, float2 v) { d[(size_t)k * os] = v; });
+                }
+            }
+        }
+    }
 }
 
 // Y: the direct convolution along axis 1 for the outputs i in
@@ -396,14 +482,30 @@ template <int N>
 cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc, float2 *scratch,
                       int Bs, double2 *q, cudaStream_t st, int stage) {
     constexpr int n = N, M = 3 * N / 2;
-    constexpr int NI = (N >= 32) ? N / 2 : N;  // outputs per thread in Y
+    constexpr int NI = N;  // outputs per thread in Y (one pass: X is read once)
     float2 *T3 = scratch, *X = scratch + fftq_t3_elems(n, Bs);
     float2 *G = T3, *H = T3 + (size_t)n * M * M * Bs;  // T3 is dead after X2
     const dim3 blk(32, kPY);
     const int gc = Bc / 32;
-    if (stage < 0 || stage == 0)
-        k_fq_x1<N><<<dim3((n * n + kPY - 1) / kPY, gc, 10), blk, 0, st>>>(F, C, Bp, c0, T3, Bs, tw);
-    if (stage < 0 || stage == 1) k_fq_x2<N><<<dim3((n * M + kPY - 1) / kPY, gc, 13), blk, 0, st>>>(T3, Bs, X, tw);
+    if constexpr (N <= 24) {
+        // X1 and X2 in one pass (stage 1 then has nothing left to do); at
+        // n = 32 the plane's 196 KB of shared memory leaves one block per SM
+        // and the separate kernels are faster
+        if (stage < 0 || stage == 0) {
+            // 16 x 12 threads at n = 16, 24: two blocks fit the register file
+            constexpr int PY = (N == 24) ? 12 : M / 2;
+            const size_t smem = sizeof(float2) * n * M * 16;
+            const cudaError_t e =
+                cudaFuncSetAttribute(k_fq_x12<N, PY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            k_fq_x12<N, PY><<<dim3(n, Bc / 16, 10), dim3(16, PY), smem, st>>>(F, C, Bp, c0, X, Bs, tw);
+        }
+    } else {
+        if (stage < 0 || stage == 0)
+            k_fq_x1<N><<<dim3((n * n + kPY - 1) / kPY, gc, 10), blk, 0, st>>>(F, C, Bp, c0, T3, Bs, tw);
+        if (stage < 0 || stage == 1)
+            k_fq_x2<N><<<dim3((n * M + kPY - 1) / kPY, gc, 13), blk, 0, st>>>(T3, Bs, X, tw);
+    }
     if (stage < 0 || stage == 2) {
         constexpr int PY = (N >= 32) ? 2 : 4;
         const size_t smem = sizeof(float2) * 2 * 2 * N * 32 * PY;
