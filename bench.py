@@ -50,7 +50,7 @@ FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x2": 107.26e6 + 147.53e6}
 def launches_per_step(line_warps):
     """Kernels of one mixed collision step at n = 24 (64 cells, one pass):
     nodes 1, forward transform 3 x 4, contraction x 4 (4 kernels in the
-    convolution form at n <= 24, 2 k-tiles in the line-tiled form),
+    convolution form, 2 k-tiles in the line-tiled form),
     conservation 2 x 4 (its correction is applied by the next kernels),
     inverse transform 3 x 3, DG projection 3, multipliers 1, scatter 1."""
     return 1 + 12 + 4 * (4 if line_warps == 0 else 2) + 8 + 9 + 3 + 1 + 1
@@ -62,13 +62,11 @@ def fq_kernel_model(n, cells):
     each kernel reads its input arrays once and writes its outputs once."""
     M, h = 3 * n // 2, n // 2
     c8 = 8 * cells
-    t3, x, g, hh = 10 * n * n * M, 13 * n * M * M, n * M * M, n * n * M
+    x, g, hh = 13 * n * M * M, n * M * M, n * n * M
     # valid (i, l) pairs of the direct axis-1 sum: 0 <= i + h - l < n
     pairs = sum(1 for i in range(n) for l in range(n) if 0 <= i + h - l < n)
     model = {
-        "k_fq_x1": (n ** 3 * c8 + 7 * n ** 3 * 4 + t3 * c8, None),
-        "k_fq_x2": (t3 * c8 + x * c8, None),
-        # n <= 24: X1 and X2 fused, the X1 outputs stay in shared memory
+        # X1 and X2 fused: the X1 outputs stay in shared memory
         "k_fq_x12": (n ** 3 * c8 + 7 * n ** 3 * 4 + x * c8, None),
         "k_fq_y": (x * c8 + g * c8, 7 * pairs * 8.0 * M * M * cells),
         "k_fq_z1": (g * c8 + hh * c8, None),
@@ -79,8 +77,7 @@ def fq_kernel_model(n, cells):
 
 def fq_kernels(n):
     """(name, lp_time_kernel code) of the convolution form's kernels."""
-    first = [("k_fq_x12", 4)] if n <= 24 else [("k_fq_x1", 4), ("k_fq_x2", 5)]
-    return first + [("k_fq_y", 6), ("k_fq_z1", 7), ("k_fq_z2", 8)]
+    return [("k_fq_x12", 4), ("k_fq_y", 6), ("k_fq_z1", 7), ("k_fq_z2", 8)]
 
 
 def _config(extra=None):

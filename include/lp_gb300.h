@@ -174,12 +174,11 @@ lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
  * context's stream, over `reps` launches after one warm-up, timed with CUDA
  * events: which = 0 the weighted contraction of ComputeQ for every collided
  * cell, 1 the forward transform, 2 the moment-conserving projection, 3 the
- * DG projection of the RK4 combination; 4..8 the kernels of the
- * convolution form (axis-3 DFTs, axis-2 DFTs, axis-1 sums, inverse axis-2
- * and axis-3 DFTs; for n <= 24 the first two are one fused kernel timed
- * under 4, and 5 launches nothing) for the first convolution chunk of
- * cells, each alone, when that form is the schedule.  Needs the resident
- * state. */
+ * DG projection of the RK4 combination; 4, 6, 7, 8 the kernels of the
+ * convolution form (axis-3 and axis-2 DFTs in one kernel, axis-1 sums,
+ * inverse axis-2 and axis-3 DFTs; 5 launches nothing) for the first
+ * convolution chunk of cells, each alone, when that form is the schedule.
+ * Needs the resident state. */
 lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
 /* Dense FMA throughput of the current device measured with dependent-chain
  * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */

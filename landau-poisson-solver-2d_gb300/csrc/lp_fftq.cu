@@ -23,7 +23,8 @@
 // forward and inverse transforms it replaces):
 //
 //   X1  axis-3 DFT of the 7 a-arrays and of F (u3-h)^e, e = 0, 1, 2;
-//   X2  axis-2 DFT of the 7 a-arrays and of the 6 (e2, e3) b-combinations;
+//   X2  axis-2 DFT of the 7 a-arrays and of the 6 (e2, e3) b-combinations
+//       (X1 and X2 in one kernel, the X1 outputs held in shared memory);
 //   Y   per (k2, k3): sum_p sum_l a_p(l) (u1-h)^e1 b_p(u1), u1 = i + h - l;
 //   Z1  inverse axis-2 DFT, only the n outputs xi2 + h;
 //   Z2  inverse axis-3 DFT, only the n outputs xi3 + h, written as FP64.
@@ -232,86 +233,26 @@ __device__ __forceinline__ float poww(int u, int h, int e) {
 
 constexpr int kPY = 4;  // pencils per block (blockDim.y); blockDim.x = 32 cells
 
-// X1: axis-3 DFT of the (l, m) pencils.  Arrays 0..6: C_p F (a-side, with
-// the phase); 7..9: (u3 - h)^e F.  T3 is [10][n][n][M][Bs].
-template <int N>
-__global__ void __launch_bounds__(32 * kPY) k_fq_x1(const float2 *__restrict__ F, const float *__restrict__ C,
-                                                    int Bp, int c0, float2 *__restrict__ T3, int Bs, FftTw tw) {
-    constexpr int n = N, h = N / 2, M = 3 * N / 2;
-    const int pen = blockIdx.x * kPY + threadIdx.y;
-    if (pen >= n * n) return;
-    const int cell = blockIdx.y * 32 + threadIdx.x, arr = blockIdx.z;
-    const float2 *src = F + (size_t)pen * n * Bp + c0 + cell;
-    float2 x[N];
-    float2 *dst = T3 + ((size_t)arr * n * n + pen) * M * Bs + cell;
-    auto put = [&](int k, float2 v) { dst[(size_t)k * Bs] = v; };
-    if (arr < 7) {
-        const float *cp = C + (size_t)arr * n * n * n + (size_t)pen * n;
-#pragma unroll
-        for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], __ldg(cp + q));
-        fwd_pencil_st<N, true>(x, tw.fa, put);
-    } else {
-        const int e = arr - 7;
-#pragma unroll
-        for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], poww(q, h, e));
-        fwd_pencil_st<N, false>(x, tw.fw, put);
-    }
-}
-
-// X2: axis-2 DFT of the (l, k3) pencils.  Arrays 0..6 the a-side; 7..12
-// the b-side combinations (e2, e3) = (0,0) (2,0) (0,2) (1,0) (0,1) (1,1),
-// from the X1 arrays 7 + e3 weighted by (u2 - h)^e2.  X is [13][n][M][M][Bs].
-template <int N>
-__global__ void __launch_bounds__(32 * kPY) k_fq_x2(const float2 *__restrict__ T3, int Bs,
-                                                    float2 *__restrict__ X, FftTw tw) {
-    constexpr int n = N, h = N / 2, M = 3 * N / 2;
-    const int pen = blockIdx.x * kPY + threadIdx.y;
-    if (pen >= n * M) return;
-    const int l = pen / M, k3 = pen - l * M;
-    const int cell = blockIdx.y * 32 + threadIdx.x, arr = blockIdx.z;
-    int sa = arr, e2 = 0;
-    if (arr >= 7) {
-        const int j = arr - 7;
-        sa = 7 + (j == 2 ? 2 : (j >= 4 ? 1 : 0));
-        e2 = (j == 1) ? 2 : ((j == 3 || j == 5) ? 1 : 0);
-    }
-    const float2 *src = T3 + (((size_t)sa * n + l) * n * M + k3) * Bs + cell;
-    float2 x[N];
-#pragma unroll
-    for (int m = 0; m < n; ++m) x[m] = src[(size_t)m * M * Bs];
-    float2 *dst = X + (((size_t)arr * n + l) * M * M + k3) * Bs + cell;
-    auto put = [&](int k, float2 v) { dst[(size_t)k * M * Bs] = v; };
-    if (arr < 7) {
-        fwd_pencil_st<N, true>(x, tw.fa, put);
-    } else {
-        if (e2) {
-#pragma unroll
-            for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2));
-        }
-        fwd_pencil_st<N, false>(x, tw.fw, put);
-    }
-}
-
-// X1 and X2 fused per (axis-1 plane l, 16 cells, X1 array t = blockIdx.z):
-// the plane's axis-3 DFTs go to shared memory ([m][k3][16 cells]) and the
+// X1 and X2 fused per (axis-1 plane l, CB cells, X1 array t = blockIdx.z):
+// the plane's axis-3 DFTs go to shared memory ([m][k3][CB cells]) and the
 // axis-2 DFTs read them from there, so the X1 outputs never reach DRAM.
-// blockDim = (16 cells, PY threads), each thread taking pencils ty,
+// blockDim = (CB cells, PY threads), each thread taking pencils ty,
 // ty + PY, ... of both phases.
-template <int N, int PY>
-__global__ void __launch_bounds__(16 * PY) k_fq_x12(const float2 *__restrict__ F, const float *__restrict__ C,
+template <int N, int PY, int CB>
+__global__ void __launch_bounds__(CB * PY) k_fq_x12(const float2 *__restrict__ F, const float *__restrict__ C,
                                                     int Bp, int c0, float2 *__restrict__ X, int Bs, FftTw tw) {
     constexpr int n = N, h = N / 2, M = 3 * N / 2;
-    extern __shared__ float2 t3[];  // [m][k3][16]
+    extern __shared__ float2 t3[];  // [m][k3][CB]
     const int tx = threadIdx.x, ty = threadIdx.y, l = blockIdx.x, t = blockIdx.z;
-    const int cell = blockIdx.y * 16 + tx;
+    const int cell = blockIdx.y * CB + tx;
     const size_t as = (size_t)n * M * M * Bs, os = (size_t)M * Bs;  // array and k2 strides of X
     {
         // axis-3 DFTs of the (l, m) pencils of array t
         for (int m = ty; m < n; m += PY) {
             const float2 *src = F + ((size_t)l * n + m) * n * Bp + c0 + cell;
             float2 x[N];
-            float2 *row = t3 + m * M * 16 + tx;
-            auto put = [&](int k, float2 v) { row[k * 16] = v; };
+            float2 *row = t3 + m * M * CB + tx;
+            auto put = [&](int k, float2 v) { row[k * CB] = v; };
             if (t < 7) {
                 const float *cp = C + (size_t)t * n * n * n + ((size_t)l * n + m) * n;
 #pragma unroll
@@ -328,7 +269,7 @@ __global__ void __launch_bounds__(16 * PY) k_fq_x12(const float2 *__restrict__ F
         for (int k3 = ty; k3 < M; k3 += PY) {
             float2 x[N];
 #pragma unroll
-            for (int m = 0; m < n; ++m) x[m] = t3[(m * M + k3) * 16 + tx];
+            for (int m = 0; m < n; ++m) x[m] = t3[(m * M + k3) * CB + tx];
             float2 *dst = X + ((size_t)l * M * M + k3) * Bs + cell;
             if (t < 7) {
                 float2 *d = dst + t * as;
@@ -483,28 +424,22 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
                       int Bs, double2 *q, cudaStream_t st, int stage) {
     constexpr int n = N, M = 3 * N / 2;
     constexpr int NI = N;  // outputs per thread in Y (one pass: X is read once)
-    float2 *T3 = scratch, *X = scratch + fftq_t3_elems(n, Bs);
-    float2 *G = T3, *H = T3 + (size_t)n * M * M * Bs;  // T3 is dead after X2
+    float2 *G = scratch, *H = scratch + (size_t)n * M * M * Bs, *X = scratch + fftq_gh_elems(n, Bs);
     const dim3 blk(32, kPY);
     const int gc = Bc / 32;
-    if constexpr (N <= 24) {
-        // X1 and X2 in one pass (stage 1 then has nothing left to do); at
-        // n = 32 the plane's 196 KB of shared memory leaves one block per SM
-        // and the separate kernels are faster
+    {
+        // X1 and X2 in one pass (stage 1 then has nothing left to do): 16
+        // cells per block up to n = 24, 8 at n = 32 (a plane of 16 cells
+        // would take 196 KB of shared memory)
+        constexpr int CB = (N == 32) ? 8 : 16;
+        constexpr int PY = (N == 24) ? 12 : (N == 32 ? 16 : M / 2);
         if (stage < 0 || stage == 0) {
-            // 16 x 12 threads at n = 16, 24: two blocks fit the register file
-            constexpr int PY = (N == 24) ? 12 : M / 2;
-            const size_t smem = sizeof(float2) * n * M * 16;
+            const size_t smem = sizeof(float2) * n * M * CB;
             const cudaError_t e =
-                cudaFuncSetAttribute(k_fq_x12<N, PY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(k_fq_x12<N, PY, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            k_fq_x12<N, PY><<<dim3(n, Bc / 16, 10), dim3(16, PY), smem, st>>>(F, C, Bp, c0, X, Bs, tw);
+            k_fq_x12<N, PY, CB><<<dim3(n, Bc / CB, 10), dim3(CB, PY), smem, st>>>(F, C, Bp, c0, X, Bs, tw);
         }
-    } else {
-        if (stage < 0 || stage == 0)
-            k_fq_x1<N><<<dim3((n * n + kPY - 1) / kPY, gc, 10), blk, 0, st>>>(F, C, Bp, c0, T3, Bs, tw);
-        if (stage < 0 || stage == 1)
-            k_fq_x2<N><<<dim3((n * M + kPY - 1) / kPY, gc, 13), blk, 0, st>>>(T3, Bs, X, tw);
     }
     if (stage < 0 || stage == 2) {
         constexpr int PY = (N >= 32) ? 2 : 4;
@@ -525,11 +460,14 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
 
 bool fftq_supported(int n) { return n == 8 || n == 16 || n == 24 || n == 32; }
 
-size_t fftq_t3_elems(int n, int Bs) { return (size_t)10 * n * n * (3 * n / 2) * Bs; }
+size_t fftq_gh_elems(int n, int Bs) {
+    const size_t M = 3 * (size_t)n / 2;
+    return (size_t)n * M * (M + n) * Bs;
+}
 
 size_t fftq_scratch_elems(int n, int Bs) {
     const size_t M = 3 * (size_t)n / 2;
-    return fftq_t3_elems(n, Bs) + (size_t)13 * n * M * M * Bs;
+    return fftq_gh_elems(n, Bs) + (size_t)13 * n * M * M * Bs;
 }
 
 FftTw fftq_twiddles(int n) {

@@ -108,11 +108,12 @@ bool fftq_supported(int n);
 FftTw fftq_twiddles(int n);
 void fftq_coefficients(const double *shat, const double *ahat, const double *cw, double h_eta, int n,
                        std::vector<float> &C);
-size_t fftq_t3_elems(int n, int Bs);
+size_t fftq_gh_elems(int n, int Bs);       // axis-1 sums and inverse axis-2 outputs
 size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
 // Cells [c0, c0 + Bc) of F and q (stride Bp); Bc and c0 multiples of 32,
-// Bc <= Bs, the cells of the scratch.  stage -1 runs the five kernels;
-// 0..4 only one of them (X1, X2, Y, Z1, Z2), on the scratch a full run left.
+// Bc <= Bs, the cells of the scratch.  stage -1 runs the four kernels; 0, 2,
+// 3, 4 only one of them (the fused X1/X2, Y, Z1, Z2; 1 launches nothing), on
+// the scratch a full run left.
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
                                 float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1);
 
