@@ -269,7 +269,15 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
     using C = typename V2<R>::t;
     constexpr int NO = N / OG;  // outputs per thread
     __shared__ C Ms[N * N];
+    __shared__ float cfs[PY][5][N];  // constraint rows of the block's pencils (cf given)
     for (int t = threadIdx.y * 32 + threadIdx.x; t < N * N; t += 32 * PY * OG) Ms[t] = mk2<R>(M[2 * t], M[2 * t + 1]);
+    if (cf) {
+        constexpr int n3 = N * N * N;
+        for (int t = threadIdx.y * 32 + threadIdx.x; t < PY * 5 * N; t += 32 * PY * OG) {
+            const int pp = t / (5 * N), r = (t / N) % 5, i = t % N, p0 = blockIdx.x * PY + pp;
+            cfs[pp][r][i] = p0 < N * N ? cf[r * n3 + p0 * N + i] : 0.f;
+        }
+    }
     __syncthreads();
     const int pid = blockIdx.x * PY + threadIdx.y / OG, og = threadIdx.y % OG;
     if (pid >= N * N) return;
@@ -286,14 +294,13 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
         else x[i] = ld2<R>(in + base + i * stride);
     }
     if (cf) {
-        constexpr int n3 = N * N * N;
         const R l0 = (R)lamc[c], l1 = (R)lamc[Bp + c], l2 = (R)lamc[2 * Bp + c], l3 = (R)lamc[3 * Bp + c],
                 l4 = (R)lamc[4 * Bp + c];
+        const float(*r)[N] = cfs[threadIdx.y / OG];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-            const int pt = pid * N + i;
-            x[i].x -= (R)cf[pt] * l0 + (R)cf[4 * n3 + pt] * l4;
-            x[i].y -= (R)cf[n3 + pt] * l1 + (R)cf[2 * n3 + pt] * l2 + (R)cf[3 * n3 + pt] * l3;
+            x[i].x -= (R)r[0][i] * l0 + (R)r[4][i] * l4;
+            x[i].y -= (R)r[1][i] * l1 + (R)r[2][i] * l2 + (R)r[3][i] * l3;
         }
     }
     R dtc = dt, nuc = nu;
@@ -652,21 +659,30 @@ __global__ void k_cons_partial(const double2 *__restrict__ q, const double *__re
     }
 }
 
-// One warp per cell: lanes sum the chunk partials (fixed order, then a fixed
-// shuffle tree), lane 0 solves (C C^T)^-1 t (solveWithCCt, K:49-55).
-__global__ void k_cons_lambda(const double *__restrict__ part, int nchunk, const double *__restrict__ cct,
-                              int Bp, double *__restrict__ lam) {
-    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (c >= Bp) return;
-    double t[5] = {0, 0, 0, 0, 0};
-    for (int k = lane; k < nchunk; k += 32)
-        for (int j = 0; j < 5; ++j) t[j] += part[((long long)k * 5 + j) * Bp + c];
-    for (int off = 16; off > 0; off >>= 1)
-        for (int j = 0; j < 5; ++j) t[j] += __shfl_down_sync(FULL, t[j], off);
-    if (lane == 0)
+// One block per cell: the threads sum the chunk partials in a fixed order
+// and a fixed tree, thread 0 solves (C C^T)^-1 t (solveWithCCt, K:49-55).
+__global__ void __launch_bounds__(256) k_cons_lambda(const double *__restrict__ part, int nchunk,
+                                                     const double *__restrict__ cct, int Bp,
+                                                     double *__restrict__ lam) {
+    __shared__ double red[5][256];
+    const int c = blockIdx.x, t = threadIdx.x;
+    double v[5] = {0, 0, 0, 0, 0};
+    for (int k = t; k < nchunk; k += 256)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) v[j] += part[((long long)k * 5 + j) * Bp + c];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) red[j][t] = v[j];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+#pragma unroll
+            for (int j = 0; j < 5; ++j) red[j][t] += red[j][t + w];
+        __syncthreads();
+    }
+    if (t == 0)
         for (int i = 0; i < 5; ++i) {
             double s = 0.;
-            for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * t[j];
+            for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * red[j][0];
             lam[(long long)i * Bp + c] = s;
         }
 }
@@ -2307,7 +2323,7 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
                             double *part, int nchunk, double *lam, cudaStream_t st, bool apply) {
     k_cons_partial<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
-    k_cons_lambda<<<(Bp + 3) / 4, 128, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     if (apply) k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
     return cudaGetLastError();
 }
