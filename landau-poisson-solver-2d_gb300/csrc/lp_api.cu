@@ -83,6 +83,9 @@ struct lp_ctx {
     // stages, lam4[4][5][Bcap]
     float *cf = nullptr;
     double *lam4 = nullptr;
+    // FP32 mode arrays of the four stages (lazy conservation with the
+    // convolution form, whose output is FP32-accurate)
+    float2 *qf[4] = {nullptr, nullptr, nullptr, nullptr};
     int nrc = 16;
     // adjoint workspace (FP64 contexts, allocated by the first adjoint call)
     struct Adj {
@@ -198,6 +201,7 @@ template <typename R> lp_status alloc_workspace(lp_ctx *c) {
             }
             LP_TRY(upload(c, &c->cf, cf.data(), cf.size()));
             LP_TRY(dalloc(c, &c->lam4, 4 * 5 * Bp));
+            for (int i = 0; i < 4; ++i) LP_TRY(dalloc(c, &c->qf[i], n3 * Bp));
         }
     }
     return LP_OK;
@@ -396,15 +400,18 @@ lp_status advect(lp_ctx *c) {
 // The weighted contraction of ComputeQ on the transformed node values F.
 // Mixed path: line_warps 0 selects the convolution form, 2 or 4 the
 // line-tiled weighted sum with that many warps per line.
-template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
+// q32: the convolution form writes the mode array in FP32 there.
+template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *q32 = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     if (c->FQC && c->line_warps == 0) {
         for (int c0 = 0; c0 < Bp; c0 += c->fq_bs)
             LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, c0,
-                                            std::min(c->fq_bs, Bp - c0), c->fscr, c->fq_bs, q, c->stream));
+                                            std::min(c->fq_bs, Bp - c0), c->fscr, c->fq_bs, q, c->stream, -1,
+                                            q32));
         return LP_OK;
     }
+    if (q32) return fail(c, LP_ERR_INVALID, "FP32 mode arrays need the convolution form");
     if (c->LW) {
         // the k-tiles run on two streams so that the short lines at the end
         // of one tile overlap the next tile
@@ -430,10 +437,16 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q) {
 // and added again after (C:551-635, K:63-98, C:656-698).
 // slot >= 0 (lazy conservation): only the multipliers of stage `slot` are
 // computed, into lam4; the consumers of q apply the correction on load.
-template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q, int slot = -1) {
+// q32 (with slot): the mode array is kept in FP32 there.
+template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q, int slot = -1, float2 *q32 = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
-    LP_TRY(contract<R>(c, Bp, q));
+    LP_TRY(contract<R>(c, Bp, q, q32));
+    if (q32) {
+        LP_CUDA(lp::launch_conserve_lam(q32, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk,
+                                        c->lam4 + slot * 5 * Bp, c->stream));
+        return LP_OK;
+    }
     if (c->WLin) {
         const long long tot = (long long)T.n3 * Bp;
         LP_CUDA(lp::launch_qlin<R>((const C *)c->F, (const R *)c->WLin, c->win_off, T.n, Bp, c->qlin, c->stream));
@@ -462,16 +475,22 @@ lp::Rates rates_at(const lp_ctx *c, int c0) {
 
 // lazy: the stages' conservation corrections are applied by the consumers
 // (the next FS pass and the first DG projection pass).
-template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp, bool lazy = false) {
+// f32 (with lazy): the mode arrays are the FP32 ones, c->qf.
+template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp, bool lazy = false, bool f32 = false) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     const R *M = (const R *)c->mfwd, *Mi = (const R *)c->minv;
     for (int s = 0; s < 3; ++s) {
-        LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
-                                       (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0),
-                                       lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr));
+        if (f32)
+            LP_CUDA(lp::launch_fs_stage32(c->qf[s], (float2 *)c->t1, (float2 *)c->t2, (const float *)Mi, T.n, Bp, s,
+                                          T.prm.dt, T.prm.nu, (const float *)c->f, (float *)c->qn, (float *)c->f1,
+                                          c->stream, rates_at(c, c0), c->cf, c->lam4 + s * 5 * Bp));
+        else
+            LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
+                                           (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0),
+                                           lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr));
         LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
-        LP_TRY(stage_q<R>(c, Bp, c->q[s + 1], lazy ? s + 1 : -1));
+        LP_TRY(stage_q<R>(c, Bp, c->q[s + 1], lazy ? s + 1 : -1, f32 ? c->qf[s + 1] : nullptr));
     }
     return LP_OK;
 }
@@ -525,7 +544,7 @@ bool fused_tail(const lp_ctx *c) { return c->mixed && (c->T.prm.fixes & LP_FIX_F
 // register-pencil kernels (the two-species operator keeps its add-conserve-add order).
 bool lazy_cons(const lp_ctx *c) { return fused_tail(c) && !c->WLin && c->cf; }
 
-lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false) {
+lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false, bool f32 = false) {
     const lp::Tables &T = c->T;
     const bool target = c->WLin != nullptr;
     cudaStream_t tst = (target && c->side) ? c->side : c->stream;
@@ -541,7 +560,7 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false) {
     LP_CUDA(lp::launch_project_inc(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const float *)c->tfac, T.n, T.nv,
                                    Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
                                    (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
-                                   lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr));
+                                   lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr, f32 ? c->qf : nullptr));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
     LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.n, T.nv, B, Bp, c->gm_inv,
@@ -559,9 +578,11 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
                                 c->stream));
     LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
     const bool lazy = lazy_cons(c);
-    LP_TRY(stage_q<R>(c, Bp, c->q[0], lazy ? 0 : -1));
-    LP_TRY(rk4_stages<R>(c, c0, Bp, lazy));
-    if (fused_tail(c)) return project_fused(c, c0, B, Bp, lazy);
+    // FP32 mode arrays: the convolution form's output is FP32-accurate
+    const bool f32 = lazy && c->FQC && c->line_warps == 0 && c->qf[0];
+    LP_TRY(stage_q<R>(c, Bp, c->q[0], lazy ? 0 : -1, f32 ? c->qf[0] : nullptr));
+    LP_TRY(rk4_stages<R>(c, c0, Bp, lazy, f32));
+    if (fused_tail(c)) return project_fused(c, c0, B, Bp, lazy, f32);
     LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
 }

@@ -40,6 +40,7 @@
 #include "lp_dev.cuh"
 
 #include <cmath>
+#include <type_traits>
 
 namespace lp {
 namespace {
@@ -401,9 +402,10 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_z1(const float2 *__restrict__ G
     for (int j = 0; j < n; ++j) dst[(size_t)j * M * Bs] = x[j];
 }
 
-// Z2: inverse axis-3 DFT of the (i, j) pencils into q (FP64, stride Bp).
-template <int N>
-__global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H, int Bs, double2 *__restrict__ q,
+// Z2: inverse axis-3 DFT of the (i, j) pencils into q (stride Bp), FP64
+// or FP32 complex.
+template <int N, typename QT>
+__global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H, int Bs, QT *__restrict__ q,
                                                     int Bp, int c0, FftTw tw) {
     constexpr int n = N, M = 3 * N / 2;
     const int pen = blockIdx.x * kPY + threadIdx.y;
@@ -414,14 +416,17 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H
 #pragma unroll
     for (int k = 0; k < M; ++k) g[k] = src[(size_t)k * Bs];
     inv_pencil<N>(g, x, tw.iv);
-    double2 *dst = q + (size_t)pen * n * Bp + c0 + cell;
+    QT *dst = q + (size_t)pen * n * Bp + c0 + cell;
 #pragma unroll
-    for (int k = 0; k < n; ++k) dst[(size_t)k * Bp] = make_double2((double)x[k].x, (double)x[k].y);
+    for (int k = 0; k < n; ++k) {
+        if constexpr (std::is_same<QT, double2>::value) dst[(size_t)k * Bp] = make_double2((double)x[k].x, (double)x[k].y);
+        else dst[(size_t)k * Bp] = x[k];
+    }
 }
 
 template <int N>
 cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc, float2 *scratch,
-                      int Bs, double2 *q, cudaStream_t st, int stage) {
+                      int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32) {
     constexpr int n = N, M = 3 * N / 2;
     constexpr int NI = N;  // outputs per thread in Y (one pass: X is read once)
     float2 *G = scratch, *H = scratch + (size_t)n * M * M * Bs, *X = scratch + fftq_gh_elems(n, Bs);
@@ -451,8 +456,10 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
         k_fq_y<N, NI, PY><<<dim3((M * M + PY - 1) / PY, gc, N / NI), dim3(32, PY), smem, st>>>(X, Bs, G);
     }
     if (stage < 0 || stage == 3) k_fq_z1<N><<<dim3((n * M + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(G, Bs, H, tw);
-    if (stage < 0 || stage == 4)
-        k_fq_z2<N><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q, Bp, c0, tw);
+    if (stage < 0 || stage == 4) {
+        if (q32) k_fq_z2<N, float2><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q32, Bp, c0, tw);
+        else k_fq_z2<N, double2><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q, Bp, c0, tw);
+    }
     return cudaGetLastError();
 }
 
@@ -500,14 +507,14 @@ void fftq_coefficients(const double *shat, const double *ahat, const double *cw,
 }
 
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
-                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage) {
+                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32) {
     if (Bc <= 0 || Bc % 32 || Bc > Bs || c0 % 32 || c0 + Bc > Bp || stage < -1 || stage > 4)
         return cudaErrorInvalidValue;
     switch (n) {
-    case 8: return launch_fq<8>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
-    case 16: return launch_fq<16>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
-    case 24: return launch_fq<24>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
-    case 32: return launch_fq<32>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage);
+    case 8: return launch_fq<8>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
+    case 16: return launch_fq<16>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
+    case 24: return launch_fq<24>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
+    case 32: return launch_fq<32>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -634,7 +634,8 @@ __global__ void k_lines_table(const double *__restrict__ eta, const double *__re
 // ---------------------------------------------------------------- conserve
 // conserveAllMoments (K:100-129): t = C q (5 dot products), lam = (CC^T)^-1 t,
 // q -= C^T lam.  Partial sums per chunk of points, then per cell.
-__global__ void k_cons_partial(const double2 *__restrict__ q, const double *__restrict__ c1,
+template <typename QT>
+__global__ void k_cons_partial(const QT *__restrict__ q, const double *__restrict__ c1,
                                const double *__restrict__ c2, int n3, int Bp, int nchunk,
                                double *__restrict__ part) {
     __shared__ double red[8][5][32];
@@ -643,7 +644,8 @@ __global__ void k_cons_partial(const double2 *__restrict__ q, const double *__re
     double t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0;
 #pragma unroll 4
     for (int pt = p0 + y; pt < p1; pt += 8) {
-        const double2 v = q[(long long)pt * Bp + c];
+        const QT w = q[(long long)pt * Bp + c];
+        const double2 v = make_double2((double)w.x, (double)w.y);
         t0 += v.x * c1[pt];
         t1 += v.y * c2[n3 + pt];
         t2 += v.y * c2[2 * n3 + pt];
@@ -1112,9 +1114,9 @@ __global__ void __launch_bounds__(32 * kIncWarps)
 // cf/lam4: the q_s were not projected by conserveAllMoments; each gets its
 // correction q_s -= C^T lambda_s (lam4[s][5][Bp]) in FP32 on load, and the
 // combination is formed in FP32.
-template <int N>
-__global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, const double2 *__restrict__ q1,
-                                             const double2 *__restrict__ q2, const double2 *__restrict__ q3,
+template <int N, typename QT>
+__global__ void __launch_bounds__(128) k_pj3(const QT *__restrict__ q0, const QT *__restrict__ q1,
+                                             const QT *__restrict__ q2, const QT *__restrict__ q3,
                                              double nu, const double *__restrict__ cnu, const float *__restrict__ tf,
                                              int nv, int Bp, float2 *__restrict__ Y, const float *__restrict__ cf,
                                              const double *__restrict__ lam4) {
@@ -1140,7 +1142,7 @@ __global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, con
             const long long o = b + (long long)k * Bp;
             const int pt = pid * N + k;
             const float r0 = cf[pt], r1 = cf[n3 + pt], r2 = cf[2 * n3 + pt], r3 = cf[3 * n3 + pt], r4 = cf[4 * n3 + pt];
-            const double2 qs[4] = {q0[o], q1[o], q2[o], q3[o]};
+            const QT qs[4] = {q0[o], q1[o], q2[o], q3[o]};
             float2 v[4];
 #pragma unroll
             for (int s = 0; s < 4; ++s) {
@@ -1154,7 +1156,7 @@ __global__ void __launch_bounds__(128) k_pj3(const double2 *__restrict__ q0, con
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             const long long o = b + (long long)k * Bp;
-            const double2 a = q0[o], e = q1[o], d = q2[o], g = q3[o];
+            const QT a = q0[o], e = q1[o], d = q2[o], g = q3[o];
             x[k] = make_float2((float)(nu * (0.5 * a.x + (e.x + d.x + g.x) * (1. / 6.))),
                                (float)(nu * (0.5 * a.y + (e.y + d.y + g.y) * (1. / 6.))));
         }
@@ -1301,14 +1303,19 @@ template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
                       double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
-                      const float *cf, const double *lam4) {
+                      const float *cf, const double *lam4, float2 *const *q32) {
     const size_t ts = sizeof(float2) * 3 * N * nv, zsm = sizeof(float2) * kPj1Pen * 5 * N * 32;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_pj3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj3<N, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj3<N, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj1<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ts + zsm)))) return e;
-    k_pj3<N><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac, nv, Bp, Y,
-                                                                       cf, lam4);
+    if (q32)
+        k_pj3<N, float2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(
+            q32[0], q32[1], q32[2], q32[3], nu, rates.nu, tfac, nv, Bp, Y, cf, lam4);
+    else
+        k_pj3<N, double2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac,
+                                                                                nv, Bp, Y, cf, lam4);
     k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
     k_pj1<N><<<dim3((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32), 32 * kPj1Warps, ts + zsm, st>>>(
         Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
@@ -2212,6 +2219,17 @@ cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2
     return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
 }
 
+cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const float *M, int n, int Bp, int stage,
+                              double dt, double nu, const float *f, float *qn, float *f1, cudaStream_t st,
+                              Rates rates, const float *cf, const double *lamc) {
+    cudaError_t e;
+    if ((e = dft_pass<float, float2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf,
+                                        lamc)))
+        return e;
+    if ((e = dft_pass<float, float2, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
+    return dft_pass<float, float2, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
+}
+
 template <typename R>
 cudaError_t launch_fs_full(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
                            typename V2<R>::t *out, const R *M, int n, int Bp, cudaStream_t st) {
@@ -2322,9 +2340,16 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
 
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
                             double *part, int nchunk, double *lam, cudaStream_t st, bool apply) {
-    k_cons_partial<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
+    k_cons_partial<double2><<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
     k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     if (apply) k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
+                                int Bp, double *part, int nchunk, double *lam, cudaStream_t st) {
+    k_cons_partial<float2><<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
+    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     return cudaGetLastError();
 }
 
@@ -2377,16 +2402,16 @@ cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const doubl
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates, const float *cf,
-                               const double *lam4) {
+                               const double *lam4, float2 *const *q32) {
     const double kfac = 1. / scalev / scaleL / scale3;
     switch (n) {
-    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
-    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
-    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
-    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4);
+    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
+    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
+    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
+    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
     default: break;
     }
-    if (cf) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil passes
+    if (cf || q32) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil passes
     const long long n3 = (long long)n * n * n;
     k_qcomb<float><<<grid1(n3 * Bp, 256), 256, 0, st>>>(q0, q1, q2, q3, nu, n3 * Bp, Bp, rates.nu, Qc);
     const int nch = (nv + JB - 1) / JB;

@@ -53,6 +53,10 @@ cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2
                             const R *M, int n, int Bp, int stage, double dt, double nu,
                             const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{},
                             const float *cf = nullptr, const double *lamc = nullptr);
+// The same from an FP32 mode array (mixed path, n in {8, 16, 24, 32}).
+cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const float *M, int n, int Bp, int stage,
+                              double dt, double nu, const float *f, float *qn, float *f1, cudaStream_t st,
+                              Rates rates, const float *cf, const double *lamc);
 
 // Inverse transform FS of q, full complex output (for the reference-shaped FS).
 template <typename R>
@@ -113,9 +117,11 @@ size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
 // Cells [c0, c0 + Bc) of F and q (stride Bp); Bc and c0 multiples of 32,
 // Bc <= Bs, the cells of the scratch.  stage -1 runs the four kernels; 0, 2,
 // 3, 4 only one of them (the fused X1/X2, Y, Z1, Z2; 1 launches nothing), on
-// the scratch a full run left.
+// the scratch a full run left.  q32: the mode array is written as FP32
+// complex there instead of q.
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
-                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1);
+                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1,
+                                float2 *q32 = nullptr);
 
 // Moment-conserving projection of q in place (FP64).
 // apply = false: only the multipliers lam[5][Bp] (the correction is left to
@@ -123,6 +129,9 @@ cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
                             int n3, int Bp, double *part, int nchunk, double *lam,
                             cudaStream_t st, bool apply = true);
+// The multipliers of an FP32 mode array (FP64 sums of its exact values).
+cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
+                                int Bp, double *part, int nchunk, double *lam, cudaStream_t st);
 
 // Final RK4 combination, DG projection and mass-matrix inverse: writes
 // dU[B][nv^3][5] for cells [c0, c0+B).  Qc, Y, Z are scratch.
@@ -155,12 +164,14 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
 // U slots {0,3,4,5,6} += increment + moment correction.
 int project_inc_blocks(int n, int nv);
 // cf/lam4 (n in {8, 16, 24, 32}): the q_s were not projected; their
-// corrections with lam4[s][5][Bp] are applied in FP32 on load.
+// corrections with lam4[s][5][Bp] are applied in FP32 on load.  q32: the
+// four mode arrays are FP32 complex (q0..q3 unused).
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{},
-                               const float *cf = nullptr, const double *lam4 = nullptr);
+                               const float *cf = nullptr, const double *lam4 = nullptr,
+                               float2 *const *q32 = nullptr);
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
