@@ -1209,69 +1209,93 @@ __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const
     }
 }
 
-// Per (j2, j3, cell): the pencils Z0..Z4 along k1 are staged in shared
-// memory (kPj1Pen pencils x 32 cells per block); the warps split the j1
-// outputs of a pencil.  The 7 real sums of each j1 give
-// the increment (see k_proj1_inc), written cell-minor, and the block's
-// moment partials.
-constexpr int kPj1Warps = 8, kPj1Pen = 1;
-template <int N>
-__global__ void __launch_bounds__(32 * kPj1Warps, 2) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
+// Per (j2, j3, cell) pencil, four warps each take a group of consecutive
+// j1 outputs (an even count).  The five pencils Z0..Z4 along k1 are read
+// into registers one at a time and feed their real sums; the per-axis
+// factors come from shared memory, for two consecutive j1 per 16-byte load
+// when nv is even.  The 7 real sums of each j1 give the increment (see
+// k_proj1_inc), written cell-minor, and the block's moment partials.
+constexpr int kPj1Warps = 8, kPj1Pen = 2, kPj1Groups = kPj1Warps / kPj1Pen, kPj1Max = 8;
+template <int N, bool EVEN>
+__global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
                                                         int nv, int Bp, int B, double dt, double kfac,
                                                         const double *__restrict__ cdt, double dv, double lv,
                                                         MomRow mr, double *__restrict__ Inc, double *__restrict__ part) {
-    extern __shared__ float2 Ts[];
+    extern __shared__ __align__(16) float2 Ts[];  // [3][N][nv]
     __shared__ double red[kPj1Warps][5][32];
-    constexpr int nq = kPj1Warps / kPj1Pen;  // j1 groups per pencil
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int t = threadIdx.x; t < 3 * N * nv; t += 32 * kPj1Warps) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
-    float2 *zs_all = Ts + 3 * N * nv;  // [pencil][5 N][32 cells]
-    const int c = blockIdx.y * 32 + lane;
-    const long long zs = (long long)N * nv * nv * Bp;
-    // stage both pencils: rows (pencil, p, k) of 32 cells, coalesced
-    for (int row = w; row < kPj1Pen * 5 * N; row += kPj1Warps) {
-        const int pp = row / (5 * N), rem = row - pp * 5 * N, p = rem / N, k = rem - p * N;
-        const int pid = blockIdx.x * kPj1Pen + pp;
-        float2 v = make_float2(0.f, 0.f);
-        if (pid < nv * nv && c < B) {
-            const int j2 = pid / nv, j3 = pid - j2 * nv;
-            v = Z[p * zs + (((long long)k * nv + j2) * nv + j3) * Bp + c];
-        }
-        zs_all[row * 32 + lane] = v;
-    }
     __syncthreads();
-    const int pp = w / nq, g = w - pp * nq;
+    const int pp = w / kPj1Groups, g = w - pp * kPj1Groups;
     const int pid = blockIdx.x * kPj1Pen + pp;
+    const int c = blockIdx.y * 32 + lane;
+    const int jg = 2 * ((nv + 2 * kPj1Groups - 1) / (2 * kPj1Groups)), j0 = g * jg;
     double m[5] = {0, 0, 0, 0, 0};
-    if (pid < nv * nv && c < B) {
+    if (pid < nv * nv && c < B && j0 < nv) {
         const int j2 = pid / nv, j3 = pid - j2 * nv;
-        const float2 *zc = zs_all + pp * 5 * N * 32 + lane;
+        const long long zs = (long long)N * nv * nv * Bp, ks = (long long)nv * nv * Bp;
+        const float2 *zb = Z + ((long long)j2 * nv + j3) * Bp + c;
+        float a[7][kPj1Max];
+#pragma unroll
+        for (int e = 0; e < 7; ++e)
+#pragma unroll
+            for (int jj = 0; jj < kPj1Max; ++jj) a[e][jj] = 0.f;
+        // source pencil p feeds (table, sum): p = 0: (T0, 0) (T1, 1) (T2, 4); p = 1..4: (T0, 2 5 3 6)
+#pragma unroll 1
+        for (int p = 0; p < 5; ++p) {
+            float2 z[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) z[k] = zb[p * zs + k * ks];
+            const int e0 = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 5 : (p == 3 ? 3 : 6)));
+#pragma unroll
+            for (int jj = 0; jj < kPj1Max; jj += 2) {
+                const int j1 = j0 + jj;
+                if (jj >= jg || j1 >= nv) break;
+                float s0[3] = {0.f, 0.f, 0.f}, s1[3] = {0.f, 0.f, 0.f};
+                const int ntab = p == 0 ? 3 : 1;
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+#pragma unroll
+                    for (int tb = 0; tb < 3; ++tb) {
+                        if (tb >= ntab) break;
+                        const float2 *T = Ts + tb * N * nv + k * nv + j1;
+                        float2 t0, t1;
+                        if constexpr (EVEN) {
+                            const float4 tt = *reinterpret_cast<const float4 *>(T);
+                            t0 = make_float2(tt.x, tt.y);
+                            t1 = make_float2(tt.z, tt.w);
+                        } else {
+                            t0 = T[0];
+                            t1 = (j1 + 1 < nv) ? T[1] : make_float2(0.f, 0.f);
+                        }
+                        s0[tb] += t0.x * z[k].x - t0.y * z[k].y;
+                        s1[tb] += t1.x * z[k].x - t1.y * z[k].y;
+                    }
+                }
+                if (p == 0) {
+                    a[0][jj] = s0[0]; a[0][jj + 1] = s1[0];
+                    a[1][jj] = s0[1]; a[1][jj + 1] = s1[1];
+                    a[4][jj] = s0[2]; a[4][jj + 1] = s1[2];
+                } else {
+#pragma unroll
+                    for (int e = 2; e < 7; ++e)
+                        if (e == e0 && e != 4) { a[e][jj] = s0[0]; a[e][jj + 1] = s1[0]; }
+                }
+            }
+        }
         const float sf = (float)((cdt ? cdt[c] : dt) * kfac);
-        const float2 *T0 = Ts, *T1 = Ts + N * nv, *T2 = Ts + 2 * N * nv;
         const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
         // running sums over this thread's j1 of d_q, G1 d_0, G1 d_4, G1 d_1,
         // G1^2 d_0, G1^2 d_4; the moments follow from them with G2, G3
         double S[5] = {0, 0, 0, 0, 0}, A0 = 0, A4 = 0, A1 = 0, B0 = 0, B4 = 0;
-        for (int j1 = g; j1 < nv; j1 += nq) {
-            float a[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-            for (int k = 0; k < N; ++k) {
-                const float2 t0 = T0[k * nv + j1], t1 = T1[k * nv + j1], t2 = T2[k * nv + j1];
-                const float2 z0 = zc[(0 * N + k) * 32], z1 = zc[(1 * N + k) * 32], z2 = zc[(2 * N + k) * 32],
-                             z3 = zc[(3 * N + k) * 32], z4 = zc[(4 * N + k) * 32];
-                a[0] += t0.x * z0.x - t0.y * z0.y;
-                a[1] += t1.x * z0.x - t1.y * z0.y;
-                a[2] += t0.x * z1.x - t0.y * z1.y;
-                a[3] += t0.x * z3.x - t0.y * z3.y;
-                a[4] += t2.x * z0.x - t2.y * z0.y;
-                a[5] += t0.x * z2.x - t0.y * z2.y;
-                a[6] += t0.x * z4.x - t0.y * z4.y;
-            }
-            // the increment in FP32 (its inputs are FP32 sums), stored and
-            // summed in FP64
-            const float tp5 = a[4] + a[5] + a[6];
-            const double d0 = sf * (4.75f * a[0] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0]);
-            const double d1 = 12.f * sf * a[1], d2 = 12.f * sf * a[2], d3 = 12.f * sf * a[3];
+#pragma unroll
+        for (int jj = 0; jj < kPj1Max; ++jj) {
+            const int j1 = j0 + jj;
+            if (jj >= jg || j1 >= nv) break;
+            // the increment in FP32 (its inputs are FP32 sums), stored and summed in FP64
+            const float tp5 = a[4][jj] + a[5][jj] + a[6][jj];
+            const double d0 = sf * (4.75f * a[0][jj] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0][jj]);
+            const double d1 = 12.f * sf * a[1][jj], d2 = 12.f * sf * a[2][jj], d3 = 12.f * sf * a[3][jj];
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
             double *o = Inc + kt * 5 * Bp + c;
             o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
@@ -1304,12 +1328,14 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
                       double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
                       const float *cf, const double *lam4, float2 *const *q32) {
-    const size_t ts = sizeof(float2) * 3 * N * nv, zsm = sizeof(float2) * kPj1Pen * 5 * N * 32;
+    const size_t ts = sizeof(float2) * 3 * N * nv;
+    if (nv > kPj1Groups * kPj1Max) return cudaErrorInvalidValue;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_pj3<N, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj3<N, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
-    if ((e = cudaFuncSetAttribute(k_pj1<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ts + zsm)))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj1<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
+    if ((e = cudaFuncSetAttribute(k_pj1<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if (q32)
         k_pj3<N, float2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(
             q32[0], q32[1], q32[2], q32[3], nu, rates.nu, tfac, nv, Bp, Y, cf, lam4);
@@ -1317,8 +1343,13 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
         k_pj3<N, double2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac,
                                                                                 nv, Bp, Y, cf, lam4);
     k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
-    k_pj1<N><<<dim3((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32), 32 * kPj1Warps, ts + zsm, st>>>(
-        Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv), Inc, part);
+    const dim3 g1((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32);
+    if (nv % 2 == 0)
+        k_pj1<N, true><<<g1, 32 * kPj1Warps, ts, st>>>(Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv),
+                                                      Inc, part);
+    else
+        k_pj1<N, false><<<g1, 32 * kPj1Warps, ts, st>>>(Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv),
+                                                       Inc, part);
     return cudaGetLastError();
 }
 
