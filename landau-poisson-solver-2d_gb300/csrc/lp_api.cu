@@ -103,9 +103,9 @@ struct lp_ctx {
         double *seg = nullptr;     // states of one checkpoint segment
         int seg_len = 0;
     } adj;
-    // captured step
-    cudaGraphExec_t gexec = nullptr;
-    cudaStream_t gstream = nullptr;
+    // captured step, and captured collision step of all collided cells
+    cudaGraphExec_t gexec = nullptr, cgexec = nullptr;
+    cudaStream_t gstream = nullptr, cgstream = nullptr;
 };
 
 namespace {
@@ -763,6 +763,7 @@ void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> 
 void destroy(lp_ctx *c) {
     if (!c) return;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->cgexec) cudaGraphExecDestroy(c->cgexec);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -1256,7 +1257,23 @@ lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
     if (cell_begin == -1 && cell_end == -1) { cell_begin = 0; cell_end = c->T.ncollide; }
     if (cell_begin < 0 || cell_end > c->T.ncollide || cell_begin > cell_end)
         return fail(c, LP_ERR_INVALID, "bad cell range");
-    return collide(c, cell_begin, cell_end);
+    if (cell_begin != 0 || cell_end != c->T.ncollide || cell_end == 0) return collide(c, cell_begin, cell_end);
+    // all collided cells: one captured graph, replayed
+    if (!c->cgexec || c->cgstream != c->stream) {
+        if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        LP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        lp_status s = collide(c, 0, c->T.ncollide);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->cgexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+        c->cgstream = c->stream;
+    }
+    LP_CUDA(cudaGraphLaunch(c->cgexec, c->stream));
+    return LP_OK;
 }
 
 lp_status lp_step(lp_ctx *c, int nsteps) {
@@ -2032,6 +2049,7 @@ lp_status lp_autotune(lp_ctx *c, int reps, const char *cache_path, int *pass_cel
         write_tune_cache(cache_path, lines);
     }
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }  // recapture with the new schedule
+    if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
     if (pass_cells) *pass_cells = c->Bpass;
     if (line_warps) *line_warps = c->line_warps;
     return LP_OK;
@@ -2048,6 +2066,7 @@ lp_status lp_set_schedule(lp_ctx *c, int pass_cells, int line_warps) {
     c->Bpass = pass_cells;
     c->line_warps = line_warps;
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
     return LP_OK;
 }
 
