@@ -38,4 +38,25 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
+// FP64 <-> FP32 conversions by bit manipulation, so that the stage copies of
+// the mixed path do not occupy the narrow FP64 unit: FP64 -> FP32 truncates
+// toward zero (within one FP32 ulp) and flushes magnitudes below the FP32
+// normal range to signed zero; FP32 -> FP64 is exact for normal numbers and
+// zero (FP32 subnormals become signed zero).
+__device__ __forceinline__ float f64_to_f32_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned u = __float_as_uint(f), sign = u & 0x80000000u, e = (u >> 23) & 0xffu;
+    if (e == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
+    const unsigned long long ee = e == 255 ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double(
+        (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 }  // namespace lp

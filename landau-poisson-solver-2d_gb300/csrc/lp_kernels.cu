@@ -645,7 +645,11 @@ __global__ void k_cons_partial(const QT *__restrict__ q, const double *__restric
 #pragma unroll 4
     for (int pt = p0 + y; pt < p1; pt += 8) {
         const QT w = q[(long long)pt * Bp + c];
-        const double2 v = make_double2((double)w.x, (double)w.y);
+        double2 v;
+        if constexpr (std::is_same<QT, float2>::value)  // exact for normal numbers, off the FP64 pipe
+            v = make_double2(f32_to_f64_bits(w.x), f32_to_f64_bits(w.y));
+        else
+            v = make_double2((double)w.x, (double)w.y);
         t0 += v.x * c1[pt];
         t1 += v.y * c2[n3 + pt];
         t2 += v.y * c2[2 * n3 + pt];
@@ -1294,8 +1298,10 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
             if (jj >= jg || j1 >= nv) break;
             // the increment in FP32 (its inputs are FP32 sums), stored and summed in FP64
             const float tp5 = a[4][jj] + a[5][jj] + a[6][jj];
-            const double d0 = sf * (4.75f * a[0][jj] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0][jj]);
-            const double d1 = 12.f * sf * a[1][jj], d2 = 12.f * sf * a[2][jj], d3 = 12.f * sf * a[3][jj];
+            const double d0 = f32_to_f64_bits(sf * (4.75f * a[0][jj] - 15.f * tp5)),
+                         d4 = f32_to_f64_bits(sf * (60.f * tp5 - 15.f * a[0][jj]));
+            const double d1 = f32_to_f64_bits(12.f * sf * a[1][jj]), d2 = f32_to_f64_bits(12.f * sf * a[2][jj]),
+                         d3 = f32_to_f64_bits(12.f * sf * a[3][jj]);
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
             double *o = Inc + kt * 5 * Bp + c;
             o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
@@ -1674,26 +1680,6 @@ __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, int npar
     }
 }
 
-// FP64 <-> FP32 conversions by bit manipulation, so that the stage copies of
-// the mixed path do not occupy the narrow FP64 unit: FP64 -> FP32 truncates
-// toward zero (within one FP32 ulp) and flushes magnitudes below the FP32
-// normal range to signed zero; FP32 -> FP64 is exact for normal numbers and
-// zero (FP32 subnormals become signed zero).
-__device__ __forceinline__ float f64_to_f32_bits(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
-}
-__device__ __forceinline__ double f32_to_f64_bits(float f) {
-    const unsigned u = __float_as_uint(f), sign = u & 0x80000000u, e = (u >> 23) & 0xffu;
-    if (e == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
-    const unsigned long long ee = e == 255 ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
-    return __longlong_as_double(
-        (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
-}
 
 // ---------------------------------------------------------------- advection
 // Right-hand side H of record k (I1, I2, I3, I5 at A:213-405 combined as at
