@@ -1392,8 +1392,12 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ 
     }
     __syncthreads();
     const int kt = kt0 + lane, j3 = kt % nv, j2 = (kt / nv) % nv, j1 = kt / (nv * nv);
-    const double G[3] = {-lv + (j1 + 0.5) * dv, -lv + (j2 + 0.5) * dv, -lv + (j3 + 0.5) * dv};
-    const double g2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+    // the correction Phi^T lambda in FP32: it is ~1e-7 of the increment, so
+    // its rounding moves the moments by ~1e-15 of the increment's
+    const float fdv = (float)dv, flv = (float)lv;
+    const float G[3] = {-flv + (j1 + 0.5f) * fdv, -flv + (j2 + 0.5f) * fdv, -flv + (j3 + 0.5f) * fdv};
+    const float g2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+    const float dv12 = (float)mr.dv12, dv6 = (float)mr.dv6, dv2q = (float)mr.dv2q, c19 = (float)mr.c19;
     // one cell per warp pass: its nrec records are 7 nrec contiguous doubles of U
     for (int cc = w; cc < 32 && cb + cc < B; cc += 8) {
         double *ug = U + 7 * ((long long)(c0 + cb + cc) * nv3 + kt0);
@@ -1410,12 +1414,14 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ 
         if (lane < nrec) {
             double a[5] = {S[lane][0][cc], S[lane][1][cc], S[lane][2][cc], S[lane][3][cc], S[lane][4][cc]};
             if (lam) {  // Phi^T lambda (mom_correct with the cell centre of this lane's record)
-                const double *l = L[cc];
-                a[0] += l[0] + G[0] * l[1] + G[1] * l[2] + G[2] * l[3] + (g2 + mr.dv2q) * l[4];
-                a[1] += mr.dv12 * l[1] + mr.dv6 * G[0] * l[4];
-                a[2] += mr.dv12 * l[2] + mr.dv6 * G[1] * l[4];
-                a[3] += mr.dv12 * l[3] + mr.dv6 * G[2] * l[4];
-                a[4] += 0.25 * l[0] + 0.25 * (G[0] * l[1] + G[1] * l[2] + G[2] * l[3]) + (mr.c19 + 0.25 * g2) * l[4];
+                const float l0 = (float)L[cc][0], l1 = (float)L[cc][1], l2 = (float)L[cc][2], l3 = (float)L[cc][3],
+                            l4 = (float)L[cc][4];
+                const float gl = G[0] * l1 + G[1] * l2 + G[2] * l3;
+                a[0] += f32_to_f64_bits(l0 + gl + (g2 + dv2q) * l4);
+                a[1] += f32_to_f64_bits(dv12 * l1 + dv6 * G[0] * l4);
+                a[2] += f32_to_f64_bits(dv12 * l2 + dv6 * G[1] * l4);
+                a[3] += f32_to_f64_bits(dv12 * l3 + dv6 * G[2] * l4);
+                a[4] += f32_to_f64_bits(0.25f * l0 + 0.25f * gl + (c19 + 0.25f * g2) * l4);
             }
             double *u = ut + 7 * lane;
             u[0] += a[0]; u[3] += a[1]; u[4] += a[2]; u[5] += a[3]; u[6] += a[4];
