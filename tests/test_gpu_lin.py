@@ -70,3 +70,30 @@ def test_mixed_vs_fp64(gpu_lib):
     a.step(2)
     b.step(2)
     assert rel(a.get_state(), b.get_state()) < 1e-6
+
+
+def test_mixed_vs_fp64_convolution_form(gpu_lib):
+    """n = 16: the quadratic term in the convolution form (the default), the
+    linear term by its window contraction; mass and energy conserved."""
+    lp = gpu_lib
+    case = Case(nx1=4, nx2=1, nv=8, n=16, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.3, k_wave=0.5,
+                linear_ei=1)
+    a = _ctx(lp, case, FIX_DEFAULT, lp.PREC_MIXED)
+    b = _ctx(lp, case, FIX_DEFAULT, lp.PREC_FP64)
+    a.set_init(1)
+    assert a.autotune(reps=1)[1] in (0, 2, 4)
+    a.set_schedule(32, 0)
+    a.set_init(1)
+    b.set_init(1)
+    m0 = a.moments()
+    a.step(2)
+    b.step(2)
+    assert rel(a.get_state(), b.get_state()) < 1e-6
+    a2 = _ctx(lp, case, FIX_DEFAULT, lp.PREC_MIXED)
+    a2.set_schedule(32, 0)
+    a2.set_init(1)
+    a2.collision_step()
+    m1 = a2.moments()
+    assert abs(m1[0] - m0[0]) / abs(m0[0]) < 1e-12
+    assert abs(m1[4] - m0[4]) / abs(m0[4]) < 1e-12
+
