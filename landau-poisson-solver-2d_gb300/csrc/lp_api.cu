@@ -481,15 +481,17 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp, bool lazy 
     const lp::Tables &T = c->T;
     const R *M = (const R *)c->mfwd, *Mi = (const R *)c->minv;
     for (int s = 0; s < 3; ++s) {
-        if (f32)
-            LP_CUDA(lp::launch_fs_stage32(c->qf[s], (float2 *)c->t1, (float2 *)c->t2, (const float *)Mi, T.n, Bp, s,
-                                          T.prm.dt, T.prm.nu, (const float *)c->f, (float *)c->qn, (float *)c->f1,
-                                          c->stream, rates_at(c, c0), c->cf, c->lam4 + s * 5 * Bp));
-        else
+        if (f32) {
+            LP_CUDA(lp::launch_fs_fwd32(c->qf[s], (float2 *)c->t1, (float2 *)c->t2, (float2 *)c->F,
+                                        (const float *)Mi, (const float *)M, T.n, Bp, s, T.prm.dt, T.prm.nu,
+                                        (const float *)c->f, (float *)c->qn, (float *)c->f1, c->stream,
+                                        rates_at(c, c0), c->cf, c->lam4 + s * 5 * Bp));
+        } else {
             LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
                                            (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0),
                                            lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr));
-        LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
+            LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
+        }
         LP_TRY(stage_q<R>(c, Bp, c->q[s + 1], lazy ? s + 1 : -1, f32 ? c->qf[s + 1] : nullptr));
     }
     return LP_OK;

@@ -57,6 +57,14 @@ cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2
 cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const float *M, int n, int Bp, int stage,
                               double dt, double nu, const float *f, float *qn, float *f1, cudaStream_t st,
                               Rates rates, const float *cf, const double *lamc);
+// One FP32 RK4 stage from its mode array to the next transformed node values
+// F: the inverse transform, the node-value stage and the forward transform,
+// with the last inverse and first forward passes (both along the slowest
+// axis) fused so that the stage's node values stay on chip (n <= 24; other n
+// run the two transforms in turn through f1).
+cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, const float *Mi, const float *M,
+                            int n, int Bp, int stage, double dt, double nu, const float *f, float *qn, float *f1,
+                            cudaStream_t st, Rates rates, const float *cf, const double *lamc);
 
 // Inverse transform FS of q, full complex output (for the reference-shaped FS).
 template <typename R>
