@@ -31,6 +31,10 @@ struct lp_ctx {
     unsigned char *rzero = nullptr, *gate = nullptr;
     int *nodecell = nullptr, *pair_off = nullptr, *ipiv = nullptr;
     void *tfac = nullptr, *mfwd = nullptr, *minv = nullptr;  // R precision
+    // the FP32 per-axis transforms as register FFTs (mixed path): the
+    // matrices' factors, forward and inverse; null when they do not apply
+    lp::DftFac dfac[2]{};
+    const lp::DftFac *dff = nullptr, *dfi = nullptr;
     void *P = nullptr;                                       // R precision
     unsigned *PI = nullptr;
     float *LW = nullptr;            // line-tiled weight table (mixed path)
@@ -223,6 +227,20 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
     LP_TRY(upload_real<R>(c, &c->tfac, T.tfac));
     LP_TRY(upload_real<R>(c, &c->mfwd, T.mfwd));
     LP_TRY(upload_real<R>(c, &c->minv, T.minv));
+    if (c->mixed && T.dft_fac_ok && (T.n == 8 || T.n == 16 || T.n == 24 || T.n == 32)) {
+        for (int d = 0; d < 2; ++d) {
+            lp::DftFac &D = c->dfac[d];
+            D.n = T.n;
+            D.sign = d == 0 ? -1 : 1;
+            for (int i = 0; i < T.n; ++i) {
+                D.pre[i] = make_float2((float)T.dpre[d][2 * i], (float)T.dpre[d][2 * i + 1]);
+                D.post[i] = make_float2((float)T.dpost[d][2 * i], (float)T.dpost[d][2 * i + 1]);
+                D.w[i] = make_float2((float)T.dw[d][2 * i], (float)T.dw[d][2 * i + 1]);
+            }
+        }
+        c->dff = &c->dfac[0];
+        c->dfi = &c->dfac[1];
+    }
     if (c->mixed && lp::lines_supported(T.n)) {
         std::vector<long long> off;
         const long long nw = lp::lines_table_floats(T.n, off);
@@ -485,12 +503,12 @@ template <typename R> lp_status rk4_stages(lp_ctx *c, int c0, int Bp, bool lazy 
             LP_CUDA(lp::launch_fs_fwd32(c->qf[s], (float2 *)c->t1, (float2 *)c->t2, (float2 *)c->F,
                                         (const float *)Mi, (const float *)M, T.n, Bp, s, T.prm.dt, T.prm.nu,
                                         (const float *)c->f, (float *)c->qn, (float *)c->f1, c->stream,
-                                        rates_at(c, c0), c->cf, c->lam4 + s * 5 * Bp));
+                                        rates_at(c, c0), c->cf, c->lam4 + s * 5 * Bp, c->dfi, c->dff));
         } else {
             LP_CUDA(lp::launch_fs_stage<R>(c->q[s], (C *)c->t1, (C *)c->t2, Mi, T.n, Bp, s, T.prm.dt, T.prm.nu,
                                            (const R *)c->f, (R *)c->qn, (R *)c->f1, c->stream, rates_at(c, c0),
-                                           lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr));
-            LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream));
+                                           lazy ? c->cf : nullptr, lazy ? c->lam4 + s * 5 * Bp : nullptr, c->dfi));
+            LP_CUDA(lp::launch_fwd<R>((const R *)c->f1, (C *)c->t1, (C *)c->F, M, T.n, Bp, c->stream, c->dff));
         }
         LP_TRY(stage_q<R>(c, Bp, c->q[s + 1], lazy ? s + 1 : -1, f32 ? c->qf[s + 1] : nullptr));
     }
@@ -578,7 +596,8 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
-    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
+    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream,
+                              c->dff));
     const bool lazy = lazy_cons(c);
     // FP32 mode arrays: the convolution form's output is FP32-accurate
     const bool f32 = lazy && c->FQC && c->line_warps == 0 && c->qf[0];
@@ -598,7 +617,8 @@ template <typename R> lp_status collide_batch_prefix(lp_ctx *c, int c0, int B) {
     const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
     LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
                                 c->stream));
-    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream));
+    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream,
+                              c->dff));
     LP_TRY(stage_q<R>(c, Bp, c->q[0]));
     LP_TRY(rk4_stages<R>(c, c0, Bp));
     return LP_OK;
@@ -1314,7 +1334,7 @@ lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
         switch (which) {
         case 0: return c->mixed ? contract<float>(c, Bp, c->q[1]) : contract<double>(c, Bp, c->q[1]);
         case 1:
-            if (c->mixed) LP_CUDA(lp::launch_fwd<float>((const float *)c->f, (float2 *)c->t1, (float2 *)c->F, (const float *)c->mfwd, T.n, Bp, c->stream));
+            if (c->mixed) LP_CUDA(lp::launch_fwd<float>((const float *)c->f, (float2 *)c->t1, (float2 *)c->F, (const float *)c->mfwd, T.n, Bp, c->stream, c->dff));
             else LP_CUDA(lp::launch_fwd<double>((const double *)c->f, (double2 *)c->t1, (double2 *)c->F, (const double *)c->mfwd, T.n, Bp, c->stream));
             return LP_OK;
         case 2:

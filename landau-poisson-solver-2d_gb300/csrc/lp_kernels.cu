@@ -543,6 +543,217 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftf_fs(const float2 *__restri
     for (int aa = 0; aa < NO; ++aa) out[base + (long long)(og * NO + aa) * stride] = up2(A[aa]);
 }
 
+// ---------------------------------------------------------------- register FFTs
+// Length-N DFTs y[a] = sum_i r^(a i) x[i], r = exp(S 2 pi i / N), S = -1
+// (forward) or +1 (inverse), on a register array: radices 2, 3, 4 and 8 in
+// closed form and Cooley-Tukey N = N1 N2 (N1-point DFTs over the strided
+// inputs, twiddles r^(a1 i2) from the factor table, N2-point DFTs) for
+// N = 16 (4 x 4), 24 (3 x 8), 32 (4 x 8).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// z * (S i)
+template <int S> __device__ __forceinline__ float2 mul_si(float2 z) {
+    return S > 0 ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x);
+}
+
+template <int S> __device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+template <int S> __device__ __forceinline__ void dft3(float2 &a, float2 &b, float2 &c) {
+    constexpr float h3 = 0.8660254037844386f;  // sqrt(3) / 2
+    const float2 t = cadd(b, c), d = mul_si<S>(csub(b, c));
+    const float2 m = make_float2(a.x - 0.5f * t.x, a.y - 0.5f * t.y);
+    a = cadd(a, t);
+    b = make_float2(m.x + h3 * d.x, m.y + h3 * d.y);
+    c = make_float2(m.x - h3 * d.x, m.y - h3 * d.y);
+}
+template <int S> __device__ __forceinline__ void dft4(float2 &a, float2 &b, float2 &c, float2 &d) {
+    const float2 a0 = cadd(a, c), a1 = csub(a, c), b0 = cadd(b, d), b1 = mul_si<S>(csub(b, d));
+    a = cadd(a0, b0);
+    b = cadd(a1, b1);
+    c = csub(a0, b0);
+    d = csub(a1, b1);
+}
+template <int S> __device__ __forceinline__ void dft8(float2 (&v)[8]) {
+    constexpr float r2 = 0.7071067811865476f;  // 1 / sqrt(2)
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<S>(e0, e1, e2, e3);
+    dft4<S>(o0, o1, o2, o3);
+    // o_k * r^k, r = exp(S 2 pi i / 8)
+    const float2 s1 = cadd(o1, mul_si<S>(o1)), s3 = csub(mul_si<S>(o3), o3);
+    o1 = make_float2(r2 * s1.x, r2 * s1.y);
+    o2 = mul_si<S>(o2);
+    o3 = make_float2(r2 * s3.x, r2 * s3.y);
+    v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+template <int K, int S> __device__ __forceinline__ void dft_small(float2 (&v)[K]) {
+    if constexpr (K == 2) dft2<S>(v[0], v[1]);
+    else if constexpr (K == 3) dft3<S>(v[0], v[1], v[2]);
+    else if constexpr (K == 4) dft4<S>(v[0], v[1], v[2], v[3]);
+    else dft8<S>(v);
+}
+template <int N> struct FftPlan;
+template <> struct FftPlan<8> { static constexpr int N1 = 8, N2 = 1; };
+template <> struct FftPlan<16> { static constexpr int N1 = 4, N2 = 4; };
+template <> struct FftPlan<24> { static constexpr int N1 = 3, N2 = 8; };
+template <> struct FftPlan<32> { static constexpr int N1 = 4, N2 = 8; };
+
+// w: the factor table's roots, w[k] = exp(S 2 pi i k / N)
+template <int N, int S> __device__ __forceinline__ void fft_reg(float2 (&x)[N], const float2 *w) {
+    constexpr int N1 = FftPlan<N>::N1, N2 = FftPlan<N>::N2;
+    if constexpr (N2 == 1) {
+        dft_small<N1, S>(x);
+    } else {
+        float2 z[N];  // z[a1 N2 + i2]
+#pragma unroll
+        for (int i2 = 0; i2 < N2; ++i2) {
+            float2 v[N1];
+#pragma unroll
+            for (int i1 = 0; i1 < N1; ++i1) v[i1] = x[N2 * i1 + i2];
+            dft_small<N1, S>(v);
+#pragma unroll
+            for (int a1 = 0; a1 < N1; ++a1) z[a1 * N2 + i2] = (a1 * i2) % N ? cmulf(v[a1], w[(a1 * i2) % N]) : v[a1];
+        }
+#pragma unroll
+        for (int a1 = 0; a1 < N1; ++a1) {
+            float2 v[N2];
+#pragma unroll
+            for (int i2 = 0; i2 < N2; ++i2) v[i2] = z[a1 * N2 + i2];
+            dft_small<N2, S>(v);
+#pragma unroll
+            for (int a2 = 0; a2 < N2; ++a2) x[a1 + N1 * a2] = v[a2];
+        }
+    }
+}
+
+// The FP32 pass of k_dftf as a register FFT: one thread per (pencil, cell)
+// holds the pencil, multiplies by pre, transforms and multiplies by post.
+template <typename TIn, int OUT, int N, int S, int PY>
+__global__ void __launch_bounds__(32 * PY) k_fftf(const TIn *__restrict__ in, float2 *__restrict__ out,
+                                                  const __grid_constant__ DftFac fac, int ax, int Bp, int stage,
+                                                  float dt, float nu, const float *__restrict__ f,
+                                                  float *__restrict__ qn, float *__restrict__ f1,
+                                                  const double *__restrict__ cnu, const double *__restrict__ cdt,
+                                                  const float *__restrict__ cf, const double *__restrict__ lamc) {
+    __shared__ float cfs[PY][5][N];
+    if (cf) {
+        constexpr int n3 = N * N * N;
+        for (int t = threadIdx.y * 32 + threadIdx.x; t < PY * 5 * N; t += 32 * PY) {
+            const int pp = t / (5 * N), r = (t / N) % 5, i = t % N, p0 = blockIdx.x * PY + pp;
+            cfs[pp][r][i] = p0 < N * N ? cf[r * n3 + p0 * N + i] : 0.f;
+        }
+        __syncthreads();
+    }
+    const int pid = blockIdx.x * PY + threadIdx.y;
+    if (pid >= N * N) return;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    long long base, stride;
+    if (ax == 2) { base = (long long)pid * N * Bp; stride = Bp; }
+    else if (ax == 1) { const int i0 = pid / N, i2 = pid % N; base = ((long long)i0 * N * N + i2) * Bp; stride = (long long)N * Bp; }
+    else { base = (long long)pid * Bp; stride = (long long)N * N * Bp; }
+    base += c;
+    float2 x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if constexpr (std::is_same<TIn, double2>::value) x[i] = ld2c<float>(in + base + i * stride);
+        else x[i] = ld2<float>(in + base + i * stride);
+    }
+    if (cf) {
+        const float l0 = (float)lamc[c], l1 = (float)lamc[Bp + c], l2 = (float)lamc[2 * Bp + c],
+                    l3 = (float)lamc[3 * Bp + c], l4 = (float)lamc[4 * Bp + c];
+        const float(*r)[N] = cfs[threadIdx.y];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            x[i].x -= r[0][i] * l0 + r[4][i] * l4;
+            x[i].y -= r[1][i] * l1 + r[2][i] * l2 + r[3][i] * l3;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if constexpr (std::is_same<TIn, float>::value) x[i] = make_float2(x[i].x * fac.pre[i].x, x[i].x * fac.pre[i].y);
+        else x[i] = cmulf(x[i], fac.pre[i]);
+    }
+    fft_reg<N, S>(x, fac.w);
+    float dtc = dt, nuc = nu;
+    if (OUT == 1 && cnu) { nuc = (float)cnu[c]; dtc = (float)cdt[c]; }
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+        const long long o = base + (long long)a * stride;
+        if constexpr (OUT == 0) {
+            out[o] = cmulf(x[a], fac.post[a]);
+        } else {
+            // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
+            const float sr = x[a].x * fac.post[a].x - x[a].y * fac.post[a].y;
+            if (stage == 0) {
+                qn[o] = sr;
+                f1[o] = f[o] + dtc * sr * nuc;
+            } else {
+                f1[o] = f[o] + 0.5f * dtc * qn[o] * nuc + 0.5f * dtc * sr * nuc;
+            }
+        }
+    }
+}
+
+// k_dftf_fs as register FFTs: the inverse transform along axis 0, the node
+// value of the stage and its forward transform along axis 0, one thread per
+// (pencil, cell).
+template <int N, int PY>
+__global__ void __launch_bounds__(32 * PY) k_fftf_fs(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                     const __grid_constant__ DftFac fi,
+                                                     const __grid_constant__ DftFac ff, int Bp, int stage, float dt,
+                                                     float nu, const float *__restrict__ f, float *__restrict__ qn,
+                                                     const double *__restrict__ cnu, const double *__restrict__ cdt) {
+    const int pid = blockIdx.x * PY + threadIdx.y;
+    if (pid >= N * N) return;
+    const int c = blockIdx.y * 32 + threadIdx.x;
+    const long long stride = (long long)N * N * Bp, base = (long long)pid * Bp + c;
+    float2 x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = cmulf(in[base + i * stride], fi.pre[i]);
+    fft_reg<N, 1>(x, fi.w);
+    float dtc = dt, nuc = nu;
+    if (cnu) { nuc = (float)cnu[c]; dtc = (float)cdt[c]; }
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+        const long long o = base + (long long)a * stride;
+        const float sr = x[a].x * fi.post[a].x - x[a].y * fi.post[a].y;
+        float v;
+        if (stage == 0) {
+            qn[o] = sr;
+            v = f[o] + dtc * sr * nuc;
+        } else {
+            v = f[o] + 0.5f * dtc * qn[o] * nuc + 0.5f * dtc * sr * nuc;
+        }
+        x[a] = make_float2(v * ff.pre[a].x, v * ff.pre[a].y);
+    }
+    fft_reg<N, -1>(x, ff.w);
+#pragma unroll
+    for (int a = 0; a < N; ++a) out[base + (long long)a * stride] = cmulf(x[a], ff.post[a]);
+}
+
+template <typename TIn, int OUT, int N>
+cudaError_t fft_launch(const TIn *in, float2 *out, const DftFac &fac, int ax, int Bp, int stage, double dt,
+                       double nu, const float *f, float *qn, float *f1, cudaStream_t st, Rates rates,
+                       const float *cf, const double *lamc) {
+    constexpr int PY = 4;
+    dim3 grid((N * N + PY - 1) / PY, Bp / 32), block(32, PY);
+    if (fac.sign < 0)
+        k_fftf<TIn, OUT, N, -1, PY><<<grid, block, 0, st>>>(in, out, fac, ax, Bp, stage, (float)dt, (float)nu, f, qn,
+                                                             f1, rates.nu, rates.dt, cf, lamc);
+    else
+        k_fftf<TIn, OUT, N, 1, PY><<<grid, block, 0, st>>>(in, out, fac, ax, Bp, stage, (float)dt, (float)nu, f, qn,
+                                                            f1, rates.nu, rates.dt, cf, lamc);
+    return cudaGetLastError();
+}
+
 template <typename R, typename TIn, int OUT, int N>
 cudaError_t dftp_launch(const TIn *in, typename V2<R>::t *out, const R *M, int ax, int Bp, int stage, double dt,
                         double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates,
@@ -566,8 +777,20 @@ cudaError_t dftp_launch(const TIn *in, typename V2<R>::t *out, const R *M, int a
 template <typename R, typename TIn, int OUT>
 cudaError_t dft_pass(const TIn *in, typename V2<R>::t *out, const R *M, int n, int ax, int Bp, int stage,
                      double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{},
-                     const float *cf = nullptr, const double *lamc = nullptr) {
+                     const float *cf = nullptr, const double *lamc = nullptr, const DftFac *fac = nullptr) {
     using C = typename V2<R>::t;
+    if constexpr (std::is_same<R, float>::value) {
+        if (fac && fac->n == n) {
+            if (cf && ax != 2) return cudaErrorInvalidValue;
+            switch (n) {
+            case 8: return fft_launch<TIn, OUT, 8>(in, out, *fac, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+            case 16: return fft_launch<TIn, OUT, 16>(in, out, *fac, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+            case 24: return fft_launch<TIn, OUT, 24>(in, out, *fac, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+            case 32: return fft_launch<TIn, OUT, 32>(in, out, *fac, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
+            default: break;
+            }
+        }
+    }
     switch (n) {
     case 8: return dftp_launch<R, TIn, OUT, 8>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
     case 16: return dftp_launch<R, TIn, OUT, 16>(in, out, M, ax, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc);
@@ -2427,12 +2650,17 @@ cudaError_t launch_nodes(const double *U, int nv, int n, int c0, int B, int Bp, 
 
 template <typename R>
 cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, const R *M, int n, int Bp,
-                       cudaStream_t st) {
+                       cudaStream_t st, const DftFac *fac) {
     using C = typename V2<R>::t;
     cudaError_t e;
-    if ((e = dft_pass<R, R, 0>(f, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    if ((e = dft_pass<R, C, 0>(F, t1, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    return dft_pass<R, C, 0>(t1, F, M, n, 0, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st);
+    if ((e = dft_pass<R, R, 0>(f, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr, nullptr,
+                               fac)))
+        return e;
+    if ((e = dft_pass<R, C, 0>(F, t1, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr, nullptr,
+                               fac)))
+        return e;
+    return dft_pass<R, C, 0>(t1, F, M, n, 0, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr, nullptr,
+                             fac);
 }
 
 template <typename R>
@@ -2448,24 +2676,30 @@ cudaError_t launch_fwd_complex(const typename V2<R>::t *in, typename V2<R>::t *t
 template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2, const R *M, int n,
                             int Bp, int stage, double dt, double nu, const R *f, R *qn, R *f1, cudaStream_t st,
-                            Rates rates, const float *cf, const double *lamc) {
+                            Rates rates, const float *cf, const double *lamc, const DftFac *fac) {
     using C = typename V2<R>::t;
     cudaError_t e;
-    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf, lamc)))
+    if ((e = dft_pass<R, double2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf, lamc,
+                                     fac)))
         return e;
-    if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    if ((e = dft_pass<R, C, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr, nullptr,
+                               fac)))
+        return e;
+    return dft_pass<R, C, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates, nullptr, nullptr, fac);
 }
 
 cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const float *M, int n, int Bp, int stage,
                               double dt, double nu, const float *f, float *qn, float *f1, cudaStream_t st,
-                              Rates rates, const float *cf, const double *lamc) {
+                              Rates rates, const float *cf, const double *lamc, const DftFac *fac) {
     cudaError_t e;
     if ((e = dft_pass<float, float2, 0>(q, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf,
-                                        lamc)))
+                                        lamc, fac)))
         return e;
-    if ((e = dft_pass<float, float2, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    return dft_pass<float, float2, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates);
+    if ((e = dft_pass<float, float2, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr,
+                                        nullptr, fac)))
+        return e;
+    return dft_pass<float, float2, 1>(t2, nullptr, M, n, 0, Bp, stage, dt, nu, f, qn, f1, st, rates, nullptr, nullptr,
+                                      fac);
 }
 
 template <int N>
@@ -2480,8 +2714,32 @@ cudaError_t fs_fwd_launch(const float2 *in, float2 *out, const float *Mi, const 
 
 cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, const float *Mi, const float *M,
                             int n, int Bp, int stage, double dt, double nu, const float *f, float *qn, float *f1,
-                            cudaStream_t st, Rates rates, const float *cf, const double *lamc) {
+                            cudaStream_t st, Rates rates, const float *cf, const double *lamc, const DftFac *fi,
+                            const DftFac *ff) {
     cudaError_t e;
+    if (fi && ff && fi->n == n && ff->n == n && fi->sign > 0 && ff->sign < 0 &&
+        (n == 8 || n == 16 || n == 24 || n == 32)) {
+        if ((e = dft_pass<float, float2, 0>(q, t1, Mi, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf,
+                                            lamc, fi)))
+            return e;
+        if ((e = dft_pass<float, float2, 0>(t1, t2, Mi, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{},
+                                            nullptr, nullptr, fi)))
+            return e;
+        constexpr int PY = 4;
+        const dim3 grid(n * n / PY, Bp / 32), block(32, PY);
+        switch (n) {
+        case 8: k_fftf_fs<8, PY><<<grid, block, 0, st>>>(t2, t1, *fi, *ff, Bp, stage, (float)dt, (float)nu, f, qn, rates.nu, rates.dt); break;
+        case 16: k_fftf_fs<16, PY><<<grid, block, 0, st>>>(t2, t1, *fi, *ff, Bp, stage, (float)dt, (float)nu, f, qn, rates.nu, rates.dt); break;
+        case 24: k_fftf_fs<24, PY><<<grid, block, 0, st>>>(t2, t1, *fi, *ff, Bp, stage, (float)dt, (float)nu, f, qn, rates.nu, rates.dt); break;
+        default: k_fftf_fs<32, PY><<<grid, block, 0, st>>>(t2, t1, *fi, *ff, Bp, stage, (float)dt, (float)nu, f, qn, rates.nu, rates.dt); break;
+        }
+        if ((e = cudaGetLastError())) return e;
+        if ((e = dft_pass<float, float2, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{},
+                                            nullptr, nullptr, ff)))
+            return e;
+        return dft_pass<float, float2, 0>(t2, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr,
+                                          nullptr, ff);
+    }
     if (n != 8 && n != 16 && n != 24) {
         if ((e = launch_fs_stage32(q, t1, t2, Mi, n, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc))) return e;
         return launch_fwd<float>(f1, t1, F, M, n, Bp, st);
@@ -2813,12 +3071,13 @@ cudaError_t launch_moments(const double *U, long long size, long long kend, int 
 #define LP_INST(R)                                                                                              \
     template cudaError_t launch_nodes<R>(const double *, int, int, int, int, int, int, const int *,             \
                                          const double *, double, R *, cudaStream_t);                            \
-    template cudaError_t launch_fwd<R>(const R *, V2<R>::t *, V2<R>::t *, const R *, int, int, cudaStream_t);   \
+    template cudaError_t launch_fwd<R>(const R *, V2<R>::t *, V2<R>::t *, const R *, int, int, cudaStream_t,    \
+                                       const DftFac *);                                                         \
     template cudaError_t launch_fwd_complex<R>(const V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, int,   \
                                                cudaStream_t);                                                   \
     template cudaError_t launch_fs_stage<R>(const double2 *, V2<R>::t *, V2<R>::t *, const R *, int, int, int,  \
                                             double, double, const R *, R *, R *, cudaStream_t, Rates,           \
-                                            const float *, const double *);                                     \
+                                            const float *, const double *, const DftFac *);                     \
     template cudaError_t launch_fs_full<R>(const double2 *, V2<R>::t *, V2<R>::t *, V2<R>::t *, const R *, int, \
                                            int, cudaStream_t);                                                  \
     template cudaError_t launch_computeq<R>(const V2<R>::t *, const R *, const unsigned *, const int *, int,    \

@@ -29,11 +29,20 @@ cudaError_t launch_nodes(const double *U, int nv, int n, int c0, int B, int Bp, 
                          const int *nodecell, const double *nodeoff, double dv, R *f,
                          cudaStream_t st);
 
+// A per-axis transform factored as out[a] = post[a] sum_i w^((a i) mod n) pre[i] in[i]
+// (FP32, passed by value to the kernels; n <= 32).  sign -1: w = exp(-2 pi i / n),
+// the forward transform; +1: the inverse.  With one, the FP32 passes for n in
+// {8, 16, 24, 32} run as register FFTs instead of the dense matrix M.
+struct DftFac {
+    float2 pre[32], post[32], w[32];
+    int n = 0, sign = 0;
+};
+
 // Forward transform (fft3D with the phases folded into per-axis matrices):
 // real f[n^3][Bp] -> complex F.  t1 is scratch of the same size as F.
 template <typename R>
 cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, const R *M, int n,
-                       int Bp, cudaStream_t st);
+                       int Bp, cudaStream_t st, const DftFac *fac = nullptr);
 
 // Per-cell collision frequency and time step of the cells of one pass
 // (indexed by the cell's lane position 0..Bp-1); nullptr: the scalars.
@@ -52,11 +61,12 @@ template <typename R>
 cudaError_t launch_fs_stage(const double2 *q, typename V2<R>::t *t1, typename V2<R>::t *t2,
                             const R *M, int n, int Bp, int stage, double dt, double nu,
                             const R *f, R *qn, R *f1, cudaStream_t st, Rates rates = Rates{},
-                            const float *cf = nullptr, const double *lamc = nullptr);
+                            const float *cf = nullptr, const double *lamc = nullptr,
+                            const DftFac *fac = nullptr);
 // The same from an FP32 mode array (mixed path, n in {8, 16, 24, 32}).
 cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const float *M, int n, int Bp, int stage,
                               double dt, double nu, const float *f, float *qn, float *f1, cudaStream_t st,
-                              Rates rates, const float *cf, const double *lamc);
+                              Rates rates, const float *cf, const double *lamc, const DftFac *fac = nullptr);
 // One FP32 RK4 stage from its mode array to the next transformed node values
 // F: the inverse transform, the node-value stage and the forward transform,
 // with the last inverse and first forward passes (both along the slowest
@@ -64,7 +74,8 @@ cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const flo
 // run the two transforms in turn through f1).
 cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, const float *Mi, const float *M,
                             int n, int Bp, int stage, double dt, double nu, const float *f, float *qn, float *f1,
-                            cudaStream_t st, Rates rates, const float *cf, const double *lamc);
+                            cudaStream_t st, Rates rates, const float *cf, const double *lamc,
+                            const DftFac *fi = nullptr, const DftFac *ff = nullptr);
 
 // Inverse transform FS of q, full complex output (for the reference-shaped FS).
 template <typename R>

@@ -5,6 +5,7 @@
 //   S = source/SetInit_1.cpp             A = source/advection_1.cpp
 #include "lp_tables.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -525,6 +526,41 @@ static lp_status build_collision_tables(const lp_params &p, Tables &t, std::stri
             t.minv[2 * ((size_t)a * n + i)] = inv_s * std::cos(angi);
             t.minv[2 * ((size_t)a * n + i) + 1] = inv_s * std::sin(angi);
         }
+
+    // The matrices' factors: the DFT core w^(a i) between a phase (and
+    // trapezoid weight) on the input index and a phase on the output index.
+    for (int d = 0; d < 2; ++d) {
+        t.dpre[d].assign(2 * (size_t)n, 0.); t.dpost[d].assign(2 * (size_t)n, 0.); t.dw[d].assign(2 * (size_t)n, 0.);
+    }
+    for (int i = 0; i < n; ++i) {
+        const double pf = (double)i * t.L_eta * t.h_v, mf = t.scale * t.h_v * t.wt[i];
+        t.dpre[0][2 * i] = mf * std::cos(pf); t.dpre[0][2 * i + 1] = mf * std::sin(pf);
+        const double pi_ = -(double)i * t.L_v * t.h_eta;
+        t.dpre[1][2 * i] = inv_s * std::cos(pi_); t.dpre[1][2 * i + 1] = inv_s * std::sin(pi_);
+        const double of = t.L_v * t.eta[i], oi = -t.L_eta * t.v[i];
+        t.dpost[0][2 * i] = std::cos(of); t.dpost[0][2 * i + 1] = std::sin(of);
+        t.dpost[1][2 * i] = std::cos(oi); t.dpost[1][2 * i + 1] = std::sin(oi);
+        const double wk = 2.0 * t.PI * (double)i / (double)n;
+        t.dw[0][2 * i] = std::cos(wk); t.dw[0][2 * i + 1] = -std::sin(wk);
+        t.dw[1][2 * i] = std::cos(wk); t.dw[1][2 * i + 1] = std::sin(wk);
+    }
+    {
+        double dev = 0., big = 0.;
+        for (int d = 0; d < 2; ++d) {
+            const std::vector<double> &M = d == 0 ? t.mfwd : t.minv;
+            for (int a = 0; a < n; ++a)
+                for (int i = 0; i < n; ++i) {
+                    const int k = (int)(((long)a * i) % n);
+                    const double *po = &t.dpost[d][2 * a], *w = &t.dw[d][2 * k], *pr = &t.dpre[d][2 * i];
+                    const double xr = po[0] * w[0] - po[1] * w[1], xi = po[0] * w[1] + po[1] * w[0];
+                    const double yr = xr * pr[0] - xi * pr[1], yi = xr * pr[1] + xi * pr[0];
+                    const size_t o = 2 * ((size_t)a * n + i);
+                    dev = std::max(dev, std::max(std::fabs(yr - M[o]), std::fabs(yi - M[o + 1])));
+                    big = std::max(big, std::max(std::fabs(M[o]), std::fabs(M[o + 1])));
+                }
+        }
+        t.dft_fac_ok = dev <= 1e-12 * big;
+    }
 
     // Pair table offsets: for xi, the window of omega is a box symmetric under
     // omega -> xi + n/2 - omega; it has ceil(cnt/2) pairs.

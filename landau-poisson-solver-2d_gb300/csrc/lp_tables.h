@@ -44,6 +44,12 @@ struct Tables {
     std::vector<double> tfac;    // 3 x n x nv complex (T0, T1, T2)
     std::vector<double> mfwd;    // n x n complex, out index major
     std::vector<double> minv;    // n x n complex, out index major
+    // The same two matrices factored as M[a][i] = post[a] w^((a i) mod n) pre[i],
+    // w = exp(-2 pi i / n) for the forward ([0]) and its conjugate for the
+    // inverse ([1]): n complex entries each.  dft_fac_ok: the factors give
+    // the matrices back to 1e-12 of their largest entry.
+    std::vector<double> dpre[2], dpost[2], dw[2];
+    bool dft_fac_ok = false;
     std::vector<int> pair_off;   // n3 + 1 prefix offsets of the pair table
     // two-species variant: n3 + 1 prefix offsets of the window entries (the
     // linear weight table) and CCt_linear's inverse embedded in rows/columns
