@@ -462,7 +462,7 @@ template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q, int slot 
     LP_TRY(contract<R>(c, Bp, q, q32));
     if (q32) {
         LP_CUDA(lp::launch_conserve_lam(q32, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk,
-                                        c->lam4 + slot * 5 * Bp, c->stream));
+                                        c->lam4 + slot * 5 * Bp, c->stream, c->cf));
         return LP_OK;
     }
     if (c->WLin) {
