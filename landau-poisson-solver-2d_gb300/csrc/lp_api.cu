@@ -579,7 +579,7 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false, boo
     }
     LP_CUDA(lp::launch_project_inc(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const float *)c->tfac, T.n, T.nv,
                                    Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
-                                   (float2 *)c->Z, c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
+                                   (float2 *)c->Z, (float *)c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
                                    lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr, f32 ? c->qf : nullptr));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
@@ -637,7 +637,7 @@ lp_status collide(lp_ctx *c, int c0, int c1) {
             return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one batch");
         LP_TRY(c->mixed ? collide_batch<float>(c, b0, B) : collide_batch<double>(c, b0, B));
         if (fused_tail(c))
-            LP_CUDA(lp::launch_scatter_inc(c->dU, round32(B), B, c->T.nv, b0, c->U, c->mlam, c->T.dv, c->T.prm.lv,
+            LP_CUDA(lp::launch_scatter_inc((const float *)c->dU, round32(B), B, c->T.nv, b0, c->U, c->mlam, c->T.dv, c->T.prm.lv,
                                            c->stream));
         else
             LP_CUDA(lp::launch_scatter(c->dU, c->T.nv3, b0, B, c->U, c->stream, nullptr, c->T.nv, c->T.dv,

@@ -1508,7 +1508,7 @@ constexpr int kIncWarps = 4, JBI = 4;
 __global__ void __launch_bounds__(32 * kIncWarps)
     k_proj1_inc(const float2 *__restrict__ Z, const float *__restrict__ tf, int n, int nv, int Bp, int B, double dt,
                 double kfac, const double *__restrict__ cdt, double dv, double lv, MomRow mr,
-                double *__restrict__ Inc, double *__restrict__ part) {
+                float *__restrict__ Inc, double *__restrict__ part) {
     __shared__ double red[kIncWarps][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c = blockIdx.y * 32 + lane;
@@ -1553,10 +1553,13 @@ __global__ void __launch_bounds__(32 * kIncWarps)
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
             const double tp0 = a[0][jj], tp2 = a[1][jj], tp3 = a[2][jj], tp4 = a[3][jj];
             const double tp5 = (double)a[4][jj] + (double)a[5][jj] + (double)a[6][jj];
-            const double d0 = s * (4.75 * tp0 - 15. * tp5), d4 = s * (60. * tp5 - 15. * tp0);
-            const double d1 = 12. * s * tp2, d2 = 12. * s * tp3, d3 = 12. * s * tp4;
-            double *o = Inc + kt * 5 * Bp + c;
-            o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
+            // stored in FP32; the moments are those of the stored values
+            const float f0 = (float)(s * (4.75 * tp0 - 15. * tp5)), f4 = (float)(s * (60. * tp5 - 15. * tp0));
+            const float f1 = (float)(12. * s * tp2), f2 = (float)(12. * s * tp3), f3 = (float)(12. * s * tp4);
+            float *o = Inc + kt * 5 * Bp + c;
+            o[0] = f0; o[Bp] = f1; o[2 * Bp] = f2; o[3 * Bp] = f3; o[4 * Bp] = f4;
+            const double d0 = f32_to_f64_bits(f0), d1 = f32_to_f64_bits(f1), d2 = f32_to_f64_bits(f2),
+                         d3 = f32_to_f64_bits(f3), d4 = f32_to_f64_bits(f4);
             const double G1 = -lv + (j1 + 0.5) * dv, g2 = G1 * G1 + G2 * G2 + G3 * G3;
             m[0] += d0 + 0.25 * d4;
             m[1] += G1 * d0 + mr.dv12 * d1 + 0.25 * G1 * d4;
@@ -1681,6 +1684,24 @@ __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const
     }
 }
 
+// A sum of FP32 terms as an unevaluated pair hi + lo: each term enters by
+// an error-free two-sum (Knuth), a weighted term w x as the exact pair
+// (w x rounded, its FMA residual).
+struct DFSum {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x), bp = __fsub_rn(s, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
+        hi = s;
+    }
+    __device__ __forceinline__ void addw(float w, float x) {
+        const float p = __fmul_rn(w, x);
+        add(p);
+        lo = __fadd_rn(lo, fmaf(w, x, -p));
+    }
+    __device__ __forceinline__ double get() const { return f32_to_f64_bits(hi) + f32_to_f64_bits(lo); }
+};
+
 // Per (j2, j3, cell) pencil, four warps each take a group of consecutive
 // j1 outputs (an even count).  The five pencils Z0..Z4 along k1 are read
 // into registers one at a time and feed their real sums; the per-axis
@@ -1692,7 +1713,7 @@ template <int N, bool EVEN>
 __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
                                                         int nv, int Bp, int B, double dt, double kfac,
                                                         const double *__restrict__ cdt, double dv, double lv,
-                                                        MomRow mr, double *__restrict__ Inc, double *__restrict__ part) {
+                                                        MomRow mr, float *__restrict__ Inc, double *__restrict__ part) {
     extern __shared__ __align__(16) float2 Ts[];  // [3][N][nv]
     __shared__ double red[kPj1Warps][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1757,34 +1778,41 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
         }
         const float sf = (float)((cdt ? cdt[c] : dt) * kfac);
         const double G2 = -lv + (j2 + 0.5) * dv, G3 = -lv + (j3 + 0.5) * dv;
-        // running sums over this thread's j1 of d_q, G1 d_0, G1 d_4, G1 d_1,
-        // G1^2 d_0, G1^2 d_4; the moments follow from them with G2, G3
-        double S[5] = {0, 0, 0, 0, 0}, A0 = 0, A4 = 0, A1 = 0, B0 = 0, B4 = 0;
+        // Sums over this thread's j1 = j0 + jj of d_q, jj d_q (q = 0, 1, 4) and
+        // jj^2 d_q (q = 0, 4) as FP32 pairs, exact to ~2^-44 of their terms:
+        // with G1 = G10 + jj dv, sum G1 d = G10 S + dv T and
+        // sum G1^2 d = G10^2 S + 2 G10 dv T + dv^2 V follow in FP64 once.
+        DFSum S[5], T0, T1, T4, V0, V4;
 #pragma unroll
         for (int jj = 0; jj < kPj1Max; ++jj) {
             const int j1 = j0 + jj;
             if (jj >= jg || j1 >= nv) break;
-            // the increment in FP32 (its inputs are FP32 sums), stored and summed in FP64
+            // the increment in FP32 (its inputs are FP32 sums), stored in FP32
             const float tp5 = a[4][jj] + a[5][jj] + a[6][jj];
-            const double d0 = f32_to_f64_bits(sf * (4.75f * a[0][jj] - 15.f * tp5)),
-                         d4 = f32_to_f64_bits(sf * (60.f * tp5 - 15.f * a[0][jj]));
-            const double d1 = f32_to_f64_bits(12.f * sf * a[1][jj]), d2 = f32_to_f64_bits(12.f * sf * a[2][jj]),
-                         d3 = f32_to_f64_bits(12.f * sf * a[3][jj]);
+            const float d0 = sf * (4.75f * a[0][jj] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0][jj]);
+            const float d1 = 12.f * sf * a[1][jj], d2 = 12.f * sf * a[2][jj], d3 = 12.f * sf * a[3][jj];
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
-            double *o = Inc + kt * 5 * Bp + c;
+            float *o = Inc + kt * 5 * Bp + c;
             o[0] = d0; o[Bp] = d1; o[2 * Bp] = d2; o[3 * Bp] = d3; o[4 * Bp] = d4;
-            const double G1 = -lv + (j1 + 0.5) * dv, G11 = G1 * G1;
-            S[0] += d0; S[1] += d1; S[2] += d2; S[3] += d3; S[4] += d4;
-            A0 += G1 * d0; A4 += G1 * d4; A1 += G1 * d1;
-            B0 += G11 * d0; B4 += G11 * d4;
+            S[0].add(d0); S[1].add(d1); S[2].add(d2); S[3].add(d3); S[4].add(d4);
+            const float w1 = (float)jj, w2 = (float)(jj * jj);
+            T0.addw(w1, d0); T1.addw(w1, d1); T4.addw(w1, d4);
+            V0.addw(w2, d0); V4.addw(w2, d4);
         }
-        const double S04 = S[0] + 0.25 * S[4], G2233 = G2 * G2 + G3 * G3;
+        const double G10 = -lv + (j0 + 0.5) * dv, G100 = G10 * G10, dv2 = dv * dv;
+        const double S0 = S[0].get(), S1 = S[1].get(), S4 = S[4].get(), T0d = T0.get(), T1d = T1.get(),
+                     T4d = T4.get();
+        const double A0 = G10 * S0 + dv * T0d, A1 = G10 * S1 + dv * T1d, A4 = G10 * S4 + dv * T4d;
+        const double B0 = G100 * S0 + 2. * G10 * dv * T0d + dv2 * V0.get();
+        const double B4 = G100 * S4 + 2. * G10 * dv * T4d + dv2 * V4.get();
+        const double S2 = S[2].get(), S3 = S[3].get();
+        const double S04 = S0 + 0.25 * S4, G2233 = G2 * G2 + G3 * G3;
         m[0] = S04;
-        m[1] = A0 + mr.dv12 * S[1] + 0.25 * A4;
-        m[2] = G2 * S04 + mr.dv12 * S[2];
-        m[3] = G3 * S04 + mr.dv12 * S[3];
-        m[4] = B0 + (G2233 + mr.dv2q) * S[0] + mr.dv6 * (A1 + G2 * S[2] + G3 * S[3]) + mr.c19 * S[4] + 0.25 * B4 +
-               0.25 * G2233 * S[4];
+        m[1] = A0 + mr.dv12 * S1 + 0.25 * A4;
+        m[2] = G2 * S04 + mr.dv12 * S2;
+        m[3] = G3 * S04 + mr.dv12 * S3;
+        m[4] = B0 + (G2233 + mr.dv2q) * S0 + mr.dv6 * (A1 + G2 * S2 + G3 * S3) + mr.c19 * S4 + 0.25 * B4 +
+               0.25 * G2233 * S4;
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) red[w][q][lane] = m[q];
@@ -1800,7 +1828,7 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
 template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
-                      double *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
+                      float *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
                       const float *cf, const double *lam4, float2 *const *q32) {
     const size_t ts = sizeof(float2) * 3 * N * nv;
     if (nv > kPj1Groups * kPj1Max) return cudaErrorInvalidValue;
@@ -1829,7 +1857,7 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
 
 constexpr int kScatRec = 32;  // records per tile (x 32 cells)
 constexpr size_t kScatSmem = sizeof(double) * (kScatRec * 5 * 33 + 32 * 5 + 8 * 7 * kScatRec);
-__global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ Inc, int Bp, int B, int nv, int c0,
+__global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ Inc, int Bp, int B, int nv, int c0,
                                                      double *__restrict__ U, const double *__restrict__ lam,
                                                      double dv, double lv, MomRow mr) {
     extern __shared__ double ssm[];
@@ -1843,16 +1871,16 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const double *__restrict__ 
     const int cb = blockIdx.y * 32;
     // rows (record, coefficient) of 32 cells: coalesced along the cells; all
     // loads of a thread are issued before the first shared-memory store
-    double v[kScatRec * 5 / 8];
+    float v[kScatRec * 5 / 8];
 #pragma unroll
     for (int j = 0; j < kScatRec * 5 / 8; ++j) {
         const int row = w + 8 * j, r = row / 5, q = row - r * 5;
-        v[j] = (r < nrec && cb + lane < B) ? Inc[((long long)(kt0 + r) * 5 + q) * Bp + cb + lane] : 0.;
+        v[j] = (r < nrec && cb + lane < B) ? Inc[((long long)(kt0 + r) * 5 + q) * Bp + cb + lane] : 0.f;
     }
 #pragma unroll
     for (int j = 0; j < kScatRec * 5 / 8; ++j) {
         const int row = w + 8 * j, r = row / 5, q = row - r * 5;
-        S[r][q][lane] = v[j];
+        S[r][q][lane] = f32_to_f64_bits(v[j]);
     }
     if (t < 160) {
         const int cc = t / 5, q = t - cc * 5;
@@ -2962,7 +2990,7 @@ int project_inc_blocks(int n, int nv) {
 
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
-                               double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
+                               double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates, const float *cf,
                                const double *lam4, float2 *const *q32) {
     const double kfac = 1. / scalev / scaleL / scale3;
@@ -2992,7 +3020,7 @@ cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *par
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_inc(const double *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
+cudaError_t launch_scatter_inc(const float *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
                                double dv, double lv, cudaStream_t st) {
     const long long nv3 = (long long)nv * nv * nv;
     const cudaError_t e = cudaFuncSetAttribute(k_scatter_inc, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -190,14 +190,14 @@ int project_inc_blocks(int n, int nv);
 // four mode arrays are FP32 complex (q0..q3 unused).
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
-                               double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, double *Inc,
+                               double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{},
                                const float *cf = nullptr, const double *lam4 = nullptr,
                                float2 *const *q32 = nullptr);
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
-cudaError_t launch_scatter_inc(const double *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
+cudaError_t launch_scatter_inc(const float *Inc, int Bp, int B, int nv, int c0, double *U, const double *lam,
                                double dv, double lv, cudaStream_t st);
 
 // U slots {0,3,4,5,6} of cells [c0, c0+B) <- dU; with lam (the mixed path's
