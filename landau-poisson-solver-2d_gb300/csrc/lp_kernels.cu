@@ -1702,78 +1702,93 @@ struct DFSum {
     __device__ __forceinline__ double get() const { return f32_to_f64_bits(hi) + f32_to_f64_bits(lo); }
 };
 
-// Per (j2, j3, cell) pencil, four warps each take a group of consecutive
-// j1 outputs (an even count).  The five pencils Z0..Z4 along k1 are read
-// into registers one at a time and feed their real sums; the per-axis
-// factors come from shared memory, for two consecutive j1 per 16-byte load
-// when nv is even.  The 7 real sums of each j1 give the increment (see
-// k_proj1_inc), written cell-minor, and the block's moment partials.
+// Per (j2, j3, cell) pencil, four warps each take a group of JG consecutive
+// j1 outputs (JG even, 4 JG >= nv).  The block's five source pencils Z0..Z4
+// along k1 (two pencils x 32 cells) are staged in shared memory by one burst
+// of cp.async copies; for each source the sums over k1 run with packed FP32
+// FMAs, P += T(k1, j1) * z(k1) element-wise (Re (T z) = P.x - P.y), the
+// factors read for two consecutive j1 per 16-byte load when nv is even.
+// The sums of each j1 give the increment (see k_proj1_inc), written
+// cell-minor, and the block's moment partials.
 constexpr int kPj1Warps = 8, kPj1Pen = 2, kPj1Groups = kPj1Warps / kPj1Pen, kPj1Max = 8;
-template <int N, bool EVEN>
-__global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
+inline size_t pj1_smem(int N, int nv) {
+    return sizeof(float2) * ((size_t)3 * N * nv + (size_t)kPj1Pen * 5 * N * 32);
+}
+template <int N, bool EVEN, int JG, int MINB = 1>
+__global__ void __launch_bounds__(32 * kPj1Warps, MINB) k_pj1(const float2 *__restrict__ Z, const float *__restrict__ tf,
                                                         int nv, int Bp, int B, double dt, double kfac,
                                                         const double *__restrict__ cdt, double dv, double lv,
                                                         MomRow mr, float *__restrict__ Inc, double *__restrict__ part) {
-    extern __shared__ __align__(16) float2 Ts[];  // [3][N][nv]
+    extern __shared__ __align__(16) float2 Ts[];  // [3][N][nv], then the pencils [kPj1Pen][5][N][32]
+    float2 *Zs = Ts + 3 * N * nv;
     __shared__ double red[kPj1Warps][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long zs = (long long)N * nv * nv * Bp, ks = (long long)nv * nv * Bp;
+    for (int t = threadIdx.x; t < kPj1Pen * 5 * N * 16; t += 32 * kPj1Warps) {
+        const int c2 = t & 15, r = t >> 4, k = r % N, p = (r / N) % 5, q = r / (5 * N);
+        const int pq = blockIdx.x * kPj1Pen + q;
+        if (pq < nv * nv)
+            cp_async16(Zs + r * 32 + 2 * c2, Z + p * zs + k * ks + (long long)pq * Bp + blockIdx.y * 32 + 2 * c2);
+    }
+    cp_async_commit();
     for (int t = threadIdx.x; t < 3 * N * nv; t += 32 * kPj1Warps) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
+    cp_async_wait0();
     __syncthreads();
     const int pp = w / kPj1Groups, g = w - pp * kPj1Groups;
     const int pid = blockIdx.x * kPj1Pen + pp;
     const int c = blockIdx.y * 32 + lane;
-    const int jg = 2 * ((nv + 2 * kPj1Groups - 1) / (2 * kPj1Groups)), j0 = g * jg;
+    const int jg = JG, j0 = g * jg;
     double m[5] = {0, 0, 0, 0, 0};
     if (pid < nv * nv && c < B && j0 < nv) {
         const int j2 = pid / nv, j3 = pid - j2 * nv;
-        const long long zs = (long long)N * nv * nv * Bp, ks = (long long)nv * nv * Bp;
-        const float2 *zb = Z + ((long long)j2 * nv + j3) * Bp + c;
-        float a[7][kPj1Max];
-#pragma unroll
-        for (int e = 0; e < 7; ++e)
-#pragma unroll
-            for (int jj = 0; jj < kPj1Max; ++jj) a[e][jj] = 0.f;
-        // source pencil p feeds (table, sum): p = 0: (T0, 0) (T1, 1) (T2, 4); p = 1..4: (T0, 2 5 3 6)
+        const float2 *zp = Zs + pp * 5 * N * 32 + lane;
+        // a[0], a[1]: T0, T1 sums of Z0; a[2], a[3]: T0 sums of Z1, Z3;
+        // a[4]: T2 sum of Z0 plus the T0 sums of Z2 and Z4 (in that order)
+        float a[5][JG];
 #pragma unroll 1
         for (int p = 0; p < 5; ++p) {
-            float2 z[N];
+            const int ntab = p == 0 ? 3 : 1;
+            unsigned long long P[3][JG];
 #pragma unroll
-            for (int k = 0; k < N; ++k) z[k] = zb[p * zs + k * ks];
-            const int e0 = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 5 : (p == 3 ? 3 : 6)));
+            for (int tb = 0; tb < 3; ++tb)
 #pragma unroll
-            for (int jj = 0; jj < kPj1Max; jj += 2) {
-                const int j1 = j0 + jj;
-                if (jj >= jg || j1 >= nv) break;
-                float s0[3] = {0.f, 0.f, 0.f}, s1[3] = {0.f, 0.f, 0.f};
-                const int ntab = p == 0 ? 3 : 1;
+                for (int jj = 0; jj < JG; ++jj) P[tb][jj] = 0ull;
 #pragma unroll
-                for (int k = 0; k < N; ++k) {
+            for (int k = 0; k < N; ++k) {
+                const float2 zk = zp[(p * N + k) * 32];
+                const unsigned long long zv = pk2(zk.x, zk.y);
 #pragma unroll
-                    for (int tb = 0; tb < 3; ++tb) {
-                        if (tb >= ntab) break;
+                for (int tb = 0; tb < 3; ++tb) {
+                    if (tb >= ntab) break;
+#pragma unroll
+                    for (int jj = 0; jj < JG; jj += 2) {
+                        const int j1 = j0 + jj;
                         const float2 *T = Ts + tb * N * nv + k * nv + j1;
-                        float2 t0, t1;
                         if constexpr (EVEN) {
-                            const float4 tt = *reinterpret_cast<const float4 *>(T);
-                            t0 = make_float2(tt.x, tt.y);
-                            t1 = make_float2(tt.z, tt.w);
+                            const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(T);
+                            P[tb][jj] = fma2(tt.x, zv, P[tb][jj]);
+                            P[tb][jj + 1] = fma2(tt.y, zv, P[tb][jj + 1]);
                         } else {
-                            t0 = T[0];
-                            t1 = (j1 + 1 < nv) ? T[1] : make_float2(0.f, 0.f);
+                            const float2 t0 = j1 < nv ? T[0] : make_float2(0.f, 0.f);
+                            const float2 t1 = j1 + 1 < nv ? T[1] : make_float2(0.f, 0.f);
+                            P[tb][jj] = fma2(pk2(t0.x, t0.y), zv, P[tb][jj]);
+                            P[tb][jj + 1] = fma2(pk2(t1.x, t1.y), zv, P[tb][jj + 1]);
                         }
-                        s0[tb] += t0.x * z[k].x - t0.y * z[k].y;
-                        s1[tb] += t1.x * z[k].x - t1.y * z[k].y;
                     }
                 }
-                if (p == 0) {
-                    a[0][jj] = s0[0]; a[0][jj + 1] = s1[0];
-                    a[1][jj] = s0[1]; a[1][jj + 1] = s1[1];
-                    a[4][jj] = s0[2]; a[4][jj + 1] = s1[2];
-                } else {
+            }
 #pragma unroll
-                    for (int e = 2; e < 7; ++e)
-                        if (e == e0 && e != 4) { a[e][jj] = s0[0]; a[e][jj + 1] = s1[0]; }
+            for (int jj = 0; jj < JG; ++jj) {
+                float v[3];
+#pragma unroll
+                for (int tb = 0; tb < 3; ++tb) {
+                    const float2 pv = up2(P[tb][jj]);
+                    v[tb] = pv.x - pv.y;
                 }
+                if (p == 0) { a[0][jj] = v[0]; a[1][jj] = v[1]; a[4][jj] = v[2]; }
+                else if (p == 1) a[2][jj] = v[0];
+                else if (p == 3) a[3][jj] = v[0];
+                else a[4][jj] += v[0];
             }
         }
         const float sf = (float)((cdt ? cdt[c] : dt) * kfac);
@@ -1784,11 +1799,11 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
         // sum G1^2 d = G10^2 S + 2 G10 dv T + dv^2 V follow in FP64 once.
         DFSum S[5], T0, T1, T4, V0, V4;
 #pragma unroll
-        for (int jj = 0; jj < kPj1Max; ++jj) {
+        for (int jj = 0; jj < JG; ++jj) {
             const int j1 = j0 + jj;
-            if (jj >= jg || j1 >= nv) break;
+            if (j1 >= nv) break;
             // the increment in FP32 (its inputs are FP32 sums), stored in FP32
-            const float tp5 = a[4][jj] + a[5][jj] + a[6][jj];
+            const float tp5 = a[4][jj];
             const float d0 = sf * (4.75f * a[0][jj] - 15.f * tp5), d4 = sf * (60.f * tp5 - 15.f * a[0][jj]);
             const float d1 = 12.f * sf * a[1][jj], d2 = 12.f * sf * a[2][jj], d3 = 12.f * sf * a[3][jj];
             const long long kt = ((long long)j1 * nv + j2) * nv + j3;
@@ -1825,6 +1840,28 @@ __global__ void __launch_bounds__(32 * kPj1Warps) k_pj1(const float2 *__restrict
         }
 }
 
+template <int N, int JG>
+cudaError_t pj1_launch(dim3 g1, const float2 *Z, const float *tfac, int nv, int Bp, int B, double dt, double kfac,
+                       const double *cdt, double dv, double lv, float *Inc, double *part, cudaStream_t st) {
+    const size_t sm = pj1_smem(N, nv);
+    cudaError_t e;
+    // two blocks per SM (at most 128 registers) up to six outputs per thread
+    constexpr int MB = JG <= 6 ? 2 : 1;
+    if (nv % 2 == 0) {
+        if ((e = cudaFuncSetAttribute(k_pj1<N, true, JG, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
+            return e;
+        k_pj1<N, true, JG, MB><<<g1, 32 * kPj1Warps, sm, st>>>(Z, tfac, nv, Bp, B, dt, kfac, cdt, dv, lv,
+                                                               mom_row(dv), Inc, part);
+    } else {
+        if ((e = cudaFuncSetAttribute(k_pj1<N, false, JG, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm)))
+            return e;
+        k_pj1<N, false, JG, MB><<<g1, 32 * kPj1Warps, sm, st>>>(Z, tfac, nv, Bp, B, dt, kfac, cdt, dv, lv,
+                                                                mom_row(dv), Inc, part);
+    }
+    return cudaGetLastError();
+}
+
 template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
@@ -1836,8 +1873,6 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
     if ((e = cudaFuncSetAttribute(k_pj3<N, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj3<N, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
-    if ((e = cudaFuncSetAttribute(k_pj1<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
-    if ((e = cudaFuncSetAttribute(k_pj1<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if (q32)
         k_pj3<N, float2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(
             q32[0], q32[1], q32[2], q32[3], nu, rates.nu, tfac, nv, Bp, Y, cf, lam4);
@@ -1846,12 +1881,14 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
                                                                                 nv, Bp, Y, cf, lam4);
     k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
     const dim3 g1((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32);
-    if (nv % 2 == 0)
-        k_pj1<N, true><<<g1, 32 * kPj1Warps, ts, st>>>(Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv),
-                                                      Inc, part);
-    else
-        k_pj1<N, false><<<g1, 32 * kPj1Warps, ts, st>>>(Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, mom_row(dv),
-                                                       Inc, part);
+    const int jg = 2 * ((nv + 2 * kPj1Groups - 1) / (2 * kPj1Groups));
+    switch (jg) {
+    case 2: e = pj1_launch<N, 2>(g1, Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, st); break;
+    case 4: e = pj1_launch<N, 4>(g1, Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, st); break;
+    case 6: e = pj1_launch<N, 6>(g1, Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, st); break;
+    default: e = pj1_launch<N, 8>(g1, Z, tfac, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, st); break;
+    }
+    if (e) return e;
     return cudaGetLastError();
 }
 
