@@ -419,14 +419,25 @@ lp_status advect(lp_ctx *c) {
 // Mixed path: line_warps 0 selects the convolution form, 2 or 4 the
 // line-tiled weighted sum with that many warps per line.
 // q32: the convolution form writes the mode array in FP32 there.
-template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *q32 = nullptr) {
+// lam (with q32): conserveAllMoments' multipliers of the FP32 mode array,
+// [5][Bp], from the constraint sums of the convolution form's last kernel.
+template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *q32 = nullptr,
+                                         double *lam = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
     if (c->FQC && c->line_warps == 0) {
+        lp::ConsFused cons;
+        if (lam) {
+            if (!q32 || !c->cf || lp::fftq_cons_blocks(T.n) > c->nchunk)
+                return fail(c, LP_ERR_INVALID, "fused conservation sums need FP32 mode arrays");
+            cons.cf = c->cf;
+            cons.part = c->cpart;
+        }
         for (int c0 = 0; c0 < Bp; c0 += c->fq_bs)
             LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, c0,
                                             std::min(c->fq_bs, Bp - c0), c->fscr, c->fq_bs, q, c->stream, -1,
-                                            q32));
+                                            q32, lam ? &cons : nullptr));
+        if (lam) LP_CUDA(lp::launch_cons_lambda(c->cpart, lp::fftq_cons_blocks(T.n), c->cct, Bp, lam, c->stream));
         return LP_OK;
     }
     if (q32) return fail(c, LP_ERR_INVALID, "FP32 mode arrays need the convolution form");
@@ -459,12 +470,8 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *
 template <typename R> lp_status stage_q(lp_ctx *c, int Bp, double2 *q, int slot = -1, float2 *q32 = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
+    if (q32) return contract<R>(c, Bp, q, q32, c->lam4 + slot * 5 * Bp);
     LP_TRY(contract<R>(c, Bp, q, q32));
-    if (q32) {
-        LP_CUDA(lp::launch_conserve_lam(q32, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk,
-                                        c->lam4 + slot * 5 * Bp, c->stream, c->cf));
-        return LP_OK;
-    }
     if (c->WLin) {
         const long long tot = (long long)T.n3 * Bp;
         LP_CUDA(lp::launch_qlin<R>((const C *)c->F, (const R *)c->WLin, c->win_off, T.n, Bp, c->qlin, c->stream));

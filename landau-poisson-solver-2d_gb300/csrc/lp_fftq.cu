@@ -403,30 +403,60 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_z1(const float2 *__restrict__ G
 }
 
 // Z2: inverse axis-3 DFT of the (i, j) pencils into q (stride Bp), FP64
-// or FP32 complex.
-template <int N, typename QT>
+// or FP32 complex.  CONS (FP32 output): each block's constraint sums of its
+// outputs (ConsFused).
+template <int N, typename QT, bool CONS>
 __global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H, int Bs, QT *__restrict__ q,
-                                                    int Bp, int c0, FftTw tw) {
+                                                    int Bp, int c0, FftTw tw, ConsFused cons) {
     constexpr int n = N, M = 3 * N / 2;
     const int pen = blockIdx.x * kPY + threadIdx.y;
-    if (pen >= n * n) return;
     const int cell = blockIdx.y * 32 + threadIdx.x;
-    const float2 *src = H + (size_t)pen * M * Bs + cell;
-    float2 g[M], x[N];
+    float t[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (pen < n * n) {
+        const float2 *src = H + (size_t)pen * M * Bs + cell;
+        float2 g[M], x[N];
 #pragma unroll
-    for (int k = 0; k < M; ++k) g[k] = src[(size_t)k * Bs];
-    inv_pencil<N>(g, x, tw.iv);
-    QT *dst = q + (size_t)pen * n * Bp + c0 + cell;
+        for (int k = 0; k < M; ++k) g[k] = src[(size_t)k * Bs];
+        inv_pencil<N>(g, x, tw.iv);
+        QT *dst = q + (size_t)pen * n * Bp + c0 + cell;
 #pragma unroll
-    for (int k = 0; k < n; ++k) {
-        if constexpr (std::is_same<QT, double2>::value) dst[(size_t)k * Bp] = make_double2((double)x[k].x, (double)x[k].y);
-        else dst[(size_t)k * Bp] = x[k];
+        for (int k = 0; k < n; ++k) {
+            if constexpr (std::is_same<QT, double2>::value) dst[(size_t)k * Bp] = make_double2((double)x[k].x, (double)x[k].y);
+            else dst[(size_t)k * Bp] = x[k];
+        }
+        if constexpr (CONS) {
+            constexpr int n3 = N * N * N;
+            const float *cr = cons.cf + pen * n;
+#pragma unroll
+            for (int k = 0; k < n; ++k) {
+                t[0] = fmaf(x[k].x, cr[k], t[0]);
+                t[1] = fmaf(x[k].y, cr[n3 + k], t[1]);
+                t[2] = fmaf(x[k].y, cr[2 * n3 + k], t[2]);
+                t[3] = fmaf(x[k].y, cr[3 * n3 + k], t[3]);
+                t[4] = fmaf(x[k].x, cr[4 * n3 + k], t[4]);
+            }
+        }
+    }
+    if constexpr (CONS) {
+        __shared__ double red[kPY][5][32];
+        const int lane = threadIdx.x, y = threadIdx.y;
+#pragma unroll
+        for (int r = 0; r < 5; ++r) red[y][r][lane] = f32_to_f64_bits(t[r]);
+        __syncthreads();
+        if (y == 0) {
+            const long long c = c0 + cell;
+            for (int r = 0; r < 5; ++r) {
+                double s = 0.;
+                for (int yy = 0; yy < kPY; ++yy) s += red[yy][r][lane];
+                cons.part[((long long)blockIdx.x * 5 + r) * Bp + c] = s;
+            }
+        }
     }
 }
 
 template <int N>
 cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc, float2 *scratch,
-                      int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32) {
+                      int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32, const ConsFused *cons) {
     constexpr int n = N, M = 3 * N / 2;
     constexpr int NI = N;  // outputs per thread in Y (one pass: X is read once)
     float2 *G = scratch, *H = scratch + (size_t)n * M * M * Bs, *X = scratch + fftq_gh_elems(n, Bs);
@@ -457,8 +487,10 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
     }
     if (stage < 0 || stage == 3) k_fq_z1<N><<<dim3((n * M + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(G, Bs, H, tw);
     if (stage < 0 || stage == 4) {
-        if (q32) k_fq_z2<N, float2><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q32, Bp, c0, tw);
-        else k_fq_z2<N, double2><<<dim3((n * n + kPY - 1) / kPY, gc, 1), blk, 0, st>>>(H, Bs, q, Bp, c0, tw);
+        const dim3 g2((n * n + kPY - 1) / kPY, gc, 1);
+        if (q32 && cons) k_fq_z2<N, float2, true><<<g2, blk, 0, st>>>(H, Bs, q32, Bp, c0, tw, *cons);
+        else if (q32) k_fq_z2<N, float2, false><<<g2, blk, 0, st>>>(H, Bs, q32, Bp, c0, tw, ConsFused{});
+        else k_fq_z2<N, double2, false><<<g2, blk, 0, st>>>(H, Bs, q, Bp, c0, tw, ConsFused{});
     }
     return cudaGetLastError();
 }
@@ -466,6 +498,7 @@ cudaError_t launch_fq(const float2 *F, const float *C, const FftTw &tw, int Bp, 
 }  // namespace
 
 bool fftq_supported(int n) { return n == 8 || n == 16 || n == 24 || n == 32; }
+int fftq_cons_blocks(int n) { return (n * n + kPY - 1) / kPY; }
 
 size_t fftq_gh_elems(int n, int Bs) {
     const size_t M = 3 * (size_t)n / 2;
@@ -507,14 +540,16 @@ void fftq_coefficients(const double *shat, const double *ahat, const double *cw,
 }
 
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
-                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32) {
+                                float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage, float2 *q32,
+                                const ConsFused *cons) {
     if (Bc <= 0 || Bc % 32 || Bc > Bs || c0 % 32 || c0 + Bc > Bp || stage < -1 || stage > 4)
         return cudaErrorInvalidValue;
+    if (cons && (!q32 || !cons->cf || !cons->part)) return cudaErrorInvalidValue;
     switch (n) {
-    case 8: return launch_fq<8>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
-    case 16: return launch_fq<16>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
-    case 24: return launch_fq<24>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
-    case 32: return launch_fq<32>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32);
+    case 8: return launch_fq<8>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32, cons);
+    case 16: return launch_fq<16>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32, cons);
+    case 24: return launch_fq<24>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32, cons);
+    case 32: return launch_fq<32>(F, C, tw, Bp, c0, Bc, scratch, Bs, q, st, stage, q32, cons);
     default: return cudaErrorInvalidValue;
     }
 }

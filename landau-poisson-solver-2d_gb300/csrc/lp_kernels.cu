@@ -2970,6 +2970,12 @@ cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, cons
     return cudaGetLastError();
 }
 
+cudaError_t launch_cons_lambda(const double *part, int nchunk, const double *cct_inv, int Bp, double *lam,
+                               cudaStream_t st) {
+    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
                                 int Bp, double *part, int nchunk, double *lam, cudaStream_t st, const float *cf) {
     if (cf && (n3 + nchunk - 1) / nchunk <= 8 * 16)

@@ -138,9 +138,21 @@ size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
 // 3, 4 only one of them (the fused X1/X2, Y, Z1, Z2; 1 launches nothing), on
 // the scratch a full run left.  q32: the mode array is written as FP32
 // complex there instead of q.
+// conserveAllMoments' sums formed by the convolution form's last kernel as it
+// writes an FP32 mode array: each thread sums its outputs times the
+// constraint rows (cf, FP32 [5][n^3]) in FP32, each block adds its threads'
+// sums in FP64 into part[block][5][Bp] (the layout of the chunk partials of
+// launch_conserve, with fftq_cons_blocks(n) chunks).
+struct ConsFused {
+    const float *cf = nullptr;
+    double *part = nullptr;
+};
+// Blocks of the last kernel per group of 32 cells (the chunks of part).
+int fftq_cons_blocks(int n);
+
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
                                 float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1,
-                                float2 *q32 = nullptr);
+                                float2 *q32 = nullptr, const ConsFused *cons = nullptr);
 
 // Moment-conserving projection of q in place (FP64).
 // apply = false: only the multipliers lam[5][Bp] (the correction is left to
@@ -151,6 +163,9 @@ cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, cons
 // The multipliers of an FP32 mode array: FP64 sums of its exact values, or
 // with cf (the constraint rows in FP32) FP32 sums of a few products each,
 // added in FP64.
+// The multipliers lam[5][Bp] from chunk partials part[nchunk][5][Bp].
+cudaError_t launch_cons_lambda(const double *part, int nchunk, const double *cct_inv, int Bp, double *lam,
+                               cudaStream_t st);
 cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
                                 int Bp, double *part, int nchunk, double *lam, cudaStream_t st,
                                 const float *cf = nullptr);
