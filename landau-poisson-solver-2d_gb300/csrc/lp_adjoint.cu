@@ -167,7 +167,7 @@ __global__ void k_collide_out_vjp(const double *__restrict__ lout, int nv, int c
     lt[4 * nv3 * Bp] = s * lp5;
 }
 
-// Transpose of setInit_spectral (k_nodes): every DG record gathers the
+// Transpose of setInit_spectral (k_nodes_t): every DG record gathers the
 // adjoints of the spectral nodes inside its velocity cell.
 __global__ void k_nodes_vjp(const double *__restrict__ lf, int nv, int n, int c0, int B, int Bp, int slot1,
                             const int *__restrict__ nfirst, const int *__restrict__ ncount,

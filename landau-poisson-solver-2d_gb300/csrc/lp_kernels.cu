@@ -166,24 +166,37 @@ __global__ void k_qadd(double2 *__restrict__ q, const double2 *__restrict__ ql, 
 }
 
 // ---------------------------------------------------------------- nodes
-// setInit_spectral for a batch of cells, cell-minor output.
+// setInit_spectral for a batch of cells, cell-minor output
+// (n <= 32): a block takes one (l, m) node pair and 32 cells; a warp takes
+// four cells with the lanes along q, so the lanes read consecutive records of
+// one cell, and the values go out cell-minor through a shared tile.
 template <typename R>
-__global__ void k_nodes(const double *__restrict__ U, int nv, int n, int c0, int B, int Bp, int slot1,
-                        const int *__restrict__ nodecell, const double *__restrict__ nodeoff, double dv,
-                        R *__restrict__ f) {
-    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long total = (long long)n * n * n * Bp;
-    if (tid >= total) return;
-    const int c = (int)(tid % Bp);
-    const int pt = (int)(tid / Bp);
-    if (c >= B) { f[tid] = R(0); return; }
-    const int l = pt / (n * n), m = (pt / n) % n, q = pt % n;
-    const int j1 = nodecell[l], j2 = nodecell[m], j3 = nodecell[q];
-    const double *u = U + 7 * ((long long)(c0 + c) * nv * nv * nv + (j1 * nv + j2) * nv + j3);
-    // nodeoff holds (v[l] - Gridv(j)) / dv, so no division per node
-    const double a = nodeoff[l], b = nodeoff[m], e = nodeoff[q];
-    const double val = u[0] + u[slot1] * a + u[4] * b + u[5] * e + u[6] * (a * a + b * b + e * e);
-    f[tid] = (R)val;
+__global__ void __launch_bounds__(256) k_nodes_t(const double *__restrict__ U, int nv, int n, int c0, int B, int Bp,
+                                                 int slot1, const int *__restrict__ nodecell,
+                                                 const double *__restrict__ nodeoff, R *__restrict__ f) {
+    __shared__ R tile[32][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lm = blockIdx.x, l = lm / n, m = lm - l * n, cb = blockIdx.y * 32;
+    const int j1 = nodecell[l], j2 = nodecell[m];
+    const double a = nodeoff[l], b = nodeoff[m];
+    const int q = lane < n ? lane : n - 1;
+    const int j3 = nodecell[q];
+    const double e = nodeoff[q];
+    const long long nv3 = (long long)nv * nv * nv, rec = (j1 * nv + j2) * nv + j3;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int cc = w + 8 * i;
+        R v = R(0);
+        if (cb + cc < B) {
+            const double *u = U + 7 * ((long long)(c0 + cb + cc) * nv3 + rec);
+            const double val = u[0] + u[slot1] * a + u[4] * b + u[5] * e + u[6] * (a * a + b * b + e * e);
+            v = (R)val;
+        }
+        tile[lane][cc] = v;
+    }
+    __syncthreads();
+    R *out = f + (long long)lm * n * Bp + cb + lane;
+    for (int qq = w; qq < n; qq += 8) out[(long long)qq * Bp] = tile[qq][lane];
 }
 
 // ---------------------------------------------------------------- DFT pass
@@ -2738,8 +2751,8 @@ cudaError_t launch_pairs(const double *eta, const double *shat, const double *ah
 template <typename R>
 cudaError_t launch_nodes(const double *U, int nv, int n, int c0, int B, int Bp, int slot1, const int *nodecell,
                          const double *nodeoff, double dv, R *f, cudaStream_t st) {
-    const long long total = (long long)n * n * n * Bp;
-    k_nodes<R><<<grid1(total, 256), 256, 0, st>>>(U, nv, n, c0, B, Bp, slot1, nodecell, nodeoff, dv, f);
+    if (n > 32) return cudaErrorInvalidValue;
+    k_nodes_t<R><<<dim3(n * n, Bp / 32), 256, 0, st>>>(U, nv, n, c0, B, Bp, slot1, nodecell, nodeoff, f);
     return cudaGetLastError();
 }
 
