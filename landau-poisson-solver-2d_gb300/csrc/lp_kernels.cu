@@ -752,6 +752,105 @@ __global__ void __launch_bounds__(32 * PY) k_fftf_fs(const float2 *__restrict__ 
     for (int a = 0; a < N; ++a) out[base + (long long)a * stride] = cmulf(x[a], ff.post[a]);
 }
 
+// The two slow axes of a transform through one (axis-0, axis-1) plane in
+// shared memory: a block holds the plane of one axis-2 index for CB cells
+// (rows of N CB values padded by 8 so that both pencil directions read
+// conflict-free), one thread per (pencil, cell).
+// STAGE: one RK4 node-value stage, from the axis-2 inverse output to the
+// axis-2 forward input: axis-1 inverse FFT, axis-0 inverse FFT with the
+// stage update (as k_fftf_fs) and axis-0 forward FFT, axis-1 forward FFT.
+// !STAGE: the forward transform's axis-1 and axis-0 passes.
+template <int N, int CB, bool STAGE>
+__global__ void __launch_bounds__(CB * N) k_fftf_plane(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                       const __grid_constant__ DftFac fi,
+                                                       const __grid_constant__ DftFac ff, int Bp, int stage,
+                                                       float dt, float nu, const float *__restrict__ f,
+                                                       float *__restrict__ qn, const double *__restrict__ cnu,
+                                                       const double *__restrict__ cdt) {
+    constexpr int RS = N * CB + 8;  // row stride (float2) of the plane
+    __shared__ float2 pl[N * RS];
+    const int c = threadIdx.x, p = threadIdx.y, i2 = blockIdx.x, cb = blockIdx.y * CB;
+    const long long s1 = (long long)N * Bp, s0 = (long long)N * N * Bp;
+    const long long gcell = (long long)i2 * Bp + cb + c;
+    // stage inputs of the axis-0 pencil (i1 = p) of this thread, fetched early
+    float fv[N], qv[N];
+    float dtc = dt, nuc = nu;
+    if constexpr (STAGE) {
+#pragma unroll
+        for (int i0 = 0; i0 < N; ++i0) {
+            const long long o = i0 * s0 + p * s1 + gcell;
+            fv[i0] = f[o];
+            qv[i0] = stage == 0 ? 0.f : qn[o];
+        }
+        if (cnu) { nuc = (float)cnu[cb + c]; dtc = (float)cdt[cb + c]; }
+    }
+    float2 x[N];
+    // axis 1: the pencil (i0 = p, ., i2)
+#pragma unroll
+    for (int i1 = 0; i1 < N; ++i1) x[i1] = in[p * s0 + i1 * s1 + gcell];
+    if constexpr (STAGE) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = cmulf(x[i], fi.pre[i]);
+        fft_reg<N, 1>(x, fi.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) x[a] = cmulf(x[a], fi.post[a]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = cmulf(x[i], ff.pre[i]);
+        fft_reg<N, -1>(x, ff.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) x[a] = cmulf(x[a], ff.post[a]);
+    }
+#pragma unroll
+    for (int i1 = 0; i1 < N; ++i1) pl[p * RS + i1 * CB + c] = x[i1];
+    __syncthreads();
+    // axis 0: the pencil (., i1 = p, i2)
+#pragma unroll
+    for (int i0 = 0; i0 < N; ++i0) x[i0] = pl[i0 * RS + p * CB + c];
+    if constexpr (STAGE) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = cmulf(x[i], fi.pre[i]);
+        fft_reg<N, 1>(x, fi.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) {
+            const float sr = x[a].x * fi.post[a].x - x[a].y * fi.post[a].y;
+            float v;
+            if (stage == 0) {
+                qn[a * s0 + p * s1 + gcell] = sr;
+                v = fv[a] + dtc * sr * nuc;
+            } else {
+                v = fv[a] + 0.5f * dtc * qv[a] * nuc + 0.5f * dtc * sr * nuc;
+            }
+            x[a] = make_float2(v * ff.pre[a].x, v * ff.pre[a].y);
+        }
+        fft_reg<N, -1>(x, ff.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) pl[a * RS + p * CB + c] = cmulf(x[a], ff.post[a]);
+        __syncthreads();
+        // axis 1 forward: the pencil (i0 = p, ., i2)
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1) x[i1] = cmulf(pl[p * RS + i1 * CB + c], ff.pre[i1]);
+        fft_reg<N, -1>(x, ff.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) out[p * s0 + a * s1 + gcell] = cmulf(x[a], ff.post[a]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = cmulf(x[i], ff.pre[i]);
+        fft_reg<N, -1>(x, ff.w);
+#pragma unroll
+        for (int a = 0; a < N; ++a) out[a * s0 + p * s1 + gcell] = cmulf(x[a], ff.post[a]);
+    }
+}
+
+template <int N, bool STAGE>
+cudaError_t plane_launch(const float2 *in, float2 *out, const DftFac &fi, const DftFac &ff, int Bp, int stage,
+                         double dt, double nu, const float *f, float *qn, cudaStream_t st, Rates rates) {
+    constexpr int CB = 8;
+    k_fftf_plane<N, CB, STAGE><<<dim3(N, Bp / CB), dim3(CB, N), 0, st>>>(in, out, fi, ff, Bp, stage, (float)dt,
+                                                                         (float)nu, f, qn, rates.nu, rates.dt);
+    return cudaGetLastError();
+}
+
 template <typename TIn, int OUT, int N>
 cudaError_t fft_launch(const TIn *in, float2 *out, const DftFac &fac, int ax, int Bp, int stage, double dt,
                        double nu, const float *f, float *qn, float *f1, cudaStream_t st, Rates rates,
@@ -2761,6 +2860,19 @@ cudaError_t launch_fwd(const R *f, typename V2<R>::t *t1, typename V2<R>::t *F, 
                        cudaStream_t st, const DftFac *fac) {
     using C = typename V2<R>::t;
     cudaError_t e;
+    if constexpr (std::is_same<R, float>::value) {
+        if (fac && fac->n == n && fac->sign < 0 && (n == 8 || n == 16 || n == 24)) {
+            // axis 2, then axes 1 and 0 through one shared-memory plane
+            if ((e = dft_pass<R, R, 0>(f, t1, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr,
+                                       nullptr, fac)))
+                return e;
+            switch (n) {
+            case 8: return plane_launch<8, false>(t1, F, *fac, *fac, Bp, 0, 0, 0, nullptr, nullptr, st, Rates{});
+            case 16: return plane_launch<16, false>(t1, F, *fac, *fac, Bp, 0, 0, 0, nullptr, nullptr, st, Rates{});
+            default: return plane_launch<24, false>(t1, F, *fac, *fac, Bp, 0, 0, 0, nullptr, nullptr, st, Rates{});
+            }
+        }
+    }
     if ((e = dft_pass<R, R, 0>(f, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr, nullptr,
                                fac)))
         return e;
@@ -2830,6 +2942,17 @@ cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, 
         if ((e = dft_pass<float, float2, 0>(q, t1, Mi, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf,
                                             lamc, fi)))
             return e;
+        if (n <= 24) {
+            // axes 1 and 0 of the stage through one shared-memory plane
+            switch (n) {
+            case 8: e = plane_launch<8, true>(t1, t2, *fi, *ff, Bp, stage, dt, nu, f, qn, st, rates); break;
+            case 16: e = plane_launch<16, true>(t1, t2, *fi, *ff, Bp, stage, dt, nu, f, qn, st, rates); break;
+            default: e = plane_launch<24, true>(t1, t2, *fi, *ff, Bp, stage, dt, nu, f, qn, st, rates); break;
+            }
+            if (e) return e;
+            return dft_pass<float, float2, 0>(t2, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{},
+                                              nullptr, nullptr, ff);
+        }
         if ((e = dft_pass<float, float2, 0>(t1, t2, Mi, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{},
                                             nullptr, nullptr, fi)))
             return e;
