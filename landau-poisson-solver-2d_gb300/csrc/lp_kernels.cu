@@ -1692,6 +1692,28 @@ __global__ void __launch_bounds__(32 * kIncWarps)
     }
 }
 
+// out_j = sum_k T(k, j) x_k for j = 0..nv-1 (nv even), two j per 16-byte
+// factor load: A += T * Re x, B += T * Im x with the pencil's broadcast pairs
+// xr[k] = (Re x_k, Re x_k), xi[k] = (Im x_k, Im x_k); out = (A.x - B.y, A.y + B.x).
+template <int N>
+__device__ __forceinline__ void proj_pairs(const unsigned long long (&xr)[N], const unsigned long long (&xi)[N],
+                                           const float2 *T, int nv, float2 *out, long long ostride) {
+    for (int j = 0; j < nv; j += 2) {
+        unsigned long long A0 = 0ull, B0 = 0ull, A1 = 0ull, B1 = 0ull;
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(T + k * nv + j);
+            A0 = fma2(tt.x, xr[k], A0);
+            B0 = fma2(tt.x, xi[k], B0);
+            A1 = fma2(tt.y, xr[k], A1);
+            B1 = fma2(tt.y, xi[k], B1);
+        }
+        const float2 a0 = up2(A0), b0 = up2(B0), a1 = up2(A1), b1 = up2(B1);
+        out[(long long)j * ostride] = make_float2(a0.x - b0.y, a0.y + b0.x);
+        out[(long long)(j + 1) * ostride] = make_float2(a1.x - b1.y, a1.y + b1.x);
+    }
+}
+
 // The same projection for n in {8, 16, 24, 32}, one thread per (pencil,
 // cell) with the pencil's n inputs in registers and the per-axis factors
 // T0, T1, T2 ([3][n][nv] complex) in shared memory (broadcast reads):
@@ -1748,6 +1770,14 @@ __global__ void __launch_bounds__(128) k_pj3(const QT *__restrict__ q0, const QT
                                (float)(nu * (0.5 * a.y + (e.y + d.y + g.y) * (1. / 6.))));
         }
     }
+    if ((nv & 1) == 0) {
+        unsigned long long xr[N], xi[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) { xr[k] = pk2(x[k].x, x[k].x); xi[k] = pk2(x[k].y, x[k].y); }
+        for (int a = 0; a < 3; ++a)
+            proj_pairs<N>(xr, xi, Ts + a * N * nv, nv, Y + ((long long)a * N * N + pid) * nv * Bp + c, Bp);
+        return;
+    }
     for (int a = 0; a < 3; ++a)
         for (int j = 0; j < nv; ++j) {
             const float2 *t = Ts + a * N * nv + j;
@@ -1774,6 +1804,24 @@ __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const
     const int k1 = pid / nv, j3 = pid - k1 * nv;
     const int c = blockIdx.y * 32 + threadIdx.x;
     const long long ys = (long long)N * N * nv * Bp, zs = (long long)N * nv * nv * Bp;
+    if ((nv & 1) == 0) {
+        for (int a = 0; a < 3; ++a) {
+            unsigned long long xr[N], xi[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const float2 v = Y[a * ys + (((long long)k1 * N + k) * nv + j3) * Bp + c];
+                xr[k] = pk2(v.x, v.x);
+                xi[k] = pk2(v.y, v.y);
+            }
+            const int nf = a == 0 ? 3 : 1;
+            for (int f = 0; f < nf; ++f) {
+                const int p = a == 0 ? f : 2 + a;
+                proj_pairs<N>(xr, xi, Ts + f * N * nv, nv, Z + p * zs + ((long long)k1 * nv * nv + j3) * Bp + c,
+                              (long long)nv * Bp);
+            }
+        }
+        return;
+    }
     for (int a = 0; a < 3; ++a) {
         float2 x[N];
 #pragma unroll
