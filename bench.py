@@ -42,18 +42,9 @@ L2_FLUSH_BYTES = 512 << 20
 # `bench.py --steps 2 --warmup 1 --no-cpu-baseline --fp64-steps 0`)
 CONTRACT_TRAFFIC_BYTES = 105.24e6 + 100.49e6
 # the same for the kernels of the convolution form, per launch, from one
-# `ncu --set full -k regex:"k_fq_y|k_fq_x2"` capture of that command (None
+# `ncu --set full -k regex:"k_fq_y|k_fq_x12"` capture of that command (None
 # where not captured)
-FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x2": 107.26e6 + 147.53e6}
-
-
-def launches_per_step(line_warps):
-    """Kernels of one mixed collision step at n = 24 (64 cells, one pass):
-    nodes 1, forward transform 3 x 4, contraction x 4 (4 kernels in the
-    convolution form, 2 k-tiles in the line-tiled form),
-    conservation 2 x 4 (its correction is applied by the next kernels),
-    inverse transform 3 x 3, DG projection 3, multipliers 1, scatter 1."""
-    return 1 + 12 + 4 * (4 if line_warps == 0 else 2) + 8 + 9 + 3 + 1 + 1
+FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x12": 9.08e6 + 146.21e6}
 
 
 def fq_kernel_model(n, cells):
@@ -531,7 +522,7 @@ def main():
                         "d2h_bytes_per_step": nbytes},
                 "roofline": roof, "compute_roofline": comp,
                 "cpu_baseline": cb, "clocks": clk.summary(),
-                "gpu_launches": launches_per_step(schedule[1]) * args.steps}
+                "gpu_launches": ctx.collision_graph_kernels() * args.steps}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -139,6 +139,9 @@ lp_status lp_advect_step(lp_ctx *ctx);
 /* Collision step of spatial cells [cell_begin, cell_end) of the resident
  * state (-1, -1: every collided cell). */
 lp_status lp_collision_step(lp_ctx *ctx, int cell_begin, int cell_end);
+/* Kernel launches in one replay of the captured collision step over every
+ * collided cell (its graph's kernel nodes); 0 before the first such step. */
+lp_status lp_collision_graph_kernels(lp_ctx *ctx, int *kernels);
 /* nsteps passes of the time loop (advection, then collisions when nu > 0),
  * replayed from one captured CUDA graph per step. */
 lp_status lp_step(lp_ctx *ctx, int nsteps);

@@ -109,6 +109,7 @@ struct lp_ctx {
     } adj;
     // captured step, and captured collision step of all collided cells
     cudaGraphExec_t gexec = nullptr, cgexec = nullptr;
+    int cg_kernels = 0;  // kernel nodes of the captured collision step
     cudaStream_t gstream = nullptr, cgstream = nullptr;
 };
 
@@ -1296,12 +1297,29 @@ lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
         if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        size_t nn = 0;
+        c->cg_kernels = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+                for (size_t i = 0; i < nn; ++i) {
+                    cudaGraphNodeType ty;
+                    if (cudaGraphNodeGetType(nodes[i], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                        ++c->cg_kernels;
+                }
+        }
         e = cudaGraphInstantiate(&c->cgexec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
         c->cgstream = c->stream;
     }
     LP_CUDA(cudaGraphLaunch(c->cgexec, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_collision_graph_kernels(lp_ctx *c, int *kernels) {
+    if (!c || !kernels) return LP_ERR_INVALID;
+    *kernels = c->cgexec ? c->cg_kernels : 0;
     return LP_OK;
 }
 

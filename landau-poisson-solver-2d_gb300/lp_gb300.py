@@ -33,7 +33,7 @@ EXPORTS = [
     "lp_device_bytes", "lp_set_state", "lp_get_state", "lp_state_device_ptr", "lp_set_init",
     "lp_fft3d", "lp_fs", "lp_compute_q", "lp_conserve", "lp_rk4_cell", "lp_nodes",
     "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_last_fields", "lp_advect_step",
-    "lp_collision_step", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
+    "lp_collision_step", "lp_collision_graph_kernels", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
     "lp_conserve_noalloc",
     "lp_batch_create", "lp_batch_destroy", "lp_batch_set_stream", "lp_batch_synchronize",
     "lp_batch_last_error", "lp_batch_device_bytes", "lp_batch_set_state", "lp_batch_get_state",
@@ -123,6 +123,7 @@ def lib():
         L.lp_last_fields.argtypes = [_vp, _dp, _dp, _dp, _dp]
         L.lp_advect_step.argtypes = [_vp]
         L.lp_collision_step.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+        L.lp_collision_graph_kernels.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
         L.lp_step.argtypes = [_vp, ctypes.c_int]
         L.lp_moments.argtypes = [_vp, _dp]
         L.lp_time_kernel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
@@ -327,6 +328,13 @@ class Context:
 
     def collision_step(self, c0=-1, c1=-1):
         self._chk(self.L.lp_collision_step(self.h, int(c0), int(c1)))
+
+    def collision_graph_kernels(self):
+        """Kernel launches in one replay of the captured collision step over
+        every collided cell (0 before the first such step)."""
+        k = ctypes.c_int()
+        self._chk(self.L.lp_collision_graph_kernels(self.h, ctypes.byref(k)))
+        return k.value
 
     def step(self, nsteps=1):
         self._chk(self.L.lp_step(self.h, int(nsteps)))
