@@ -1215,36 +1215,6 @@ __global__ void k_cons_partial(const QT *__restrict__ q, const double *__restric
     }
 }
 
-// The same sums of an FP32 mode array with the constraint rows in FP32 (cf:
-// C1[0], C2[1..3], C1[4]): each thread's few products (at most n^3 / 2048)
-// are summed in FP32, the threads' and the chunks' sums in FP64.  The
-// multipliers then carry the FP32 mode array's own rounding level; the
-// moments of the step are fixed afterwards from FP64 sums of its increments.
-__global__ void __launch_bounds__(256) k_cons_partial32(const float2 *__restrict__ q, const float *__restrict__ cf,
-                                                        int n3, int Bp, int nchunk, double *__restrict__ part) {
-    __shared__ double red[8][5][32];
-    const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
-    const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
-    float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f, t4 = 0.f;
-#pragma unroll 4
-    for (int pt = p0 + y; pt < p1; pt += 8) {
-        const float2 v = q[(long long)pt * Bp + c];
-        t0 = fmaf(v.x, cf[pt], t0);
-        t1 = fmaf(v.y, cf[n3 + pt], t1);
-        t2 = fmaf(v.y, cf[2 * n3 + pt], t2);
-        t3 = fmaf(v.y, cf[3 * n3 + pt], t3);
-        t4 = fmaf(v.x, cf[4 * n3 + pt], t4);
-    }
-    red[y][0][cl] = f32_to_f64_bits(t0); red[y][1][cl] = f32_to_f64_bits(t1); red[y][2][cl] = f32_to_f64_bits(t2);
-    red[y][3][cl] = f32_to_f64_bits(t3); red[y][4][cl] = f32_to_f64_bits(t4);
-    __syncthreads();
-    if (y < 5) {
-        double s = 0;
-        for (int yy = 0; yy < 8; ++yy) s += red[yy][y][cl];
-        part[((long long)k * 5 + y) * Bp + c] = s;
-    }
-}
-
 // One block per cell: the threads sum the chunk partials in a fixed order
 // and a fixed tree, thread 0 solves (C C^T)^-1 t (solveWithCCt, K:49-55).
 __global__ void __launch_bounds__(256) k_cons_lambda(const double *__restrict__ part, int nchunk,
@@ -3156,16 +3126,6 @@ cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, cons
 
 cudaError_t launch_cons_lambda(const double *part, int nchunk, const double *cct_inv, int Bp, double *lam,
                                cudaStream_t st) {
-    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
-                                int Bp, double *part, int nchunk, double *lam, cudaStream_t st, const float *cf) {
-    if (cf && (n3 + nchunk - 1) / nchunk <= 8 * 16)
-        k_cons_partial32<<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, cf, n3, Bp, nchunk, part);
-    else
-        k_cons_partial<float2><<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
     k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     return cudaGetLastError();
 }

@@ -160,15 +160,9 @@ cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv,
                             int n3, int Bp, double *part, int nchunk, double *lam,
                             cudaStream_t st, bool apply = true);
-// The multipliers of an FP32 mode array: FP64 sums of its exact values, or
-// with cf (the constraint rows in FP32) FP32 sums of a few products each,
-// added in FP64.
 // The multipliers lam[5][Bp] from chunk partials part[nchunk][5][Bp].
 cudaError_t launch_cons_lambda(const double *part, int nchunk, const double *cct_inv, int Bp, double *lam,
                                cudaStream_t st);
-cudaError_t launch_conserve_lam(const float2 *q, const double *c1, const double *c2, const double *cct_inv, int n3,
-                                int Bp, double *part, int nchunk, double *lam, cudaStream_t st,
-                                const float *cf = nullptr);
 
 // Final RK4 combination, DG projection and mass-matrix inverse: writes
 // dU[B][nv^3][5] for cells [c0, c0+B).  Qc, Y, Z are scratch.
