@@ -48,7 +48,7 @@ FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x12": 9.08e6 + 146.21e6}
 
 
 def fq_kernel_model(n, cells):
-    """Algorithmic DRAM bytes and FP32 flops per launch of the five kernels of
+    """Algorithmic DRAM bytes and FP32 flops per launch of the four kernels of
     the convolution form (complex FP32 intermediates of 8 bytes, q in FP64):
     each kernel reads its input arrays once and writes its outputs once."""
     M, h = 3 * n // 2, n // 2
@@ -409,7 +409,7 @@ def main():
 
     # Dominant kernel: the weighted contraction of ComputeQ for the 64 cells,
     # timed alone with CUDA events on the context's stream; in the
-    # convolution form each of its five kernels is timed alone too.
+    # convolution form each of its four kernels is timed alone too.
     extra = {}
     with torch.cuda.stream(stream):
         flush.zero_()
