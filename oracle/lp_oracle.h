@@ -20,7 +20,8 @@
 extern "C" {
 #endif
 
-/* Fixes of reference defects (see the defect table in the design doc). */
+/* Fixes of reference defects, one flag each (the same bits as LP_FIX_* of
+ * lp_gb300.h); with a flag clear the oracle keeps the reference's behaviour. */
 #define LPO_FIX_F1 1u   /* RK4 reads the stride-7 slots {0,3,4,5,6} */
 #define LPO_FIX_F2 2u   /* setInit_spectral uses slot 3 as the v1 slope */
 #define LPO_FIX_F3 4u   /* collide every spatial cell, not only s < nx1 */
