@@ -108,3 +108,23 @@ def test_set_schedule_rejects(gpu_lib):
     with pytest.raises(lp.LPError):
         ctx.set_schedule(48, 2)
     ctx.set_schedule(32, 2)
+
+
+@pytest.mark.parametrize("n,nv", [(16, 5), (16, 7), (8, 28)], ids=["nv5", "nv7", "nv28"])
+def test_collision_odd_and_large_nv(gpu_lib, n, nv):
+    """The mixed projection's odd-Nv branches (guarded factor loads, the
+    scalar axis-3/axis-2 loops) and its eight-outputs-per-thread variant
+    (Nv in 25..32) against the FP64 path, with mass and energy kept."""
+    lp = gpu_lib
+    case = Case(nx1=2, nx2=1, nv=nv, n=n, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.5, k_wave=0.5)
+    mix = _ctx(lp, case, lp.PREC_MIXED)
+    ref = _ctx(lp, case, lp.PREC_FP64)
+    mix.set_init(1)
+    ref.set_init(1)
+    m0 = mix.moments()
+    mix.collision_step()
+    ref.collision_step()
+    assert rel(mix.get_state(), ref.get_state()) < 1e-6
+    m1 = mix.moments()
+    assert abs(m1[0] - m0[0]) / abs(m0[0]) < 1e-12
+    assert abs(m1[4] - m0[4]) / abs(m0[4]) < 1e-12
