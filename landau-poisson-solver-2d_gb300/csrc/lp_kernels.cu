@@ -349,213 +349,6 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
     }
 }
 
-// The FP32 form of the pass: OG threads per (pencil, cell), each holding the
-// pencil's N inputs in registers and forming N / OG outputs with packed
-// f32x2 FMAs over the real and imaginary parts of M:
-//   A_a += (Re M[a][i], Im M[a][i]) * Re x_i,  B_a += (...) * Im x_i,
-//   out_a = (A_a.x - B_a.y, A_a.y + B_a.x).
-// M is staged transposed, Mt[i][a], so one 16-byte shared load gives the
-// entries of two consecutive outputs.  A real input (TIn = float) needs A only.
-template <typename TIn, int OUT, int N, int PY, int OG>
-__global__ void __launch_bounds__(32 * PY * OG) k_dftf(const TIn *__restrict__ in, float2 *__restrict__ out,
-                                                       const float *__restrict__ M, int ax, int Bp, int stage,
-                                                       float dt, float nu, const float *__restrict__ f,
-                                                       float *__restrict__ qn, float *__restrict__ f1,
-                                                       const double *__restrict__ cnu, const double *__restrict__ cdt,
-                                                       const float *__restrict__ cf, const double *__restrict__ lamc) {
-    constexpr int NO = N / OG;
-    static_assert(NO % 2 == 0, "outputs are formed in pairs");
-    constexpr bool REAL = std::is_same<TIn, float>::value;
-    __shared__ __align__(16) float2 Mt[N * N];
-    __shared__ float cfs[PY][5][N];
-    for (int t = threadIdx.y * 32 + threadIdx.x; t < N * N; t += 32 * PY * OG) {
-        const int a = t / N, i = t % N;
-        Mt[i * N + a] = make_float2(M[2 * t], M[2 * t + 1]);
-    }
-    if (cf) {
-        constexpr int n3 = N * N * N;
-        for (int t = threadIdx.y * 32 + threadIdx.x; t < PY * 5 * N; t += 32 * PY * OG) {
-            const int pp = t / (5 * N), r = (t / N) % 5, i = t % N, p0 = blockIdx.x * PY + pp;
-            cfs[pp][r][i] = p0 < N * N ? cf[r * n3 + p0 * N + i] : 0.f;
-        }
-    }
-    __syncthreads();
-    const int pid = blockIdx.x * PY + threadIdx.y / OG, og = threadIdx.y % OG;
-    if (pid >= N * N) return;
-    const int c = blockIdx.y * 32 + threadIdx.x;
-    long long base, stride;
-    if (ax == 2) { base = (long long)pid * N * Bp; stride = Bp; }
-    else if (ax == 1) { const int i0 = pid / N, i2 = pid % N; base = ((long long)i0 * N * N + i2) * Bp; stride = (long long)N * Bp; }
-    else { base = (long long)pid * Bp; stride = (long long)N * N * Bp; }
-    base += c;
-    float2 x[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        if constexpr (std::is_same<TIn, double2>::value) x[i] = ld2c<float>(in + base + i * stride);
-        else x[i] = ld2<float>(in + base + i * stride);
-    }
-    if (cf) {
-        const float l0 = (float)lamc[c], l1 = (float)lamc[Bp + c], l2 = (float)lamc[2 * Bp + c],
-                    l3 = (float)lamc[3 * Bp + c], l4 = (float)lamc[4 * Bp + c];
-        const float(*r)[N] = cfs[threadIdx.y / OG];
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            x[i].x -= r[0][i] * l0 + r[4][i] * l4;
-            x[i].y -= r[1][i] * l1 + r[2][i] * l2 + r[3][i] * l3;
-        }
-    }
-    unsigned long long A[NO], B[NO];
-#pragma unroll
-    for (int a = 0; a < NO; ++a) A[a] = B[a] = 0ull;
-    if constexpr (OUT == 1 && !REAL) {
-        // the stage needs the real part only: A_a += (Re M, Im M) * (Re x, Im x)
-        // element-wise, Re out_a = A_a.x - A_a.y
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            const unsigned long long xv = pk2(x[i].x, x[i].y);
-            const ulonglong2 *mrow = reinterpret_cast<const ulonglong2 *>(Mt + i * N + og * NO);
-#pragma unroll
-            for (int aa = 0; aa < NO; aa += 2) {
-                const ulonglong2 m = mrow[aa / 2];
-                A[aa] = fma2(m.x, xv, A[aa]);
-                A[aa + 1] = fma2(m.y, xv, A[aa + 1]);
-            }
-        }
-    } else
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        const unsigned long long xr = pk2(x[i].x, x[i].x);
-        const ulonglong2 *mrow = reinterpret_cast<const ulonglong2 *>(Mt + i * N + og * NO);
-        if constexpr (REAL) {
-#pragma unroll
-            for (int aa = 0; aa < NO; aa += 2) {
-                const ulonglong2 m = mrow[aa / 2];
-                A[aa] = fma2(m.x, xr, A[aa]);
-                A[aa + 1] = fma2(m.y, xr, A[aa + 1]);
-            }
-        } else {
-            const unsigned long long xi = pk2(x[i].y, x[i].y);
-#pragma unroll
-            for (int aa = 0; aa < NO; aa += 2) {
-                const ulonglong2 m = mrow[aa / 2];
-                A[aa] = fma2(m.x, xr, A[aa]);
-                B[aa] = fma2(m.x, xi, B[aa]);
-                A[aa + 1] = fma2(m.y, xr, A[aa + 1]);
-                B[aa + 1] = fma2(m.y, xi, B[aa + 1]);
-            }
-        }
-    }
-    float dtc = dt, nuc = nu;
-    if (OUT == 1 && cnu) { nuc = (float)cnu[c]; dtc = (float)cdt[c]; }
-#pragma unroll
-    for (int aa = 0; aa < NO; ++aa) {
-        const float2 av = up2(A[aa]);
-        float sr = av.x, si = av.y;
-        if constexpr (OUT == 1 && !REAL) {
-            sr = av.x - av.y;
-        } else if constexpr (!REAL) {
-            const float2 bv = up2(B[aa]);
-            sr -= bv.y;
-            si += bv.x;
-        }
-        const long long o = base + (long long)(og * NO + aa) * stride;
-        if constexpr (OUT == 0) {
-            out[o] = make_float2(sr, si);
-        } else {
-            // RK4 node-value stages (C:831-862); per-cell nu and dt when given.
-            if (stage == 0) {
-                qn[o] = sr;
-                f1[o] = f[o] + dtc * sr * nuc;
-            } else {
-                f1[o] = f[o] + 0.5f * dtc * qn[o] * nuc + 0.5f * dtc * sr * nuc;
-            }
-        }
-    }
-}
-
-// One RK4 node-value stage across the last inverse pass and the first
-// forward pass, both along axis 0 (pencil stride n^2 Bp): the pencil's
-// inverse DFT (Mi) gives the stage's Q at the nodes (its real part), the
-// node value
-//   stage 0: qn = Q, v = f + dt nu Q;   stages 1, 2: v = f + dt nu qn / 2 + dt nu Q / 2
-// (C:831-862) goes through shared memory to the OG threads of its (pencil,
-// cell), and their forward DFT (M) of the pencil of v is stored complex.
-template <int N, int PY, int OG>
-__global__ void __launch_bounds__(32 * PY * OG) k_dftf_fs(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                                          const float *__restrict__ Mi, const float *__restrict__ Mf,
-                                                          int Bp, int stage, float dt, float nu,
-                                                          const float *__restrict__ f, float *__restrict__ qn,
-                                                          const double *__restrict__ cnu,
-                                                          const double *__restrict__ cdt) {
-    constexpr int NO = N / OG;
-    static_assert(NO % 2 == 0 && (N * N) % PY == 0, "outputs in pairs, whole blocks of pencils");
-    __shared__ __align__(16) float2 Ti[N * N], Tf[N * N];
-    __shared__ float sv[PY][N][32];
-    for (int t = threadIdx.y * 32 + threadIdx.x; t < N * N; t += 32 * PY * OG) {
-        const int a = t / N, i = t % N;
-        Ti[i * N + a] = make_float2(Mi[2 * t], Mi[2 * t + 1]);
-        Tf[i * N + a] = make_float2(Mf[2 * t], Mf[2 * t + 1]);
-    }
-    __syncthreads();
-    const int py = threadIdx.y / OG, og = threadIdx.y % OG, lane = threadIdx.x;
-    const int pid = blockIdx.x * PY + py;
-    const int c = blockIdx.y * 32 + lane;
-    const long long stride = (long long)N * N * Bp, base = (long long)pid * Bp + c;
-    unsigned long long A[NO];
-    {
-        float2 x[N];
-#pragma unroll
-        for (int i = 0; i < N; ++i) x[i] = in[base + i * stride];
-#pragma unroll
-        for (int a = 0; a < NO; ++a) A[a] = 0ull;
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            const unsigned long long xv = pk2(x[i].x, x[i].y);
-            const ulonglong2 *mrow = reinterpret_cast<const ulonglong2 *>(Ti + i * N + og * NO);
-#pragma unroll
-            for (int aa = 0; aa < NO; aa += 2) {
-                const ulonglong2 m = mrow[aa / 2];
-                A[aa] = fma2(m.x, xv, A[aa]);
-                A[aa + 1] = fma2(m.y, xv, A[aa + 1]);
-            }
-        }
-    }
-    float dtc = dt, nuc = nu;
-    if (cnu) { nuc = (float)cnu[c]; dtc = (float)cdt[c]; }
-#pragma unroll
-    for (int aa = 0; aa < NO; ++aa) {
-        const float2 av = up2(A[aa]);
-        const float sr = av.x - av.y;
-        const int a = og * NO + aa;
-        const long long o = base + (long long)a * stride;
-        float v;
-        if (stage == 0) {
-            qn[o] = sr;
-            v = f[o] + dtc * sr * nuc;
-        } else {
-            v = f[o] + 0.5f * dtc * qn[o] * nuc + 0.5f * dtc * sr * nuc;
-        }
-        sv[py][a][lane] = v;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int a = 0; a < NO; ++a) A[a] = 0ull;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        const float xs = sv[py][i][lane];
-        const unsigned long long xr = pk2(xs, xs);
-        const ulonglong2 *mrow = reinterpret_cast<const ulonglong2 *>(Tf + i * N + og * NO);
-#pragma unroll
-        for (int aa = 0; aa < NO; aa += 2) {
-            const ulonglong2 m = mrow[aa / 2];
-            A[aa] = fma2(m.x, xr, A[aa]);
-            A[aa + 1] = fma2(m.y, xr, A[aa + 1]);
-        }
-    }
-#pragma unroll
-    for (int aa = 0; aa < NO; ++aa) out[base + (long long)(og * NO + aa) * stride] = up2(A[aa]);
-}
-
 // ---------------------------------------------------------------- register FFTs
 // Length-N DFTs y[a] = sum_i r^(a i) x[i], r = exp(S 2 pi i / N), S = -1
 // (forward) or +1 (inverse), on a register array: radices 2, 3, 4 and 8 in
@@ -647,8 +440,10 @@ template <int N, int S> __device__ __forceinline__ void fft_reg(float2 (&x)[N], 
     }
 }
 
-// The FP32 pass of k_dftf as a register FFT: one thread per (pencil, cell)
+// The FP32 per-axis pass as a register FFT: one thread per (pencil, cell)
 // holds the pencil, multiplies by pre, transforms and multiplies by post.
+// OUT 0: complex store; OUT 1: the RK4 node-value stage on the real part.
+// cf/lamc (axis 2 only): the lazy conservation correction on load.
 template <typename TIn, int OUT, int N, int S, int PY>
 __global__ void __launch_bounds__(32 * PY) k_fftf(const TIn *__restrict__ in, float2 *__restrict__ out,
                                                   const __grid_constant__ DftFac fac, int ax, int Bp, int stage,
@@ -715,9 +510,11 @@ __global__ void __launch_bounds__(32 * PY) k_fftf(const TIn *__restrict__ in, fl
     }
 }
 
-// k_dftf_fs as register FFTs: the inverse transform along axis 0, the node
-// value of the stage and its forward transform along axis 0, one thread per
-// (pencil, cell).
+// One RK4 node-value stage across the last inverse pass and the first
+// forward pass, both along axis 0, as register FFTs, one thread per (pencil,
+// cell): the inverse gives the stage's Q at the nodes (its real part), the
+// node value (stage 0: qn = Q, v = f + dt nu Q; stages 1, 2:
+// v = f + dt nu qn / 2 + dt nu Q / 2, C:831-862) and its forward transform.
 template <int N, int PY>
 __global__ void __launch_bounds__(32 * PY) k_fftf_fs(const float2 *__restrict__ in, float2 *__restrict__ out,
                                                      const __grid_constant__ DftFac fi,
@@ -872,14 +669,6 @@ cudaError_t dftp_launch(const TIn *in, typename V2<R>::t *out, const R *M, int a
                         const float *cf = nullptr, const double *lamc = nullptr) {
     constexpr int PY = 2, OG = 4;
     if (cf && ax != 2) return cudaErrorInvalidValue;
-    if constexpr (std::is_same<R, float>::value && N <= 24) {
-        // two threads per (pencil, cell): at 64 cells the pass is one wave of blocks
-        constexpr int OGF = 2, PYF = 4;
-        dim3 grid((N * N + PYF - 1) / PYF, Bp / 32), block(32, PYF * OGF);
-        k_dftf<TIn, OUT, N, PYF, OGF><<<grid, block, 0, st>>>(in, out, M, ax, Bp, stage, (float)dt, (float)nu, f, qn,
-                                                               f1, rates.nu, rates.dt, cf, lamc);
-        return cudaGetLastError();
-    }
     dim3 grid((N * N + PY - 1) / PY, Bp / 32), block(32, PY * OG);
     k_dftp<R, TIn, OUT, N, PY, OG><<<grid, block, 0, st>>>(in, out, M, ax, Bp, stage, (R)dt, (R)nu, f, qn, f1,
                                                            rates.nu, rates.dt, cf, lamc);
@@ -2940,16 +2729,6 @@ cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const flo
                                       fac);
 }
 
-template <int N>
-cudaError_t fs_fwd_launch(const float2 *in, float2 *out, const float *Mi, const float *M, int Bp, int stage,
-                          double dt, double nu, const float *f, float *qn, cudaStream_t st, Rates rates) {
-    constexpr int OG = 2, PY = 4;
-    dim3 grid(N * N / PY, Bp / 32), block(32, PY * OG);
-    k_dftf_fs<N, PY, OG><<<grid, block, 0, st>>>(in, out, Mi, M, Bp, stage, (float)dt, (float)nu, f, qn, rates.nu,
-                                                 rates.dt);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, const float *Mi, const float *M,
                             int n, int Bp, int stage, double dt, double nu, const float *f, float *qn, float *f1,
                             cudaStream_t st, Rates rates, const float *cf, const double *lamc, const DftFac *fi,
@@ -2989,23 +2768,9 @@ cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, 
         return dft_pass<float, float2, 0>(t2, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, nullptr,
                                           nullptr, ff);
     }
-    if (n != 8 && n != 16 && n != 24) {
-        if ((e = launch_fs_stage32(q, t1, t2, Mi, n, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc))) return e;
-        return launch_fwd<float>(f1, t1, F, M, n, Bp, st);
-    }
-    if ((e = dft_pass<float, float2, 0>(q, t1, Mi, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st, Rates{}, cf,
-                                        lamc)))
-        return e;
-    if ((e = dft_pass<float, float2, 0>(t1, t2, Mi, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    switch (n) {
-    case 8: e = fs_fwd_launch<8>(t2, t1, Mi, M, Bp, stage, dt, nu, f, qn, st, rates); break;
-    case 16: e = fs_fwd_launch<16>(t2, t1, Mi, M, Bp, stage, dt, nu, f, qn, st, rates); break;
-    default: e = fs_fwd_launch<24>(t2, t1, Mi, M, Bp, stage, dt, nu, f, qn, st, rates); break;
-    }
-    if (e) return e;
-    // the forward transform continues along axes 1 and 2
-    if ((e = dft_pass<float, float2, 0>(t1, t2, M, n, 1, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st))) return e;
-    return dft_pass<float, float2, 0>(t2, F, M, n, 2, Bp, 0, 0, 0, nullptr, nullptr, nullptr, st);
+    // without the factors: the inverse passes into f1, then the forward transform
+    if ((e = launch_fs_stage32(q, t1, t2, Mi, n, Bp, stage, dt, nu, f, qn, f1, st, rates, cf, lamc))) return e;
+    return launch_fwd<float>(f1, t1, F, M, n, Bp, st);
 }
 
 template <typename R>

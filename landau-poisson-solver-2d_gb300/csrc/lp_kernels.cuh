@@ -70,8 +70,8 @@ cudaError_t launch_fs_stage32(const float2 *q, float2 *t1, float2 *t2, const flo
 // One FP32 RK4 stage from its mode array to the next transformed node values
 // F: the inverse transform, the node-value stage and the forward transform,
 // with the last inverse and first forward passes (both along the slowest
-// axis) fused so that the stage's node values stay on chip (n <= 24; other n
-// run the two transforms in turn through f1).
+// axis) fused so that the stage's node values stay on chip; without the
+// per-axis factors (fi, ff) the two transforms run in turn through f1.
 cudaError_t launch_fs_fwd32(const float2 *q, float2 *t1, float2 *t2, float2 *F, const float *Mi, const float *M,
                             int n, int Bp, int stage, double dt, double nu, const float *f, float *qn, float *f1,
                             cudaStream_t st, Rates rates, const float *cf, const double *lamc,
