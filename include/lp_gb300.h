@@ -51,12 +51,15 @@ typedef enum {
     LP_ERR_STATE = 5        /* call out of order (e.g. no state uploaded) */
 } lp_status;
 
-/* Fixes of reference defects; LP_FIX_DEFAULT is F1 | F2 | F3 | F11. */
+/* Fixes of reference defects; LP_FIX_DEFAULT is F1 | F2 | F3 | F11 | F12. */
 #define LP_FIX_F1 1u   /* RK4 reads the stride-7 slots {0,3,4,5,6} of each record */
 #define LP_FIX_F2 2u   /* node sampling uses slot 3 as the v1 slope */
 #define LP_FIX_F3 4u   /* collide every spatial cell (the reference: s < nx1 only) */
 #define LP_FIX_F11 8u  /* snap the middle Fourier node eta[n/2] to exactly 0 */
-#define LP_FIX_DEFAULT (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3 | LP_FIX_F11)
+#define LP_FIX_F12 16u /* the DG flux takes the cell integrals of E_x (dx times the
+                          cell averages that pois2d leaves in IE_X, IXE_X, IXXE_X;
+                          without it the electric force is 1/dx too strong) */
+#define LP_FIX_DEFAULT (LP_FIX_F1 | LP_FIX_F2 | LP_FIX_F3 | LP_FIX_F11 | LP_FIX_F12)
 
 /* Arithmetic of the collision operator. */
 #define LP_PREC_FP64 0   /* every kernel in FP64 (the plain path) */

@@ -291,7 +291,8 @@ __global__ void k_flux_vjp(AdvectDev ad, const double *__restrict__ V, const dou
     }
     // v1 direction (I5), upwind by the sign of the cell-average E_x
     const long long nc = (long long)ad.nx1 * ad.nx2;
-    const double ie = fields[s], ixe = fields[nc + s], ixxe = fields[3 * nc + s];
+    const double fs = ad.fscale;  // dx with LP_FIX_F12, else 1
+    const double ie = fields[s] * fs, ixe = fields[nc + s] * fs, ixxe = fields[3 * nc + s] * fs;
     long long kR5 = -1, kL5 = -1;
     double s5;
     if (ie > 0) {
@@ -336,9 +337,9 @@ __global__ void k_flux_vjp(AdvectDev ad, const double *__restrict__ V, const dou
     const double lixe = m0 * dv2 * (R5[1] - L5[1]) + m1 * dv2 * (A5R - A5L) + 0.5 * m2 * dv2 * (R5[1] + L5[1]) +
                         m5 * dv2 * 5. / 12. * (R5[1] - L5[1]) - m2 * u[1] * sv_dv;
     const double lixxe = m1 * dv2 * (R5[1] - L5[1]);
-    atomicAdd(lamF + 3 * s + 0, lie);
-    atomicAdd(lamF + 3 * s + 1, lixe);
-    atomicAdd(lamF + 3 * s + 2, lixxe);
+    atomicAdd(lamF + 3 * s + 0, fs * lie);
+    atomicAdd(lamF + 3 * s + 1, fs * lixe);
+    atomicAdd(lamF + 3 * s + 2, fs * lixxe);
 }
 
 // lam_H = c * lam_out for every record (stage adjoint source)

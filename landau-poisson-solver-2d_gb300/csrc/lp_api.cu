@@ -351,6 +351,8 @@ lp::AdvectDev advect_dev(const lp_ctx *c) {
     a.dt_f = (float)T.prm.dt; a.dt6 = T.prm.dt / 6.;
     a.f.lv = (float)a.lv; a.f.dv = (float)a.dv; a.f.rdv = (float)a.rdv; a.f.scalev = (float)a.scalev;
     a.f.inv = (float)a.inv;
+    a.fscale = (T.prm.fixes & LP_FIX_F12) ? T.dx : 1.0;
+    a.f.fscale = (float)a.fscale;
     return a;
 }
 

@@ -2187,10 +2187,15 @@ __device__ __forceinline__ void flux_rhs(const AdvectDev &ad, const S *__restric
     const long long nc = (long long)ad.nx1 * ad.nx2;
     const double ie_d = fields[s];
     T ie, ixe, ixxe;
+    // the reference's field terms are cell averages; with LP_FIX_F12 they are
+    // scaled to the cell integrals the DG weak form needs (fscale = dx)
     if constexpr (F32) {
-        ie = f64_to_f32_bits(ie_d); ixe = f64_to_f32_bits(fields[nc + s]); ixxe = f64_to_f32_bits(fields[3 * nc + s]);
+        const float fs = ad.f.fscale;
+        ie = f64_to_f32_bits(ie_d) * fs; ixe = f64_to_f32_bits(fields[nc + s]) * fs;
+        ixxe = f64_to_f32_bits(fields[3 * nc + s]) * fs;
     } else {
-        ie = ie_d; ixe = fields[nc + s]; ixxe = fields[3 * nc + s];
+        const double fs = ad.fscale;
+        ie = ie_d * fs; ixe = fields[nc + s] * fs; ixxe = fields[3 * nc + s] * fs;
     }
     // ie > 0 from the bit pattern (a positive double is a positive integer)
     const bool ie_pos = F32 ? (__double_as_longlong(ie_d) > 0) : (ie_d > 0);

@@ -249,8 +249,10 @@ struct AdvectDev {
     double rdv, inv;  // 1/dv and 1/dx/scalev
     float dt_f;       // dt in FP32 (mixed-path stage copies)
     double dt6;       // dt/6 (mixed-path final stage)
+    double fscale;    // factor of the field integrals in the flux: dx with
+                      // LP_FIX_F12 (cell integrals), else 1 (the reference's averages)
     struct {
-        float lv, dv, rdv, scalev, inv;
+        float lv, dv, rdv, scalev, inv, fscale;
     } f;              // FP32 copies for the FP32 flux
 };
 // One SSP-RK3 stage: Uout = combination(U0, Us, H).  H is evaluated in FP64

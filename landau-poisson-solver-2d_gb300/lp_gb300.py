@@ -21,8 +21,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "liblp_gb300.so")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_NO_DEVICE, ERR_STATE = range(6)
-FIX_F1, FIX_F2, FIX_F3, FIX_F11 = 1, 2, 4, 8
-FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3 | FIX_F11
+FIX_F1, FIX_F2, FIX_F3, FIX_F11, FIX_F12 = 1, 2, 4, 8, 16
+FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3 | FIX_F11 | FIX_F12
 PREC_FP64, PREC_MIXED = 0, 1
 
 _dp = ctypes.POINTER(ctypes.c_double)

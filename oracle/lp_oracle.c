@@ -1138,8 +1138,12 @@ static void flux_h(const lpo_ctx *c, const double *U, long k, const double *IE, 
         ul3 = U[kl3 * 7 + 1];
     }
     const double *R3 = U + 7 * kr3, *L3 = U + 7 * kl3;
-    /* I5 neighbours (v1 upwind by sign of the cell-average E_x, zero inflow). */
-    const double ie = IE[s], ixe = IXE[s], ixxe = IXXE[s];
+    /* I5 neighbours (v1 upwind by sign of the cell-average E_x, zero inflow).
+     * pois2d leaves cell averages of E_x in IE_X, IXE_X, IXXE_X
+     * where the weak form needs cell integrals (the 1-D field code at A:180
+     * uses intE, the integral); LPO_FIX_F12 scales them by dx. */
+    const double fs = (c->p.fixes & LPO_FIX_F12) ? c->dx : 1.;
+    const double ie = IE[s] * fs, ixe = IXE[s] * fs, ixxe = IXXE[s] * fs;
     int j1r, j1l;
     long kr5, kl5;
     double ur5 = 0., ul5 = 0.;

@@ -26,7 +26,8 @@ extern "C" {
 #define LPO_FIX_F2 2u   /* setInit_spectral uses slot 3 as the v1 slope */
 #define LPO_FIX_F3 4u   /* collide every spatial cell, not only s < nx1 */
 #define LPO_FIX_F11 8u  /* snap the middle Fourier node eta[n/2] to exactly 0 */
-#define LPO_FIX_DEFAULT (LPO_FIX_F1 | LPO_FIX_F2 | LPO_FIX_F3 | LPO_FIX_F11)
+#define LPO_FIX_F12 16u /* the DG flux takes cell integrals of E_x (dx x averages) */
+#define LPO_FIX_DEFAULT (LPO_FIX_F1 | LPO_FIX_F2 | LPO_FIX_F3 | LPO_FIX_F11 | LPO_FIX_F12)
 
 typedef struct {
     int nx1, nx2, nv, n;

@@ -17,8 +17,8 @@ ORACLE_SO = os.path.join(HERE, "_build", "liblp_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
 REF_LIN_SO = os.path.join(HERE, "_ref", "libref_lin.so")  # the FullandLinear build
 
-FIX_F1, FIX_F2, FIX_F3, FIX_F11 = 1, 2, 4, 8
-FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3 | FIX_F11
+FIX_F1, FIX_F2, FIX_F3, FIX_F11, FIX_F12 = 1, 2, 4, 8, 16
+FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3 | FIX_F11 | FIX_F12
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
