@@ -301,8 +301,12 @@ lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path);
  * library until the process exits); larger ncell is rejected with
  * LP_ERR_INVALID.  The first call on a device looks up that array's device
  * address (cudaGetSymbolAddress) with the device current; make that first
- * call before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU race and must be serialised. */
+ * call before any stream capture.  That address is kept for the life of the
+ * process: do not call this function again after a cudaDeviceReset of that
+ * device.  An error already pending on the calling thread is reported as
+ * LP_ERR_CUDA (and left pending) before anything is launched.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * serialised. */
 #define LP_NOALLOC_MAX_CELLS 4096
 lp_status lp_conserve_noalloc(double *qhat_dev, int ncell, int n3, const double *c1_dev,
                               const double *c2_dev, const double *cct_inv_dev, void *cuda_stream);

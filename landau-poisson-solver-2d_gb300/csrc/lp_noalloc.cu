@@ -33,7 +33,8 @@ constexpr size_t kScratchDoubles = (size_t)LP_NOALLOC_MAX_CELLS * (kChunks * 5 +
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 // Device address of g_noalloc_scratch per device ordinal, looked up once per
-// device with that device current.
+// device with that device current.  A cudaDeviceReset unloads the module and
+// leaves this address stale, so the entry point must not be used across one.
 double *g_scratch_addr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;
 
@@ -103,6 +104,9 @@ extern "C" lp_status lp_conserve_noalloc(double *qhat_dev, int ncell, int n3, co
     if (reinterpret_cast<uintptr_t>(qhat_dev) % 16 || reinterpret_cast<uintptr_t>(c1_dev) % 8 ||
         reinterpret_cast<uintptr_t>(c2_dev) % 8 || reinterpret_cast<uintptr_t>(cct_inv_dev) % 8)
         return LP_ERR_INVALID;
+    // an error left pending by the caller's earlier CUDA work is reported, not
+    // cleared, and nothing is launched
+    if (cudaPeekAtLastError() != cudaSuccess) return LP_ERR_CUDA;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
@@ -126,8 +130,12 @@ extern "C" lp_status lp_conserve_noalloc(double *qhat_dev, int ncell, int n3, co
     double *lam = scratch + (size_t)LP_NOALLOC_MAX_CELLS * kChunks * 5;
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     double2 *q = reinterpret_cast<double2 *>(qhat_dev);
+    // each launch is checked before the next; a failed launch's own error is
+    // the only one cleared here
     k_na_partial<<<dim3(kChunks, ncell), 256, 0, st>>>(q, c1_dev, c2_dev, n3, part);
+    if (cudaGetLastError() != cudaSuccess) return LP_ERR_CUDA;
     k_na_lambda<<<(ncell + 127) / 128, 128, 0, st>>>(part, cct_inv_dev, ncell, lam);
+    if (cudaGetLastError() != cudaSuccess) return LP_ERR_CUDA;
     const long long total = (long long)ncell * n3;
     k_na_apply<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(q, c1_dev, c2_dev, lam, n3, total);
     return cudaGetLastError() == cudaSuccess ? LP_OK : LP_ERR_CUDA;
