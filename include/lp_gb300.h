@@ -283,6 +283,45 @@ lp_status lp_batch_class_info(const lp_batch *b, int cls, int *info6, double *tu
  * was. */
 lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path);
 
+/* ---- x1 slabs of a sharded run ------------------------------------------ */
+/* Replace the reference's MPI decomposition (cells split over ranks,
+ * source/LP_ompi_1.cpp:164-178; the whole state root-gathered and broadcast
+ * every step, LP_ompi_1.cpp:518-567, and in RK3, advection_1.cpp:472-489) by
+ * contiguous x1 slabs.  A slab context holds global x1 rows [i1_begin,
+ * i1_end) of the grid `global` as its local rows 1..i1_end-i1_begin, plus one
+ * halo row on each side (local rows 0 and i1_end-i1_begin+1; its state has
+ * (i1_end-i1_begin+2)*nx2*nv^3 records).  One time step on the slab is, for
+ * stage = 0, 1, 2 of SSP-RK3:
+ *   1. the caller copies the neighbour slabs' edge rows of stage buffer
+ *      `stage` into its halo rows (periodic in x1);
+ *   2. lp_slab_charge: the charge moments of the own cells of that buffer;
+ *   3. the caller all-gathers them in x1 order (3 per cell, global order);
+ *   4. lp_slab_fields: the global LDG Poisson solve from them (every rank
+ *      solves the same small system) and the field integrals of its rows;
+ *   5. lp_slab_advect_stage: the stage's flux and update of every record;
+ * then lp_collision_step over the own cells (cells nx2 .. (i1_end-i1_begin+1)
+ * *nx2), which needs no exchange.  The advection of a slab runs in FP64 for
+ * either precision.  lp_set_init places the slab in the global grid. */
+lp_status lp_slab_create(const lp_params *global, int i1_begin, int i1_end, lp_ctx **out);
+/* Device pointer of stage buffer `stage` of the state: 0 = U (the step's
+ * input and, after stage 2, its output), 1 = U1, 2 = Ut (the inputs of
+ * stages 1 and 2), records in the state's layout. */
+lp_status lp_stage_device_ptr(lp_ctx *ctx, int stage, double **dev);
+/* Charge moments (3 per cell, the reference's order and sums) of the own
+ * cells of stage buffer `stage` into rt_dev (device, 3*(i1_end-i1_begin)*nx2
+ * doubles). */
+lp_status lp_slab_charge(lp_ctx *ctx, int stage, double *rt_dev);
+/* LDG Poisson solve of the whole grid from its charge moments rt_global_dev
+ * (device, 3*nx1*nx2 doubles in global cell order), and the field integrals
+ * of the slab's rows (halo rows included) for the next lp_slab_advect_stage. */
+lp_status lp_slab_fields(lp_ctx *ctx, const double *rt_global_dev);
+/* SSP-RK3 stage `stage` (0, 1, 2) of every record of the slab with the field
+ * integrals of the last lp_slab_fields (FP64). */
+lp_status lp_slab_advect_stage(lp_ctx *ctx, int stage);
+/* Potential and field coefficients of the whole grid from the last
+ * lp_slab_fields (host, 3*nx1*nx2 doubles each; any may be NULL). */
+lp_status lp_slab_fields_host(lp_ctx *ctx, double *potc, double *phix, double *phiy);
+
 /* ---- allocation-free projection ---------------------------------------- */
 /* No counterpart in the reference.  The moment-conserving projection of
  * lp_conserve for `ncell` mode arrays at once, for callers that may not

@@ -107,6 +107,17 @@ struct lp_ctx {
         double *seg = nullptr;     // states of one checkpoint segment
         int seg_len = 0;
     } adj;
+    // x1 slab of a sharded run (lp_slab_create): own x1 rows are local rows
+    // 1..slab_nown, rows 0 and slab_nown + 1 are halo copies of the
+    // neighbours' edge rows; i1_off is the global x1 row of local row 0 and
+    // slab_gnx1 the global row count (0: not a slab).  The global LDG
+    // Poisson factors and their solve buffers (gfields: 14 x global cells).
+    int i1_off = 0, slab_gnx1 = 0, slab_nown = 0;
+    lp::PoissonTables gpois;
+    double *gab = nullptr, *gpb = nullptr, *gpotc = nullptr, *gphix = nullptr, *gphiy = nullptr,
+           *gfields = nullptr;
+    int *gipiv = nullptr;
+    unsigned char *ggate = nullptr;
     // captured step, and captured collision step of all collided cells
     cudaGraphExec_t gexec = nullptr, cgexec = nullptr;
     int cg_kernels = 0;  // kernel nodes of the captured collision step
@@ -323,21 +334,28 @@ lp_status setup_advection(lp_ctx *c) {
     return LP_OK;
 }
 
-// fast = false: the host's operations (pois2d bit for bit); fast = true: the
-// mixed path's variant (reciprocals, charge from block partials).
-lp::PoissonDev poisson_dev(const lp_ctx *c, bool fast) {
-    const lp::PoissonTables &p = c->T.pois;
+lp::PoissonDev poisson_dev_of(const lp::PoissonTables &p, const double *ab, const int *ipiv,
+                              const unsigned char *gate) {
     lp::PoissonDev d{};
     d.nx = p.nx; d.ny = p.ny; d.ndim = p.ndim; d.kl = p.kl; d.ku = p.ku; d.ldab = p.ldab;
-    d.ab = c->ab; d.ipiv = c->ipiv; d.dxp = p.dxp; d.dyp = p.dyp; d.gate = c->gate;
+    d.ab = ab; d.ipiv = ipiv; d.dxp = p.dxp; d.dyp = p.dyp; d.gate = gate;
     std::memcpy(d.blk[0], p.acvx, sizeof(p.acvx));
     std::memcpy(d.blk[1], p.acyrr, sizeof(p.acyrr));
     std::memcpy(d.blk[2], p.acyrl, sizeof(p.acyrl));
     std::memcpy(d.blk[3], p.acvy, sizeof(p.acvy));
     std::memcpy(d.blk[4], p.acxrr, sizeof(p.acxrr));
     std::memcpy(d.blk[5], p.acxrl, sizeof(p.acxrl));
-    d.rdiag = fast ? c->rdiag : nullptr;
+    d.rdiag = nullptr;
     d.rdxp = 1.0 / p.dxp; d.rdyp = 1.0 / p.dyp;
+    d.cscale = 1.0;
+    return d;
+}
+
+// fast = false: the host's operations (pois2d bit for bit); fast = true: the
+// mixed path's variant (reciprocals, charge from block partials).
+lp::PoissonDev poisson_dev(const lp_ctx *c, bool fast) {
+    lp::PoissonDev d = poisson_dev_of(c->T.pois, c->ab, c->ipiv, c->gate);
+    d.rdiag = fast ? c->rdiag : nullptr;
     d.cscale = (fast && c->apart) ? c->T.scalev : 1.0;
     return d;
 }
@@ -734,7 +752,8 @@ template <typename R> lp_status do_rk4_cell(lp_ctx *c, const double *f, int cell
 }
 
 // SetInit_LD (source/SetInit_1.cpp:60-115) and its two variants, on the host.
-void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> &U) {
+// i1_off: global x1 index of the context's row 0 (a slab's halo row).
+void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> &U, int i1_off = 0) {
     static const double GW[5] = {0.5688888888888889, 0.4786286704993665, 0.4786286704993665, 0.2369268850561891,
                                  0.2369268850561891};
     static const double GX[5] = {0., -0.5384693101056831, 0.5384693101056831, -0.9061798459386640,
@@ -772,10 +791,11 @@ void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> 
                 t0 = t0 * 0.5 * 0.5 * 0.5; t1 = t1 * 0.5 * 0.5 * 0.5; t2 = t2 * 0.5 * 0.5 * 0.5;
                 t3 = t3 * 0.5 * 0.5 * 0.5; t4 = t4 * 0.5 * 0.5 * 0.5;
                 for (int i1 = 0; i1 < nx1; ++i1) {
-                    double sp = std::sin(cw * gridx(i1 + 0.5)), sm = std::sin(cw * gridx(i1 - 0.5));
+                    const int ig = i1 + i1_off;
+                    double sp = std::sin(cw * gridx(ig + 0.5)), sm = std::sin(cw * gridx(ig - 0.5));
                     double tp0 = (dx + (sp - sm) * a / cw) * t0 / dx;
                     double tp5 = (dx + (sp - sm) * a / cw) * t4 / dx;
-                    double u1 = (0.5 * (sp + sm) + (std::cos(cw * gridx(i1 + 0.5)) - std::cos(cw * gridx(i1 - 0.5))) / (cw * dx)) * (a / cw) * t0 * 12. / dx;
+                    double u1 = (0.5 * (sp + sm) + (std::cos(cw * gridx(ig + 0.5)) - std::cos(cw * gridx(ig - 0.5))) / (cw * dx)) * (a / cw) * t0 * 12. / dx;
                     double u3 = (dx + (sp - sm) * a / cw) * t1 * 12 / dx;
                     double u4 = (dx + (sp - sm) * a / cw) * t2 * 12 / dx;
                     double u5 = (dx + (sp - sm) * a / cw) * t3 * 12 / dx;
@@ -1156,7 +1176,7 @@ lp_status lp_state_device_ptr(lp_ctx *c, double **U) {
 lp_status lp_set_init(lp_ctx *c, int kind, double u) {
     if (!c || kind < 0 || kind > 2) return fail(c, LP_ERR_INVALID, "unknown initial condition");
     std::vector<double> U;
-    set_init_host(c->T, kind, u, U);
+    set_init_host(c->T, kind, u, U, c->i1_off);
     return lp_set_state(c, U.data(), U.size());
 }
 
@@ -2116,6 +2136,135 @@ lp_status lp_set_schedule(lp_ctx *c, int pass_cells, int line_warps) {
     c->line_warps = line_warps;
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
     if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
+    return LP_OK;
+}
+
+}  // extern "C"
+
+// ============================================================== x1 slabs
+// A sharded run splits the x1 rows of the spatial grid into contiguous slabs,
+// one per rank (the reference splits the cells over MPI ranks at
+// LP_ompi_1.cpp:164-178 and re-assembles the whole state on every rank with a
+// root gather and broadcast, LP_ompi_1.cpp:518-567, advection_1.cpp:472-489).
+// Here a rank keeps only its slab plus one halo row on each side:
+//   - collisions are local to a spatial cell: no exchange;
+//   - each SSP-RK3 stage needs the neighbours' edge rows (the x1 upwind flux
+//     of I3 reads one row to each side) -- the caller exchanges them into the
+//     halo rows of the stage buffer;
+//   - each stage needs the field of the whole grid: the caller all-gathers
+//     the three charge moments of every cell, and every rank solves the same
+//     (small) LDG Poisson system redundantly.
+// The exchanges themselves are the caller's (torch.distributed in the
+// package's slab schedule); these entry points do the device work.
+
+namespace {
+
+// Field integrals of the slab's local rows (halo rows included, periodic in
+// x1) from those of the whole grid; layout [14][cells] on both sides.
+__global__ void k_slab_fields(const double *__restrict__ gf, int gnc, double *__restrict__ f, int nc, int nx2,
+                              int i1_off, int gnx1) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nc) return;
+    const int i1 = s / nx2, i2 = s % nx2;
+    int g = (i1 + i1_off) % gnx1;
+    if (g < 0) g += gnx1;
+    const int gs = g * nx2 + i2;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) f[q * nc + s] = gf[q * gnc + gs];
+}
+
+double *stage_buffer(lp_ctx *c, int stage) { return stage == 0 ? c->U : stage == 1 ? c->U1 : c->Ut; }
+
+}  // namespace
+
+extern "C" {
+
+lp_status lp_slab_create(const lp_params *g, int i1_begin, int i1_end, lp_ctx **out) {
+    if (!g || !out) return LP_ERR_INVALID;
+    *out = nullptr;
+    if (g->nx1 < 2 || g->nx2 < 1 || i1_begin < 0 || i1_end > g->nx1 || i1_end - i1_begin < 1)
+        return LP_ERR_INVALID;
+    lp::Tables gt;
+    std::string err;
+    lp_status s = lp::build_tables(*g, gt, err, lp::kTablesPoisson);
+    if (s != LP_OK) return s;
+    lp_params p = *g;
+    p.nx1 = i1_end - i1_begin + 2;
+    lp_ctx *c = nullptr;
+    s = ctx_create(&p, CtxOpts{}, &c);
+    if (s != LP_OK) return s;
+    // the global cell sizes (the local geometry's lx / nx1 can differ in the
+    // last bit), the slab's place in the global grid, the global Poisson factors
+    c->T.dx = gt.dx;
+    c->T.dy = gt.dy;
+    c->i1_off = i1_begin - 1;
+    c->slab_gnx1 = g->nx1;
+    c->slab_nown = i1_end - i1_begin;
+    c->gpois = gt.pois;
+    const size_t gnc = (size_t)g->nx1 * g->nx2;
+    s = upload(c, &c->gab, gt.pois.ab.data(), gt.pois.ab.size());
+    if (s == LP_OK) s = upload(c, &c->gipiv, gt.pois.ipiv.data(), gt.pois.ipiv.size());
+    if (s == LP_OK) s = upload(c, &c->ggate, gt.pois.gate.data(), gt.pois.gate.size());
+    if (s == LP_OK) s = dalloc(c, &c->gpb, (size_t)gt.pois.ndim);
+    if (s == LP_OK) s = dalloc(c, &c->gpotc, 3 * gnc);
+    if (s == LP_OK) s = dalloc(c, &c->gphix, 3 * gnc);
+    if (s == LP_OK) s = dalloc(c, &c->gphiy, 3 * gnc);
+    if (s == LP_OK) s = dalloc(c, &c->gfields, 14 * gnc);
+    if (s == LP_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) s = LP_ERR_CUDA;
+    if (s != LP_OK) {
+        destroy(c);
+        return s;
+    }
+    *out = c;
+    return LP_OK;
+}
+
+lp_status lp_stage_device_ptr(lp_ctx *c, int stage, double **dev) {
+    if (!c || !dev || stage < 0 || stage > 2) return LP_ERR_INVALID;
+    *dev = stage_buffer(c, stage);
+    if (stage == 0) c->has_state = true;
+    return LP_OK;
+}
+
+lp_status lp_slab_charge(lp_ctx *c, int stage, double *rt_dev) {
+    if (!c || !rt_dev || stage < 0 || stage > 2) return LP_ERR_INVALID;
+    if (!c->slab_gnx1) return fail(c, LP_ERR_INVALID, "not a slab context");
+    const int nx2 = c->T.prm.nx2;
+    const double *Us = stage_buffer(c, stage) + (size_t)nx2 * c->T.nv3 * 7;  // skip halo row 0
+    LP_CUDA(lp::launch_charge(Us, c->slab_nown * nx2, c->T.nv3, c->T.scalev, rt_dev, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_slab_fields(lp_ctx *c, const double *rt_global_dev) {
+    if (!c || !rt_global_dev) return LP_ERR_INVALID;
+    if (!c->slab_gnx1) return fail(c, LP_ERR_INVALID, "not a slab context");
+    const int nx2 = c->T.prm.nx2, gnc = c->slab_gnx1 * nx2;
+    LP_CUDA(lp::launch_poisson(poisson_dev_of(c->gpois, c->gab, c->gipiv, c->ggate), rt_global_dev, 1, c->gpb,
+                               c->gpotc, c->gphix, c->gphiy, c->gfields, c->stream));
+    k_slab_fields<<<(c->T.ncell + 127) / 128, 128, 0, c->stream>>>(c->gfields, gnc, c->fields, c->T.ncell, nx2,
+                                                                   c->i1_off, c->slab_gnx1);
+    LP_CUDA(cudaGetLastError());
+    return LP_OK;
+}
+
+lp_status lp_slab_advect_stage(lp_ctx *c, int stage) {
+    if (!c || stage < 0 || stage > 2) return LP_ERR_INVALID;
+    if (!c->slab_gnx1) return fail(c, LP_ERR_INVALID, "not a slab context");
+    if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
+    double *out = stage == 0 ? c->U1 : stage == 1 ? c->Ut : c->U;
+    LP_CUDA(lp::launch_flux_stage(advect_dev(c), c->U, stage_buffer(c, stage), nullptr, c->fields, stage, out,
+                                  nullptr, nullptr, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_slab_fields_host(lp_ctx *c, double *potc, double *phix, double *phiy) {
+    if (!c) return LP_ERR_INVALID;
+    if (!c->slab_gnx1) return fail(c, LP_ERR_INVALID, "not a slab context");
+    const size_t n = 3 * (size_t)c->slab_gnx1 * c->T.prm.nx2;
+    if (potc) LP_CUDA(cudaMemcpyAsync(potc, c->gpotc, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (phix) LP_CUDA(cudaMemcpyAsync(phix, c->gphix, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (phiy) LP_CUDA(cudaMemcpyAsync(phiy, c->gphiy, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    LP_CUDA(cudaStreamSynchronize(c->stream));
     return LP_OK;
 }
 

@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 
 import numpy as np
 
@@ -42,6 +42,8 @@ EXPORTS = [
     "lp_field_energy", "lp_collision_vjp", "lp_advect_vjp", "lp_step_vjp", "lp_field_energy_gradient",
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
     "lp_autotune", "lp_set_schedule", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
+    "lp_slab_create", "lp_stage_device_ptr", "lp_slab_charge", "lp_slab_fields", "lp_slab_advect_stage",
+    "lp_slab_fields_host",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -162,6 +164,12 @@ def lib():
         L.lp_marginal_x1v1.argtypes = [_vp, _dp]
         L.lp_state_append.argtypes = [_vp, ctypes.c_char_p]
         L.lp_state_restart.argtypes = [_vp, ctypes.c_char_p]
+        L.lp_slab_create.argtypes = [ctypes.POINTER(_Params), ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]
+        L.lp_stage_device_ptr.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(_dp)]
+        L.lp_slab_charge.argtypes = [_vp, ctypes.c_int, _vp]
+        L.lp_slab_fields.argtypes = [_vp, _vp]
+        L.lp_slab_advect_stage.argtypes = [_vp, ctypes.c_int]
+        L.lp_slab_fields_host.argtypes = [_vp, _dp, _dp, _dp]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
@@ -190,13 +198,18 @@ def measure_fp_peaks():
 class Context:
     """One solver instance on the current CUDA device."""
 
-    def __init__(self, params: Params):
-        self.params = params
+    def __init__(self, params: Params, _slab=None):
         self.L = lib()
         h = _vp()
-        st = self.L.lp_ctx_create(ctypes.byref(params._c()), ctypes.byref(h))
+        if _slab is None:
+            self.params = params
+            st = self.L.lp_ctx_create(ctypes.byref(params._c()), ctypes.byref(h))
+        else:
+            i1_begin, i1_end = _slab
+            self.params = replace(params, nx1=i1_end - i1_begin + 2)
+            st = self.L.lp_slab_create(ctypes.byref(params._c()), int(i1_begin), int(i1_end), ctypes.byref(h))
         if st != OK:
-            raise LPError(st, "lp_ctx_create failed")
+            raise LPError(st, "lp_ctx_create failed" if _slab is None else "lp_slab_create failed")
         self.h = h
         self.n3 = params.n ** 3
         self.nv3 = params.nv ** 3
@@ -411,6 +424,38 @@ class Context:
         self._chk(self.L.lp_field_energy_gradient(self.h, int(nsteps), int(checkpoint), ctypes.byref(J),
                                                   _vp(dU0_ptr), ctypes.byref(d)))
         return J.value, d.value
+
+
+class SlabContext(Context):
+    """Global x1 rows [i1_begin, i1_end) of the grid `params` with one halo
+    row on each side (lp_slab_* of the C ABI); `params` of the instance is the
+    local geometry (nx1 = i1_end - i1_begin + 2), `global_params` the grid's."""
+
+    def __init__(self, params: Params, i1_begin: int, i1_end: int):
+        super().__init__(params, _slab=(i1_begin, i1_end))
+        self.global_params = params
+        self.i1_begin, self.i1_end = int(i1_begin), int(i1_end)
+        self.nown = self.i1_end - self.i1_begin
+
+    def stage_device_ptr(self, stage):
+        p = _dp()
+        self._chk(self.L.lp_stage_device_ptr(self.h, int(stage), ctypes.byref(p)))
+        return ctypes.cast(p, ctypes.c_void_p).value
+
+    def charge(self, stage, rt_dev_ptr):
+        self._chk(self.L.lp_slab_charge(self.h, int(stage), _vp(rt_dev_ptr)))
+
+    def fields(self, rt_global_dev_ptr):
+        self._chk(self.L.lp_slab_fields(self.h, _vp(rt_global_dev_ptr)))
+
+    def advect_stage(self, stage):
+        self._chk(self.L.lp_slab_advect_stage(self.h, int(stage)))
+
+    def global_fields(self):
+        n = 3 * self.global_params.ncell
+        potc, px, py = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._chk(self.L.lp_slab_fields_host(self.h, _p(potc), _p(px), _p(py)))
+        return potc, px, py
 
 
 class Batch:

@@ -1011,28 +1011,43 @@ void lpo_band(const lpo_ctx *c, int *dims, double *ab, int *ipiv)
 /* pois2d: charge moments, right-hand side, band solve, field
  * reconstruction and the cell integrals used by the advection.  Cells are
  * indexed ii = (ix-1)*ny + (jy-1) throughout (defect F8 used nx there). */
+/* Charge moments of spatial cells [s0, s1): rt[3*(s-s0)+m]. */
+void lpo_charge(const lpo_ctx *c, const double *U, int s0, int s1, double *rt)
+{
+    const int nv = c->p.nv;
+    for (int s = s0; s < s1; ++s) {
+        double r0 = 0., r1 = 0., r2 = 0.;
+        for (int j1 = 0; j1 < nv; ++j1)
+            for (int j2 = 0; j2 < nv; ++j2)
+                for (int j3 = 0; j3 < nv; ++j3) {
+                    long k = (long)s * c->nv3 + j1 * nv * nv + j2 * nv + j3;
+                    r0 += c->scalev * (U[7 * k + 0] + 0.25 * U[7 * k + 6]);
+                    r1 += c->scalev * U[7 * k + 1];
+                    r2 += c->scalev * U[7 * k + 2];
+                }
+        const int ii = s - s0;
+        rt[3 * ii] = r0; rt[3 * ii + 1] = r1; rt[3 * ii + 2] = r2;
+    }
+}
+
 void lpo_poisson(const lpo_ctx *c, const double *U, double *potc, double *phix, double *phiy,
                  double *fields)
 {
-    const pois_t *ps = &c->ps;
-    const int NXp = ps->nx, NYp = ps->ny, nv = c->p.nv;
-    const int nc = NXp * NYp;
+    const int nc = c->ps.nx * c->ps.ny;
     double *rt = (double *)calloc(3 * (size_t)nc, sizeof(double));
+    lpo_charge(c, U, 0, nc, rt);
+    lpo_poisson_rt(c, rt, potc, phix, phiy, fields);
+    free(rt);
+}
+
+/* The rest of pois2d from given charge moments rt (3 per spatial cell). */
+void lpo_poisson_rt(const lpo_ctx *c, const double *rt, double *potc, double *phix, double *phiy,
+                    double *fields)
+{
+    const pois_t *ps = &c->ps;
+    const int NXp = ps->nx, NYp = ps->ny;
+    const int nc = NXp * NYp;
     double *b = (double *)calloc(ps->ndim, sizeof(double));
-    for (int i1 = 0; i1 < NXp; ++i1)
-        for (int i2 = 0; i2 < NYp; ++i2) {
-            double r0 = 0., r1 = 0., r2 = 0.;
-            for (int j1 = 0; j1 < nv; ++j1)
-                for (int j2 = 0; j2 < nv; ++j2)
-                    for (int j3 = 0; j3 < nv; ++j3) {
-                        long k = (long)i1 * NYp * c->nv3 + (long)i2 * c->nv3 + j1 * nv * nv + j2 * nv + j3;
-                        r0 += c->scalev * (U[7 * k + 0] + 0.25 * U[7 * k + 6]);
-                        r1 += c->scalev * U[7 * k + 1];
-                        r2 += c->scalev * U[7 * k + 2];
-                    }
-            int ii = i1 * NYp + i2;
-            rt[3 * ii] = r0; rt[3 * ii + 1] = r1; rt[3 * ii + 2] = r2;
-        }
     const double PEP = 1., DOP = 1., DXv = ps->dxp, DYv = ps->dyp;
     for (int ii = 0; ii < nc; ++ii) {
         /* boundary data are zero, so only the charge terms remain */
@@ -1101,7 +1116,7 @@ void lpo_poisson(const lpo_ctx *c, const double *U, double *potc, double *phix, 
             F[13 * nc + ii] = phiy[3 * ii] > 0. ? 1. : -1.;
         }
     }
-    free(rt); free(b);
+    free(b);
 }
 
 /* ----------------------------------------------------------- advection */
@@ -1220,6 +1235,33 @@ static void flux_h(const lpo_ctx *c, const double *U, long k, const double *IE, 
     H[3] = tp[2] * 12. / dx / sv3;
     H[4] = tp[3] * 12. / dx / sv3;
     H[5] = tp[4] * 12. / dx / sv3;
+}
+
+/* Cell sizes of a slab of a larger grid: its own geometry gives lx / nx1
+ * of the slab, which can differ from the grid's in the last bit. */
+void lpo_set_cell_size(lpo_ctx *c, double dx, double dy)
+{
+    c->dx = dx;
+    c->dy = dy;
+}
+
+/* One SSP-RK3 stage (A:455-581) with given field integrals fields14 (the
+ * 14 x ncell output of pois2d): Uout = combination(U0, Us, H(Us)). */
+void lpo_rk3_stage(const lpo_ctx *c, const double *U0, const double *Us, const double *fl, int stage,
+                   double *Uout)
+{
+    const long size = c->size, nc = c->ncell;
+    const double dt = c->p.dt;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < size; ++k) {
+        double H[7];
+        flux_h(c, Us, k, fl, fl + nc, fl + 3 * nc, H);
+        for (int l = 0; l < 7; ++l) {
+            if (stage == 0) Uout[7 * k + l] = U0[7 * k + l] + dt * H[l];
+            else if (stage == 1) Uout[7 * k + l] = 0.75 * U0[7 * k + l] + 0.25 * Us[7 * k + l] + 0.25 * dt * H[l];
+            else Uout[7 * k + l] = U0[7 * k + l] / 3. + Us[7 * k + l] * 2. / 3. + dt * H[l] * 2. / 3.;
+        }
+    }
 }
 
 /* RK3 (A:428-601): SSP-RK3 with a Poisson solve before each stage. */

@@ -63,6 +63,16 @@ void lpo_set_init(const lpo_ctx *c, double *U, int kind, double u);
 void lpo_poisson(const lpo_ctx *c, const double *U, double *potc, double *phix, double *phiy,
                  double *fields14);
 void lpo_rk3(const lpo_ctx *c, double *U);
+/* Pieces of pois2d and RK3 for a slab of spatial cells: the charge moments
+ * of cells [s0, s1) (3 per cell), the solve from given charges of every
+ * cell, and one SSP-RK3 stage (0, 1, 2) with given field integrals. */
+void lpo_charge(const lpo_ctx *c, const double *U, int s0, int s1, double *rt);
+void lpo_poisson_rt(const lpo_ctx *c, const double *rt, double *potc, double *phix, double *phiy,
+                    double *fields14);
+void lpo_rk3_stage(const lpo_ctx *c, const double *U0, const double *Us, const double *fields14, int stage,
+                   double *Uout);
+/* Overrides the cell sizes (a slab context takes the whole grid's). */
+void lpo_set_cell_size(lpo_ctx *c, double dx, double dy);
 int lpo_collide(const lpo_ctx *c, double *U, int direct);
 void lpo_step(const lpo_ctx *c, double *U, int direct);
 void lpo_moments(const lpo_ctx *c, const double *U, const double *phix, const double *phiy,

@@ -120,6 +120,12 @@ def _oracle_lib():
         L.lpo_conserve_lin.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.lpo_cct_lin.argtypes = [ctypes.c_void_p, _dp]
         L.lpo_rk4_lin.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, ctypes.c_int]
+        for name in ["lpo_charge", "lpo_poisson_rt", "lpo_rk3_stage", "lpo_set_cell_size"]:
+            getattr(L, name).restype = None
+        L.lpo_charge.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, _dp]
+        L.lpo_poisson_rt.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]
+        L.lpo_rk3_stage.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, _dp]
+        L.lpo_set_cell_size.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         _olib = L
     return _olib
 
@@ -229,6 +235,29 @@ class Oracle:
         U = np.array(U, dtype=np.float64).reshape(-1)
         self.L.lpo_step(self.h, _p(U), int(direct))
         return U
+
+    # pieces of RK3 for slabs of a sharded run
+    def charge(self, U, s0, s1):
+        rt = np.zeros(3 * (s1 - s0))
+        self.L.lpo_charge(self.h, _p(np.ascontiguousarray(U, dtype=np.float64).reshape(-1)), int(s0), int(s1),
+                          _p(rt))
+        return rt
+
+    def poisson_rt(self, rt):
+        nc = self.case.ncell
+        potc, px, py, fl = np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(3 * nc), np.zeros(14 * nc)
+        self.L.lpo_poisson_rt(self.h, _p(np.ascontiguousarray(rt, dtype=np.float64)), _p(potc), _p(px), _p(py),
+                              _p(fl))
+        return potc, px, py, fl.reshape(14, nc)
+
+    def rk3_stage(self, U0, Us, fields14, stage, Uout):
+        """Uout (a C-contiguous float64 array, written in place) =
+        SSP-RK3 stage `stage` from U0, Us with the given field integrals."""
+        self.L.lpo_rk3_stage(self.h, _p(U0), _p(Us), _p(np.ascontiguousarray(fields14, dtype=np.float64)),
+                             int(stage), _p(Uout))
+
+    def set_cell_size(self, dx, dy):
+        self.L.lpo_set_cell_size(self.h, float(dx), float(dy))
 
     def moments(self, U, phix, phiy):
         out = np.zeros(6)

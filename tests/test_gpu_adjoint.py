@@ -136,15 +136,19 @@ def test_gradient_through_50_steps(gpu_lib):
     h = 1e-6
     fdA = (_J_after(lp, a_amp=CFG4["a_amp"] + h) - _J_after(lp, a_amp=CFG4["a_amp"] - h)) / (2 * h)
     assert abs(dA - fdA) <= 1e-6 * abs(fdA), (dA, fdA)
-    # J = 0.18 moves by only 5e-10 relative when nu moves by 1e-6, so a central
-    # difference with h = 1e-6 sits on the FP64 rounding floor of the 50-step
-    # run (1.6e-5 relative scatter); h = 1e-4 (truncation error below 1e-7)
-    # resolves it.
-    hn = 1e-4
-    fdnu = (_J_after(lp, nu=CFG4["nu"] + hn) - _J_after(lp, nu=CFG4["nu"] - hn)) / (2 * hn)
+    # J moves very little with nu (dJ/dnu = -5.2e-5), so a central difference
+    # with h = 1e-6 sits on the FP64 rounding floor of the 50-step run, and
+    # one with h = 1e-4 has a truncation error of about 1.5e-6; central
+    # differences at h = 2e-4 and 1e-4 combined by Richardson extrapolation
+    # (truncation O(h^4)) resolve it to 1e-6, and h = 1e-6 agrees to its
+    # rounding floor.
+    def cd(hn):
+        return (_J_after(lp, nu=CFG4["nu"] + hn) - _J_after(lp, nu=CFG4["nu"] - hn)) / (2 * hn)
+
+    fdnu = (4 * cd(1e-4) - cd(2e-4)) / 3
     assert abs(dnu - fdnu) <= 1e-6 * abs(fdnu), (dnu, fdnu)
-    fdnu_h = (_J_after(lp, nu=CFG4["nu"] + h) - _J_after(lp, nu=CFG4["nu"] - h)) / (2 * h)
-    assert abs(dnu - fdnu_h) <= 1e-4 * abs(fdnu_h), (dnu, fdnu_h)
+    fdnu_h = cd(h)
+    assert abs(dnu - fdnu_h) <= 1e-3 * abs(fdnu_h), (dnu, fdnu_h)
     rng = np.random.default_rng(20261203)
     for i in range(8):
         d = rng.standard_normal(U0.size) * np.abs(U0)
