@@ -142,6 +142,26 @@ lp_status lp_advect_step(lp_ctx *ctx);
 /* Collision step of spatial cells [cell_begin, cell_end) of the resident
  * state (-1, -1: every collided cell). */
 lp_status lp_collision_step(lp_ctx *ctx, int cell_begin, int cell_end);
+/* The collision step of every collided cell with the state in HOST memory,
+ * for a caller whose state lives on the host (it replaces the loop of main
+ * with its scatter into U, LP_ompi_1.cpp:500-568): U_in (ncell*nv^3*7
+ * doubles) is copied to the device, collided and copied back into U_out
+ * (which may equal U_in).  The cells go in `chunks` (1..16) groups: the copy
+ * in of one group, the collision of the previous one and the copy out of the
+ * one before run at the same time (two copy streams and the context's
+ * stream, joined by events), which pays once a group is still a large batch
+ * (the two-stream workload's 256 cells in 4 chunks).  Successive calls
+ * alternate between two device staging states, so the copy in of a call
+ * overlaps the collision of the one before; with LP_HOST_ASYNC in `flags`
+ * the context's stream does not wait for this call's copy out either, so
+ * the next call's collision overlaps it too.  U_out is complete after
+ * lp_synchronize (or, without LP_HOST_ASYNC, once the context's stream has
+ * reached this call's end), and U_in must not change before then; pinned
+ * (page-locked) host buffers make the copies asynchronous.  The resident
+ * state (lp_set_state) is not used or changed.  More than one chunk needs
+ * LP_FIX_F1 (collisions in passes of cells). */
+#define LP_HOST_ASYNC 1
+lp_status lp_collision_step_host(lp_ctx *ctx, const double *U_in, double *U_out, int chunks, int flags);
 /* Kernel launches in one replay of the captured collision step over every
  * collided cell (its graph's kernel nodes); 0 before the first such step. */
 lp_status lp_collision_graph_kernels(lp_ctx *ctx, int *kernels);

@@ -16,6 +16,8 @@
 
 using lp::V2;
 
+constexpr int kHostChunksMax = 16;  // chunks of lp_collision_step_host
+
 struct lp_ctx {
     lp::Tables T;
     int device = 0;
@@ -118,6 +120,19 @@ struct lp_ctx {
            *gfields = nullptr;
     int *gipiv = nullptr;
     unsigned char *ggate = nullptr;
+    // lp_collision_step_host: two staging states used by alternate calls,
+    // copy streams, per (staging buffer, chunk) events, and the captured
+    // collision of each (staging buffer, cell range)
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    double *hstage[2] = {nullptr, nullptr};
+    int hnext = 0;
+    cudaEvent_t hev_in[2][kHostChunksMax] = {}, hev_col[2][kHostChunksMax] = {}, hev_rest[2] = {},
+                hev_free[2] = {};
+    struct HostGraph {
+        int b, c0, c1;
+        cudaGraphExec_t g;
+    };
+    std::vector<HostGraph> hgraphs;
     // captured step, and captured collision step of all collided cells
     cudaGraphExec_t gexec = nullptr, cgexec = nullptr;
     int cg_kernels = 0;  // kernel nodes of the captured collision step
@@ -814,6 +829,17 @@ void set_init_host(const lp::Tables &T, int kind, double u, std::vector<double> 
 
 void destroy(lp_ctx *c) {
     if (!c) return;
+    if (c->h2d) { cudaStreamSynchronize(c->h2d); cudaStreamDestroy(c->h2d); }
+    if (c->d2h) { cudaStreamSynchronize(c->d2h); cudaStreamDestroy(c->d2h); }
+    for (int b = 0; b < 2; ++b) {
+        for (int j = 0; j < kHostChunksMax; ++j) {
+            if (c->hev_in[b][j]) cudaEventDestroy(c->hev_in[b][j]);
+            if (c->hev_col[b][j]) cudaEventDestroy(c->hev_col[b][j]);
+        }
+        if (c->hev_rest[b]) cudaEventDestroy(c->hev_rest[b]);
+        if (c->hev_free[b]) cudaEventDestroy(c->hev_free[b]);
+    }
+    for (auto &h : c->hgraphs) cudaGraphExecDestroy(h.g);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->cgexec) cudaGraphExecDestroy(c->cgexec);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
@@ -1144,6 +1170,8 @@ lp_status lp_set_stream(lp_ctx *c, void *st) {
 lp_status lp_synchronize(lp_ctx *c) {
     if (!c) return LP_ERR_INVALID;
     LP_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->h2d) LP_CUDA(cudaStreamSynchronize(c->h2d));
+    if (c->d2h) LP_CUDA(cudaStreamSynchronize(c->d2h));
     return LP_OK;
 }
 
@@ -1336,6 +1364,91 @@ lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
         c->cgstream = c->stream;
     }
     LP_CUDA(cudaGraphLaunch(c->cgexec, c->stream));
+    return LP_OK;
+}
+
+lp_status lp_collision_step_host(lp_ctx *c, const double *U_in, double *U_out, int chunks, int flags) {
+    if (!c || !U_in || !U_out || chunks < 1 || chunks > kHostChunksMax || (flags & ~LP_HOST_ASYNC))
+        return LP_ERR_INVALID;
+    if (!c->collide_on || !c->owns_state) return fail(c, LP_ERR_INVALID, "no collision tables or state in this context");
+    const lp::Tables &T = c->T;
+    if (chunks > 1 && !(T.prm.fixes & LP_FIX_F1))
+        return fail(c, LP_ERR_INVALID, "reference slot reads (F1 unfixed) need all cells in one chunk");
+    const size_t rec = (size_t)T.nv3 * 7;  // doubles per spatial cell
+    if (!c->h2d) {
+        LP_TRY(dalloc(c, &c->hstage[0], rec * T.ncell));
+        LP_TRY(dalloc(c, &c->hstage[1], rec * T.ncell));
+        LP_CUDA(cudaStreamCreateWithFlags(&c->h2d, cudaStreamNonBlocking));
+        LP_CUDA(cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            for (int j = 0; j < kHostChunksMax; ++j) {
+                LP_CUDA(cudaEventCreateWithFlags(&c->hev_in[b][j], cudaEventDisableTiming));
+                LP_CUDA(cudaEventCreateWithFlags(&c->hev_col[b][j], cudaEventDisableTiming));
+            }
+            LP_CUDA(cudaEventCreateWithFlags(&c->hev_rest[b], cudaEventDisableTiming));
+            LP_CUDA(cudaEventCreateWithFlags(&c->hev_free[b], cudaEventDisableTiming));
+            LP_CUDA(cudaEventRecord(c->hev_free[b], c->d2h));
+        }
+    }
+    const int ncol = T.ncollide, ncell = T.ncell;
+    const int per = std::max(32, round32((ncol + chunks - 1) / chunks));
+    const int b = c->hnext;
+    c->hnext ^= 1;
+    double *Us = c->hstage[b];
+    // the copies into staging state b start once its last copy out is done:
+    // the previous call's collision (on the other staging state) can still run
+    LP_CUDA(cudaStreamWaitEvent(c->h2d, c->hev_free[b], 0));
+    int nch = 0;
+    for (int c0 = 0; c0 < ncol; c0 += per, ++nch) {
+        const int c1 = std::min(ncol, c0 + per);
+        LP_CUDA(cudaMemcpyAsync(Us + c0 * rec, U_in + c0 * rec, sizeof(double) * rec * (c1 - c0),
+                                cudaMemcpyHostToDevice, c->h2d));
+        LP_CUDA(cudaEventRecord(c->hev_in[b][nch], c->h2d));
+    }
+    if (ncell > ncol) {  // cells that are not collided pass through unchanged
+        LP_CUDA(cudaMemcpyAsync(Us + ncol * rec, U_in + ncol * rec, sizeof(double) * rec * (ncell - ncol),
+                                cudaMemcpyHostToDevice, c->h2d));
+        LP_CUDA(cudaEventRecord(c->hev_rest[b], c->h2d));
+    }
+    // chunk j collides (a captured graph per staging state and cell range, on
+    // the context's stream) once its records are on the device, and is copied
+    // back while chunk j + 1 collides
+    int j = 0;
+    for (int c0 = 0; c0 < ncol; c0 += per, ++j) {
+        const int c1 = std::min(ncol, c0 + per);
+        cudaGraphExec_t g = nullptr;
+        for (auto &h : c->hgraphs)
+            if (h.b == b && h.c0 == c0 && h.c1 == c1) g = h.g;
+        if (!g) {
+            double *keep = c->U;
+            c->U = Us;  // the captured kernels take the staging state
+            cudaGraph_t gr = nullptr;
+            LP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            lp_status st = collide(c, c0, c1);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+            c->U = keep;
+            if (st != LP_OK) { if (gr) cudaGraphDestroy(gr); return st; }
+            if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&g, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+            c->hgraphs.push_back({b, c0, c1, g});
+        }
+        LP_CUDA(cudaStreamWaitEvent(c->stream, c->hev_in[b][j], 0));
+        LP_CUDA(cudaGraphLaunch(g, c->stream));
+        LP_CUDA(cudaEventRecord(c->hev_col[b][j], c->stream));
+        LP_CUDA(cudaStreamWaitEvent(c->d2h, c->hev_col[b][j], 0));
+        LP_CUDA(cudaMemcpyAsync(U_out + c0 * rec, Us + c0 * rec, sizeof(double) * rec * (c1 - c0),
+                                cudaMemcpyDeviceToHost, c->d2h));
+    }
+    if (ncell > ncol) {
+        LP_CUDA(cudaStreamWaitEvent(c->d2h, c->hev_rest[b], 0));
+        LP_CUDA(cudaMemcpyAsync(U_out + ncol * rec, Us + ncol * rec, sizeof(double) * rec * (ncell - ncol),
+                                cudaMemcpyDeviceToHost, c->d2h));
+    }
+    LP_CUDA(cudaEventRecord(c->hev_free[b], c->d2h));
+    // without LP_HOST_ASYNC the context's stream orders after the last copy
+    if (!(flags & LP_HOST_ASYNC)) LP_CUDA(cudaStreamWaitEvent(c->stream, c->hev_free[b], 0));
     return LP_OK;
 }
 

@@ -24,6 +24,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_NO_DEVICE, ERR_STATE = range(6)
 FIX_F1, FIX_F2, FIX_F3, FIX_F11, FIX_F12 = 1, 2, 4, 8, 16
 FIX_DEFAULT = FIX_F1 | FIX_F2 | FIX_F3 | FIX_F11 | FIX_F12
 PREC_FP64, PREC_MIXED = 0, 1
+HOST_ASYNC = 1
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _vp = ctypes.c_void_p
@@ -43,7 +44,7 @@ EXPORTS = [
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
     "lp_autotune", "lp_set_schedule", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
     "lp_slab_create", "lp_stage_device_ptr", "lp_slab_charge", "lp_slab_fields", "lp_slab_advect_stage",
-    "lp_slab_fields_host",
+    "lp_slab_fields_host", "lp_collision_step_host",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -170,6 +171,7 @@ def lib():
         L.lp_slab_fields.argtypes = [_vp, _vp]
         L.lp_slab_advect_stage.argtypes = [_vp, ctypes.c_int]
         L.lp_slab_fields_host.argtypes = [_vp, _dp, _dp, _dp]
+        L.lp_collision_step_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
@@ -341,6 +343,20 @@ class Context:
 
     def collision_step(self, c0=-1, c1=-1):
         self._chk(self.L.lp_collision_step(self.h, int(c0), int(c1)))
+
+    def collision_step_host(self, U_in, U_out, chunks=1, asynchronous=False):
+        """Collision step of host buffers (numpy arrays or pinned torch CPU
+        tensors of float64, ncell*nv^3*7 values), lp_collision_step_host:
+        queued on the context's streams; U_out is complete after
+        synchronize()."""
+        def ptr(a):
+            if isinstance(a, np.ndarray):
+                assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and a.size == self.params.size * 7
+                return a.ctypes.data
+            assert a.dtype.itemsize == 8 and a.is_contiguous() and a.numel() == self.params.size * 7
+            return a.data_ptr()
+        self._chk(self.L.lp_collision_step_host(self.h, _vp(ptr(U_in)), _vp(ptr(U_out)), int(chunks),
+                                                HOST_ASYNC if asynchronous else 0))
 
     def collision_graph_kernels(self):
         """Kernel launches in one replay of the captured collision step over

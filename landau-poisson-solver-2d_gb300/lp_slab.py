@@ -55,15 +55,18 @@ class _DevView:
 class GpuSlab:
     """One rank's slab on the current GPU (lp_slab_create): global x1 rows
     [i1_begin, i1_end) of the grid `params` (an lp_gb300.Params).  The
-    context runs on torch's current stream, so its kernels, the exchanges'
-    copies and the collectives are ordered on one stream."""
+    context runs on `stream` (a torch.cuda.Stream; a new one if None), and
+    SlabSchedule issues the exchanges' copies and collectives on the same
+    stream, so they are ordered with the slab's kernels.  Slabs stepped in
+    one process share one stream."""
 
-    def __init__(self, params, i1_begin, i1_end):
+    def __init__(self, params, i1_begin, i1_end, stream=None):
         import torch
         import lp_gb300 as lp
         self.torch = torch
+        self.stream = stream if stream is not None else torch.cuda.Stream()
         self.ctx = lp.SlabContext(params, i1_begin, i1_end)
-        self.ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+        self.ctx.set_stream(self.stream.cuda_stream)
         self.params = params
         self.nown = i1_end - i1_begin
         self.row = params.nx2 * params.nv ** 3 * 7  # doubles per x1 row
@@ -76,13 +79,16 @@ class GpuSlab:
 
     def set_own_state(self, U_own):
         """Own rows from the host (nown * nx2 * nv^3 * 7 doubles)."""
-        self.buf[0][self.row:(self.nown + 1) * self.row].copy_(
-            self.torch.from_numpy(np.ascontiguousarray(U_own, dtype=np.float64)))
-        self.torch.cuda.synchronize()
+        with self.torch.cuda.stream(self.stream):
+            self.buf[0][self.row:(self.nown + 1) * self.row].copy_(
+                self.torch.from_numpy(np.ascontiguousarray(U_own, dtype=np.float64)))
+        self.stream.synchronize()
 
     def own_state(self):
-        self.torch.cuda.synchronize()
-        return self.buf[0][self.row:(self.nown + 1) * self.row].cpu().numpy()
+        self.stream.synchronize()
+        with self.torch.cuda.stream(self.stream):
+            out = self.buf[0][self.row:(self.nown + 1) * self.row].cpu().numpy()
+        return out
 
     def rows(self, stage):
         b, r, m = self.buf[stage], self.row, self.nown
@@ -173,6 +179,14 @@ class SlabSchedule:
         self.comm = comm
 
     def step(self, nsteps=1):
+        stream = getattr(self.slabs[0], "stream", None)
+        if stream is None:
+            return self._step(nsteps)
+        import torch
+        with torch.cuda.stream(stream):
+            self._step(nsteps)
+
+    def _step(self, nsteps):
         for _ in range(nsteps):
             for stage in range(3):
                 self.comm.exchange([s.rows(stage) for s in self.slabs])

@@ -20,12 +20,14 @@ CASE_2D = dict(nx1=7, nx2=2, nv=6, n=8, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01,
 
 
 def _slabs(lp, kw, nslab, precision, U0=None):
+    import torch
     P = lp.Params(**kw, fixes=FIX_DEFAULT, precision=precision)
     row = P.nx2 * P.nv ** 3 * 7
+    stream = torch.cuda.Stream()  # one stream for every slab of this process
     slabs = []
     for r in range(nslab):
         i0, i1 = slab_bounds(P.nx1, nslab, r)
-        s = GpuSlab(P, i0, i1)
+        s = GpuSlab(P, i0, i1, stream)
         if U0 is None:
             s.set_init(1)
         else:
