@@ -41,10 +41,27 @@ L2_FLUSH_BYTES = 512 << 20
 # from one ncu capture of
 # `bench.py --steps 2 --warmup 1 --no-cpu-baseline --fp64-steps 0`)
 CONTRACT_TRAFFIC_BYTES = 105.24e6 + 100.49e6
-# the same for the kernels of the convolution form, per launch, from one
-# `ncu --set full -k regex:"k_fq_y|k_fq_x12"` capture of that command (None
-# where not captured)
-FQ_TRAFFIC_BYTES = {"k_fq_y": 207.07e6 + 9.76e6, "k_fq_x12": 9.08e6 + 146.21e6}
+PROFILES = os.path.join(ROOT, "profiles")
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+    of `kernel` from the committed ncu summaries under profiles/: the first
+    summary with a line `traffic <kernel>: <read MB> + <write MB> MB` (the
+    capture of the same command, kernel and workload).  Returns (bytes,
+    summary file) or (None, None) when no summary covers the kernel."""
+    import re
+    if not os.path.isdir(PROFILES):
+        return None, None
+    pat = re.compile(r"^traffic\s+" + re.escape(kernel) + r":\s*([0-9.]+)\s*\+\s*([0-9.]+)\s*MB", re.M)
+    for name in sorted(os.listdir(PROFILES)):
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(PROFILES, name)) as f:
+            m = pat.search(f.read())
+        if m:
+            return (float(m.group(1)) + float(m.group(2))) * 1e6, "profiles/" + name
+    return None, None
 
 
 def fq_kernel_model(n, cells):
@@ -299,11 +316,13 @@ WEAK = dict(nx1=24, nx2=1, nv=16, n=16, lv=5.25, lx=4 * np.pi, nu=0.01, dt=0.01,
 WEAK_REFERENCE_S_PER_STEP = 56.7
 
 
-def run_workload(args):
+def run_workload(args, emit=True):
     """Secondary workloads, one JSON line each: `batch` (64 seeded uneven runs
     in one batch, full time steps from the batch's per-step graph, schedules
-    picked by the autotuner) and `twostream` (the large two-stream instance,
-    Nx = 256, N = Nv = 32, full time steps, plus its error against FP64)."""
+    picked by the autotuner), `twostream` (the large two-stream instance,
+    Nx = 256, N = Nv = 32, full time steps, plus its error against FP64) and
+    `weak` (the whole 100-step weak-damping run).  emit=False returns the
+    line instead of printing it."""
     import torch
     import lp_gb300 as lp
     torch.cuda.set_device(0)
@@ -367,6 +386,8 @@ def run_workload(args):
                 "dtype": "f32+f64" if args.precision == "mixed" else "f64",
                 "data": "synthetic (analytic initial state)", "config": cfg, "clocks": clk.summary()}
         line.update(extra)
+        if not emit:
+            return line
         print(json.dumps(line), flush=True)
         return 0
     if args.workload == "batch":
@@ -426,8 +447,26 @@ def run_workload(args):
             "data": "synthetic (seeded analytic initial states)", "config": cfg,
             "clocks": clk.summary()}
     line.update(extra)
+    if not emit:
+        return line
     print(json.dumps(line), flush=True)
     return 0
+
+
+def secondary_lines(args):
+    """Short runs of the secondary workloads for the headline line: the
+    batch of 64 uneven runs and the two-stream instance (3 timed full steps
+    after 2 warm-up steps each, the two-stream error against FP64 after one
+    step) and the whole weak-damping run."""
+    out = {}
+    for name in ("batch", "twostream", "weak"):
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.steps, a.warmup, a.fp64_steps = name, 3, 2, 1
+        try:
+            out[name] = run_workload(a, emit=False)
+        except Exception as e:  # reported, not hidden: the headline line still prints
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
 
 
 def main():
@@ -440,6 +479,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="full time steps of the mixed and FP64 paths compared after the timing")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the short runs of the batch, two-stream and whole-run workloads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="landau64", choices=["landau64", "batch", "twostream", "weak"])
     ap.add_argument("--schedule", default=None,
@@ -618,8 +659,9 @@ def main():
             extra["contraction_kernels"] = kern
             dom = max(kern, key=lambda k: k["ms_per_launch"])
             hbm_frac = dom["gbs"] / peak
+            traffic, traffic_src = profiled_traffic(dom["kernel"])
             roof = {"bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s", "frac": hbm_frac,
-                    "traffic": FQ_TRAFFIC_BYTES.get(dom["kernel"]),
+                    "traffic": traffic, "traffic_source": traffic_src,
                     "algorithmic_bytes": dom["algorithmic_bytes"], "peak_kind": peak_kind,
                     "kernel": dom["kernel"] + " (the largest kernel of the convolution form)",
                     "ms_per_launch": dom["ms_per_launch"]}
@@ -655,6 +697,8 @@ def main():
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "gpu_launches": ctx.collision_graph_kernels() * args.steps}
         line.update(extra)
+        if ws == 1 and not args.no_secondary and args.precision == "mixed":
+            line["secondary"] = secondary_lines(args)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

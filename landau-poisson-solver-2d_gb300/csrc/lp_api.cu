@@ -5,6 +5,7 @@
 #include <cmath>
 #include <type_traits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -89,6 +90,10 @@ struct lp_ctx {
     // stages, lam4[4][5][Bcap]
     float *cf = nullptr;
     double *lam4 = nullptr;
+    // the axis-3 projection pass on the tensor cores (mixed path): its shared
+    // GEMM operand and the device error flag of its bounded waits
+    float *pj3_tab = nullptr;
+    int *tc_err = nullptr;
     // FP32 mode arrays of the four stages (lazy conservation with the
     // convolution form, whose output is FP32-accurate)
     float2 *qf[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -252,6 +257,19 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
     LP_TRY(upload(c, &c->nodeoff, T.nodeoff.data(), T.nodeoff.size()));
     LP_TRY(upload(c, &c->pair_off, T.pair_off.data(), T.pair_off.size()));
     LP_TRY(upload_real<R>(c, &c->tfac, T.tfac));
+    // the axis-3 projection pass on the tensor cores: its shared GEMM operand
+    // from the FP32 factors (LP_PJ3_TC=0 in the environment keeps the
+    // CUDA-core pass, for comparisons)
+    const char *tcenv = std::getenv("LP_PJ3_TC");
+    if (c->mixed && !(tcenv && tcenv[0] == '0') && lp::pj3_tc_np(T.nv) <= 256 &&
+        (T.n == 8 || T.n == 16 || T.n == 24 || T.n == 32)) {
+        std::vector<float> tf(T.tfac.size()), tab;
+        for (size_t i = 0; i < tf.size(); ++i) tf[i] = (float)T.tfac[i];
+        lp::pj3_tc_table(tf.data(), T.n, T.nv, tab);
+        LP_TRY(upload(c, &c->pj3_tab, tab.data(), tab.size()));
+        LP_TRY(dalloc(c, &c->tc_err, 1));
+        LP_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    }
     LP_TRY(upload_real<R>(c, &c->mfwd, T.mfwd));
     LP_TRY(upload_real<R>(c, &c->minv, T.minv));
     if (c->mixed && T.dft_fac_ok && (T.n == 8 || T.n == 16 || T.n == 24 || T.n == 32)) {
@@ -623,7 +641,8 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false, boo
     LP_CUDA(lp::launch_project_inc(c->q[0], c->q[1], c->q[2], c->q[3], T.prm.nu, (const float *)c->tfac, T.n, T.nv,
                                    Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
                                    (float2 *)c->Z, (float *)c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
-                                   lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr, f32 ? c->qf : nullptr));
+                                   lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr, f32 ? c->qf : nullptr,
+                                   c->pj3_tab, c->tc_err));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
     LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.n, T.nv, B, Bp, c->gm_inv,
@@ -1172,6 +1191,12 @@ lp_status lp_synchronize(lp_ctx *c) {
     LP_CUDA(cudaStreamSynchronize(c->stream));
     if (c->h2d) LP_CUDA(cudaStreamSynchronize(c->h2d));
     if (c->d2h) LP_CUDA(cudaStreamSynchronize(c->d2h));
+    if (c->tc_err) {  // a bounded wait of the tensor-core projection that ran out
+        int e = 0;
+        LP_CUDA(cudaMemcpy(&e, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) return fail(c, LP_ERR_CUDA, "tensor-core projection: a bounded wait ran out (code " +
+                                               std::to_string(e) + ")");
+    }
     return LP_OK;
 }
 

@@ -1785,14 +1785,20 @@ template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
                       float *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
-                      const float *cf, const double *lam4, float2 *const *q32) {
+                      const float *cf, const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err) {
     const size_t ts = sizeof(float2) * 3 * N * nv;
     if (nv > kPj1Groups * kPj1Max) return cudaErrorInvalidValue;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_pj3<N, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj3<N, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
     if ((e = cudaFuncSetAttribute(k_pj2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ts))) return e;
-    if (q32)
+    if (tc_tab && pj3_tc_supported(N, nv, Bp)) {
+        // the axis-3 pass as a GEMM on the tensor cores (lp_pjtc.cu)
+        e = q32 ? launch_pj3_tc<float2>(q32[0], q32[1], q32[2], q32[3], nu, rates.nu, tc_tab, N, nv, Bp, Y, cf, lam4,
+                                        tc_err, st)
+                : launch_pj3_tc<double2>(q0, q1, q2, q3, nu, rates.nu, tc_tab, N, nv, Bp, Y, cf, lam4, tc_err, st);
+        if (e) return e;
+    } else if (q32)
         k_pj3<N, float2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(
             q32[0], q32[1], q32[2], q32[3], nu, rates.nu, tfac, nv, Bp, Y, cf, lam4);
     else
@@ -2949,13 +2955,13 @@ cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const doubl
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates, const float *cf,
-                               const double *lam4, float2 *const *q32) {
+                               const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err) {
     const double kfac = 1. / scalev / scaleL / scale3;
     switch (n) {
-    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
-    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
-    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
-    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32);
+    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
+    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
+    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
+    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
     default: break;
     }
     if (cf || q32) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil passes

@@ -196,13 +196,16 @@ cudaError_t launch_moment_finish(const double *tpart, int nchunk, const double *
 int project_inc_blocks(int n, int nv);
 // cf/lam4 (n in {8, 16, 24, 32}): the q_s were not projected; their
 // corrections with lam4[s][5][Bp] are applied in FP32 on load.  q32: the
-// four mode arrays are FP32 complex (q0..q3 unused).
+// four mode arrays are FP32 complex (q0..q3 unused).  tc_tab (the table of
+// pj3_tc_table on the device) runs the axis-3 pass on the tensor cores where
+// pj3_tc_supported, with tc_err its device error flag.
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{},
                                const float *cf = nullptr, const double *lam4 = nullptr,
-                               float2 *const *q32 = nullptr);
+                               float2 *const *q32 = nullptr, const float *tc_tab = nullptr,
+                               int *tc_err = nullptr);
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
@@ -262,6 +265,23 @@ struct AdvectDev {
 cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const double *Us, const float *Uin_f32,
                               const double *fields, int stage, double *Uout, float *Uout_f32, double *part,
                               cudaStream_t st);
+
+// ---- axis-3 DG projection pass on the tensor cores (lp_pjtc.cu) ----
+// Columns of the shared GEMM operand (6 nv rounded up to a multiple of 16).
+int pj3_tc_np(int nv);
+// n in {8, 16, 24, 32}, 6 nv <= 256, Bp one of 32, 64 or a multiple of 128.
+bool pj3_tc_supported(int n, int nv, int Bp);
+size_t pj3_tc_table_floats(int n, int nv);
+size_t pj3_tc_smem(int n, int nv);
+// The shared operand from the per-axis factors tfac ([3][n][nv] complex FP32):
+// TF32 head then tail, in the MMA's shared-memory layout.
+void pj3_tc_table(const float *tfac, int n, int nv, std::vector<float> &out);
+// k_pj3 on the tensor cores: the same inputs and output Y; err (device) is
+// set to 1 or 2 when a bounded wait for the shared operand or the MMAs ran out.
+template <typename QT>
+cudaError_t launch_pj3_tc(const QT *q0, const QT *q1, const QT *q2, const QT *q3, double nu, const double *cnu,
+                          const float *btab, int n, int nv, int Bp, float2 *Y, const float *cf, const double *lam4,
+                          int *err, cudaStream_t st);
 
 // ---- mixed-path advection (increment form of SSP-RK3, FP32 fluxes) ----
 // FP32 copy of the state and FP64 charge partials of every group of 128
