@@ -683,6 +683,23 @@ def main():
                     "frac": contract_tflops / fp32_peak if fp32_peak else None,
                     "peak_kind": "measured (FMA-chain microbenchmark)", "fp64_peak_tflops": fp64_peak}
         extra["contraction_ms"] = t_contract_ms
+        # the step against the per-cell-step figures of the workload's
+        # algorithmic counts: HBM bytes Nv^3 (7 + 5) 8 (read the records,
+        # write the 5 collided coefficients) and the FFT form's FLOP
+        # 4 [15 * 5 m log2 m + 7 * 8 m] with m = (2N)^3, plus the separable
+        # projection 8 * 5 (Nv N^3 + Nv^2 N^2 + Nv^3 N)
+        nv_, n_ = WORKLOAD["nv"], WORKLOAD["n"]
+        m_ = (2 * n_) ** 3
+        flop_cs = 4 * (15 * 5 * m_ * np.log2(m_) + 7 * 8 * m_) + 8 * 5 * (nv_ * n_ ** 3 + nv_ ** 2 * n_ ** 2 + nv_ ** 3 * n_)
+        bytes_cs = nv_ ** 3 * 12 * 8
+        step_s = t_max / args.steps
+        extra["step_roofline_per_cell_step_counts"] = {
+            "bytes_per_cell_step": bytes_cs, "flop_per_cell_step": float(flop_cs),
+            "hbm_gbs": bytes_cs * cells / step_s / 1e9, "hbm_frac": bytes_cs * cells / step_s / 1e9 / peak,
+            "tflops": flop_cs * cells / step_s / 1e12,
+            "fp32_frac": (flop_cs * cells / step_s / 1e12) / fp32_peak if fp32_peak else None,
+            "note": "whole collision step; the step moves its intermediates through HBM and L2, so the per-step "
+                    "HBM figure is far below the copy peak while the FLOP figure is near the FP32 FMA peak"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

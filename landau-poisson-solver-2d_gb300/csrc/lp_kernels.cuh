@@ -269,7 +269,7 @@ cudaError_t launch_flux_stage(const AdvectDev &ad, const double *U0, const doubl
 // ---- axis-3 DG projection pass on the tensor cores (lp_pjtc.cu) ----
 // Columns of the shared GEMM operand (6 nv rounded up to a multiple of 16).
 int pj3_tc_np(int nv);
-// n in {8, 16, 24, 32}, 6 nv <= 256, Bp one of 32, 64 or a multiple of 128.
+// n in {8, 16, 24, 32}, 6 nv <= 256, Bp a multiple of 32.
 bool pj3_tc_supported(int n, int nv, int Bp);
 size_t pj3_tc_table_floats(int n, int nv);
 size_t pj3_tc_smem(int n, int nv);

@@ -33,17 +33,13 @@ namespace {
 
 constexpr int kRows = 128;
 
-// row r of tile `tile` -> (pencil, cell) for Bp cells per pencil
+// row r of tile `tile` -> (pencil, cell): the rows run over (pencil, cell)
+// pairs in the arrays' own order, 128 per tile; Bp is a multiple of 32, so
+// the 32 rows of a warp are 32 consecutive cells of one pencil
 __device__ __forceinline__ void tile_row(int tile, int r, int Bp, int &pid, int &c) {
-    if (Bp <= kRows) {
-        const int pt = kRows / Bp;  // pencils per tile
-        pid = tile * pt + r / Bp;
-        c = r % Bp;
-    } else {
-        const int tp = Bp / kRows;  // tiles per pencil
-        pid = tile / tp;
-        c = (tile % tp) * kRows + r;
-    }
+    const long long g = (long long)tile * kRows + r;
+    pid = (int)(g / Bp);
+    c = (int)(g % Bp);
 }
 
 template <int N, typename QT>
@@ -183,7 +179,7 @@ int pj3_tc_np(int nv) { return ((6 * nv + 15) / 16) * 16; }
 bool pj3_tc_supported(int n, int nv, int Bp) {
     if (!(n == 8 || n == 16 || n == 24 || n == 32)) return false;
     if (pj3_tc_np(nv) > 256) return false;
-    if (!(Bp == 32 || Bp == 64 || Bp == 128 || Bp % 128 == 0)) return false;
+    if (Bp < 32 || Bp % 32) return false;
     return ((long long)n * n * Bp) % kRows == 0;
 }
 

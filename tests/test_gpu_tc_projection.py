@@ -1,9 +1,10 @@
 """The axis-3 DG projection pass on the tensor cores (tcgen05.mma, TF32
 operands split into head and tail) against the CUDA-core pass it replaces
 (LP_PJ3_TC=0 at context creation) and against the FP64 path: one mixed
-collision step at n = 16 and n = 24 (both Bp layouts of the tiles: 64 and
-128 cells per pencil segment), the state within 1e-9 of the CUDA-core pass
-and 1e-6 of FP64, mass, momentum and energy kept to 1e-12."""
+collision step at n = 16 and n = 24 with 64, 128 and 96 cells per pass (the
+128-row tiles hold two pencils, one pencil, or a pencil and a part), the
+state within 1e-9 of the CUDA-core pass and 1e-6 of FP64, mass, momentum and
+energy kept to 1e-12."""
 from __future__ import annotations
 
 import os
@@ -29,8 +30,8 @@ def _ctx(lp, kw, precision, tc):
             os.environ["LP_PJ3_TC"] = old
 
 
-@pytest.mark.parametrize("nx1,nv,n", [(64, 24, 24), (128, 16, 16), (40, 8, 16)],
-                         ids=["n24-64cells", "n16-128cells", "n16-nv8-64cells"])
+@pytest.mark.parametrize("nx1,nv,n", [(64, 24, 24), (128, 16, 16), (40, 8, 16), (80, 8, 16)],
+                         ids=["n24-64cells", "n16-128cells", "n16-nv8-40cells", "n16-nv8-80cells"])
 def test_tc_projection_collision_step(gpu_lib, nx1, nv, n):
     lp = gpu_lib
     kw = dict(nx1=nx1, nx2=1, nv=nv, n=n, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.005, a_amp=0.5, k_wave=0.5)
