@@ -92,7 +92,7 @@ struct lp_ctx {
     double *lam4 = nullptr;
     // the axis-3 projection pass on the tensor cores (mixed path): its shared
     // GEMM operand and the device error flag of its bounded waits
-    float *pj3_tab = nullptr;
+    float *pj3_tab = nullptr, *pj1_tab = nullptr;
     int *tc_err = nullptr;
     // FP32 mode arrays of the four stages (lazy conservation with the
     // convolution form, whose output is FP32-accurate)
@@ -257,9 +257,9 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
     LP_TRY(upload(c, &c->nodeoff, T.nodeoff.data(), T.nodeoff.size()));
     LP_TRY(upload(c, &c->pair_off, T.pair_off.data(), T.pair_off.size()));
     LP_TRY(upload_real<R>(c, &c->tfac, T.tfac));
-    // the axis-3 projection pass on the tensor cores: its shared GEMM operand
-    // from the FP32 factors (LP_PJ3_TC=0 in the environment keeps the
-    // CUDA-core pass, for comparisons)
+    // the axis-3 and axis-1 projection passes on the tensor cores: their
+    // shared GEMM operands from the FP32 factors (LP_PJ3_TC=0 in the
+    // environment keeps the CUDA-core passes, for comparisons)
     const char *tcenv = std::getenv("LP_PJ3_TC");
     if (c->mixed && !(tcenv && tcenv[0] == '0') && lp::pj3_tc_np(T.nv) <= 256 &&
         (T.n == 8 || T.n == 16 || T.n == 24 || T.n == 32)) {
@@ -267,6 +267,10 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
         for (size_t i = 0; i < tf.size(); ++i) tf[i] = (float)T.tfac[i];
         lp::pj3_tc_table(tf.data(), T.n, T.nv, tab);
         LP_TRY(upload(c, &c->pj3_tab, tab.data(), tab.size()));
+        if (T.nv <= 32 && T.nv % 2 == 0) {
+            lp::pj1_tc_table(tf.data(), T.n, T.nv, tab);
+            LP_TRY(upload(c, &c->pj1_tab, tab.data(), tab.size()));
+        }
         LP_TRY(dalloc(c, &c->tc_err, 1));
         LP_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
     }
@@ -642,7 +646,7 @@ lp_status project_fused(lp_ctx *c, int c0, int B, int Bp, bool lazy = false, boo
                                    Bp, B, T.prm.dt, T.scalev, T.scaleL, T.scale3, (float2 *)c->Qc, (float2 *)c->Y,
                                    (float2 *)c->Z, (float *)c->dU, c->incpart, T.prm.lv, T.dv, c->stream, rates_at(c, c0),
                                    lazy ? c->cf : nullptr, lazy ? c->lam4 : nullptr, f32 ? c->qf : nullptr,
-                                   c->pj3_tab, c->tc_err));
+                                   c->pj3_tab, c->tc_err, c->pj1_tab));
     if (tst != c->stream) LP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     const double kfac = 1. / T.scalev / T.scaleL / T.scale3;
     LP_CUDA(lp::launch_lambda_inc(target ? c->mtpart : nullptr, c->nchunk, c->incpart, T.n, T.nv, B, Bp, c->gm_inv,

@@ -59,4 +59,22 @@ __device__ __forceinline__ double f32_to_f64_bits(float f) {
         (long long)(((unsigned long long)sign << 32) | (ee << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
+// A sum of FP32 terms as an unevaluated pair hi + lo: each term enters by
+// an error-free two-sum (Knuth), a weighted term w x as the exact pair
+// (w x rounded, its FMA residual).
+struct DFSum {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x), bp = __fsub_rn(s, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
+        hi = s;
+    }
+    __device__ __forceinline__ void addw(float w, float x) {
+        const float p = __fmul_rn(w, x);
+        add(p);
+        lo = __fadd_rn(lo, fmaf(w, x, -p));
+    }
+    __device__ __forceinline__ double get() const { return f32_to_f64_bits(hi) + f32_to_f64_bits(lo); }
+};
+
 }  // namespace lp

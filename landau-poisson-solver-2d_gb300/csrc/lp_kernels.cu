@@ -1603,23 +1603,6 @@ __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const
     }
 }
 
-// A sum of FP32 terms as an unevaluated pair hi + lo: each term enters by
-// an error-free two-sum (Knuth), a weighted term w x as the exact pair
-// (w x rounded, its FMA residual).
-struct DFSum {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        const float s = __fadd_rn(hi, x), bp = __fsub_rn(s, hi);
-        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
-        hi = s;
-    }
-    __device__ __forceinline__ void addw(float w, float x) {
-        const float p = __fmul_rn(w, x);
-        add(p);
-        lo = __fadd_rn(lo, fmaf(w, x, -p));
-    }
-    __device__ __forceinline__ double get() const { return f32_to_f64_bits(hi) + f32_to_f64_bits(lo); }
-};
 
 // Per (j2, j3, cell) pencil, four warps each take a group of JG consecutive
 // j1 outputs (JG even, 4 JG >= nv).  The block's five source pencils Z0..Z4
@@ -1785,7 +1768,8 @@ template <int N>
 cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                       const float *tfac, int nv, int Bp, int B, double dt, double kfac, float2 *Y, float2 *Z,
                       float *Inc, double *part, double lv, double dv, cudaStream_t st, Rates rates,
-                      const float *cf, const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err) {
+                      const float *cf, const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err,
+                      const float *tc_tab1) {
     const size_t ts = sizeof(float2) * 3 * N * nv;
     if (nv > kPj1Groups * kPj1Max) return cudaErrorInvalidValue;
     cudaError_t e;
@@ -1805,6 +1789,10 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
         k_pj3<N, double2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac,
                                                                                 nv, Bp, Y, cf, lam4);
     k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
+    if (tc_tab1 && pj1_tc_supported(N, nv, Bp)) {
+        // the axis-1 pass as GEMMs on the tensor cores (lp_pjtc.cu)
+        return launch_pj1_tc(Z, tc_tab1, N, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, tc_err, st);
+    }
     const dim3 g1((nv * nv + kPj1Pen - 1) / kPj1Pen, Bp / 32);
     const int jg = 2 * ((nv + 2 * kPj1Groups - 1) / (2 * kPj1Groups));
     switch (jg) {
@@ -2955,13 +2943,14 @@ cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const doubl
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates, const float *cf,
-                               const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err) {
+                               const double *lam4, float2 *const *q32, const float *tc_tab, int *tc_err,
+                               const float *tc_tab1) {
     const double kfac = 1. / scalev / scaleL / scale3;
     switch (n) {
-    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
-    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
-    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
-    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err);
+    case 8: return launch_pj<8>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err, tc_tab1);
+    case 16: return launch_pj<16>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err, tc_tab1);
+    case 24: return launch_pj<24>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err, tc_tab1);
+    case 32: return launch_pj<32>(q0, q1, q2, q3, nu, tfac, nv, Bp, B, dt, kfac, Y, Z, Inc, part, lv, dv, st, rates, cf, lam4, q32, tc_tab, tc_err, tc_tab1);
     default: break;
     }
     if (cf || q32) return cudaErrorInvalidValue;  // lazy conservation needs the register-pencil passes

@@ -198,14 +198,15 @@ int project_inc_blocks(int n, int nv);
 // corrections with lam4[s][5][Bp] are applied in FP32 on load.  q32: the
 // four mode arrays are FP32 complex (q0..q3 unused).  tc_tab (the table of
 // pj3_tc_table on the device) runs the axis-3 pass on the tensor cores where
-// pj3_tc_supported, with tc_err its device error flag.
+// pj3_tc_supported, tc_tab1 (pj1_tc_table) the axis-1 pass where
+// pj1_tc_supported, with tc_err their device error flag.
 cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const double2 *q2, const double2 *q3, double nu,
                                const float *tfac, int n, int nv, int Bp, int B, double dt, double scalev,
                                double scaleL, double scale3, float2 *Qc, float2 *Y, float2 *Z, float *Inc,
                                double *part, double lv, double dv, cudaStream_t st, Rates rates = Rates{},
                                const float *cf = nullptr, const double *lam4 = nullptr,
                                float2 *const *q32 = nullptr, const float *tc_tab = nullptr,
-                               int *tc_err = nullptr);
+                               int *tc_err = nullptr, const float *tc_tab1 = nullptr);
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates = Rates{});
@@ -282,6 +283,17 @@ template <typename QT>
 cudaError_t launch_pj3_tc(const QT *q0, const QT *q1, const QT *q2, const QT *q3, double nu, const double *cnu,
                           const float *btab, int n, int nv, int Bp, float2 *Y, const float *cf, const double *lam4,
                           int *err, cudaStream_t st);
+
+// The axis-1 pass (k_pj1's increments and moment partials) on the tensor
+// cores: n in {8, 16, 24, 32}, even nv <= 32, Bp a multiple of 32.
+int pj1_tc_nvp(int nv);
+bool pj1_tc_supported(int n, int nv, int Bp);
+size_t pj1_tc_table_floats(int n, int nv);
+size_t pj1_tc_smem(int n, int nv);
+void pj1_tc_table(const float *tfac, int n, int nv, std::vector<float> &out);
+cudaError_t launch_pj1_tc(const float2 *Z, const float *btab, int n, int nv, int Bp, int B, double dt, double kfac,
+                          const double *cdt, double dv, double lv, float *Inc, double *part, int *err,
+                          cudaStream_t st);
 
 // ---- mixed-path advection (increment form of SSP-RK3, FP32 fluxes) ----
 // FP32 copy of the state and FP64 charge partials of every group of 128
