@@ -239,13 +239,20 @@ lp_status lp_state_restart(lp_ctx *ctx, const char *path);
  * LP_FIX_F3; Poisson matrix of order 3*nx1*nx2 <= 4096), evaluated at the
  * resident state, which they leave unchanged.  Adjoint vectors are DEVICE
  * pointers of ncell*nv^3*7 doubles in the state's layout.
- *   collision step: the bilinear ComputeQ linearised (a correlation with the
- *     pair weights), the transposed transforms, the self-adjoint conservation
+ *   collision step: the bilinear ComputeQ linearised (correlations of the
+ *     adjoint with the convolution form's arrays, lp_set_adjoint_form), the
+ *     transposed transforms, the self-adjoint conservation
  *     projection and the transposed DG projection, through the RK4 stages;
  *   advection step: the transposed upwind DG flux of each SSP-RK3 stage and
  *     the transposed LDG Poisson solve of its field;
  *   field energy J = 1/2 sum_cells dx dy (E_0^2 + (E_1^2 + E_2^2)/12) over E_x
  *     and E_y of the Poisson solve on the state. */
+/* The form of ComputeQ's VJP in the collision step's adjoint: 0 (default)
+ * the two families of correlations of lam_q with the omega-factor arrays of
+ * the convolution form, by 3n/2-point DFTs along the three axes; 1 the
+ * gather over the pair table of the weighted sum.  Both give the transpose of
+ * source/collisionRoutines_1.cpp:739-822 linearised at F. */
+lp_status lp_set_adjoint_form(lp_ctx *ctx, int form);
 /* J of the resident state and, when lam_U_dev is not NULL, dJ/dU. */
 lp_status lp_field_energy(lp_ctx *ctx, double *J, double *lam_U_dev);
 /* lam_in = (d collision step / dU)^T lam_out; *dJ_dnu (optional) = the

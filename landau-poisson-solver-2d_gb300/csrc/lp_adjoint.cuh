@@ -10,6 +10,19 @@ namespace lp {
 // transpose of the weighted contraction of ComputeQ linearised at F).
 cudaError_t launch_qvjp(const double2 *F, const double2 *lq, const double *P, const int *pair_off, int n, int Bp,
                         double2 *lF, cudaStream_t st);
+// The same VJP as correlations of lam_q with the conjugated a_p = C_p F and
+// b_p = w_p F of the convolution form, by M = 3n/2-point DFTs along the
+// three axes (lp_corr.cu): Cp the seven omega factors [7][n^3], Wf (M x n)
+// and Wi (n x M, the 1/M and the output shift folded in) per-axis matrices,
+// scratch of corr_scratch_elems(n) values; cells [0, B) of the Bp-strided
+// arrays, in chunks of corr_cells().
+int corr_cells();
+size_t corr_scratch_elems(int n);
+void corr_tables(const double *shat, const double *ahat, const double *cw, double h_eta, int n, std::vector<double> &Cp,
+                 std::vector<double> &Wf, std::vector<double> &Wi);
+cudaError_t launch_qvjp_corr(const double2 *F, const double2 *lq, const double *Cp, const double2 *Wf,
+                             const double2 *Wi, int n, int Bp, int B, double2 *lF, double2 *scratch,
+                             cudaStream_t st);
 // Transpose of the DG projection: lam_tp [5][nv^3][Bp] -> lam_Qc [n^3][Bp]
 // (lZ, lY scratch as the forward's Z, Y).
 cudaError_t launch_project_vjp(const double *ltp, const double *tf, int n, int nv, int Bp, double2 *lZ, double2 *lY,

@@ -109,6 +109,11 @@ struct lp_ctx {
         int *nfirst = nullptr, *ncount = nullptr;
         double *Ainv = nullptr, *lrt = nullptr, *lamF = nullptr, *lphix = nullptr, *lphiy = nullptr, *J = nullptr;
         double *dnu = nullptr;  // per collided cell
+        // ComputeQ's VJP: 0 the correlation form (omega factors Cp, per-axis
+        // DFT matrices Wf / Wi, scratch cscr), 1 the pair-table gather
+        int qvjp_form = 0;
+        double *Cp = nullptr;
+        double2 *Wf = nullptr, *Wi = nullptr, *cscr = nullptr;
         double *lU = nullptr, *lU1 = nullptr, *lUt = nullptr, *lH = nullptr, *lC = nullptr, *Ukeep = nullptr;
         std::vector<double *> ck;  // checkpoints
         double *seg = nullptr;     // states of one checkpoint segment
@@ -1000,6 +1005,17 @@ lp_status adj_setup(lp_ctx *c) {
     LP_TRY(dalloc(c, &A.lH, rec));
     LP_TRY(dalloc(c, &A.lC, rec));
     LP_TRY(dalloc(c, &A.Ukeep, rec));
+    {
+        std::vector<double> Cp, Wf, Wi;
+        lp::corr_tables(T.shat.data(), T.ahat.data(), T.cw.data(), T.h_eta, n, Cp, Wf, Wi);
+        LP_TRY(upload(c, &A.Cp, Cp.data(), Cp.size()));
+        double *wf = nullptr, *wi = nullptr;
+        LP_TRY(upload(c, &wf, Wf.data(), Wf.size()));
+        LP_TRY(upload(c, &wi, Wi.data(), Wi.size()));
+        A.Wf = reinterpret_cast<double2 *>(wf);
+        A.Wi = reinterpret_cast<double2 *>(wi);
+        LP_TRY(dalloc(c, &A.cscr, lp::corr_scratch_elems(n)));
+    }
     A.ready = true;
     return LP_OK;
 }
@@ -1018,7 +1034,10 @@ lp_status adj_q_back(lp_ctx *c, const double2 *F, double2 *lq, int Bp, double *l
     auto &A = c->adj;
     const long long N = (long long)T.n3 * Bp;
     LP_CUDA(lp::launch_conserve(lq, c->c1, c->c2, c->cct, T.n3, Bp, c->cpart, c->nchunk, c->lam, c->stream));
-    LP_CUDA(lp::launch_qvjp(F, lq, (const double *)c->P, c->pair_off, T.n, Bp, A.lF, c->stream));
+    if (A.qvjp_form == 0)
+        LP_CUDA(lp::launch_qvjp_corr(F, lq, A.Cp, A.Wf, A.Wi, T.n, Bp, Bp, A.lF, A.cscr, c->stream));
+    else
+        LP_CUDA(lp::launch_qvjp(F, lq, (const double *)c->P, c->pair_off, T.n, Bp, A.lF, c->stream));
     LP_CUDA(lp::launch_fwd_complex<double>(A.lF, (double2 *)c->t1, A.tq, A.mfH, T.n, Bp, c->stream));
     LP_CUDA(lp::launch_add_re(lf, beta, A.tq, 1.0, N, c->stream));
     return LP_OK;
@@ -2109,6 +2128,12 @@ lp_status lp_state_restart(lp_ctx *c, const char *path) {
 }
 
 // ---- adjoint ----
+lp_status lp_set_adjoint_form(lp_ctx *c, int form) {
+    if (!c || (form != 0 && form != 1)) return LP_ERR_INVALID;
+    c->adj.qvjp_form = form;
+    return LP_OK;
+}
+
 lp_status lp_field_energy(lp_ctx *c, double *J, double *lamU) {
     if (!c || !J) return LP_ERR_INVALID;
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");

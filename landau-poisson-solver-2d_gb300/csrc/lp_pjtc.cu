@@ -163,8 +163,9 @@ __global__ void __launch_bounds__(kThreads) k_pj3_tc(const QT *__restrict__ q0, 
         }
         tc::mma_commit(&mbar[1]);
     }
-    const bool done = tc::mbar_wait(&mbar[1], 0);
+    bool done = tc::mbar_wait(&mbar[1], 0);
     if (!done) atomicExch(err, 2);
+    done = __all_sync(0xffffffffu, done);  // the TMEM loads below are warp-wide
     tc::fence_after_sync();
     if (done) {
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), the two warps
@@ -305,10 +306,14 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
         atomicExch(err, 2);
     }
     tc::fence_after_sync();
-    // epilogue: this thread's row and j1 in [16 half, 16 half + 16)
+    // epilogue: this thread's row and j1 in [16 half, 16 half + 16).  The
+    // TMEM loads are warp-wide (.sync.aligned): every lane of a warp takes
+    // them or none does (j0 and the warp's agreement on `ok` are uniform;
+    // whether a lane's cell is a padding cell is not)
     double m[5] = {0, 0, 0, 0, 0};
     const int j0 = 16 * half;
-    if (ok && c < B && j0 < nv) {
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok && j0 < nv) {
         const uint32_t lane_base = tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)j0;
         float a0[16], a1[16], a4[16], a2[16], a3[16];
         tc::tmem_ld16(lane_base, a0);
@@ -316,6 +321,7 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
         tc::tmem_ld16(lane_base + (uint32_t)(2 * nvp), a4);
         tc::tmem_ld16(lane_base + (uint32_t)(3 * nvp), a2);
         tc::tmem_ld16(lane_base + (uint32_t)(4 * nvp), a3);
+      if (c < B) {
         const int j2 = pq / nv, j3 = pq - j2 * nv;
         const float sf = (float)((cdt ? cdt[c] : dt) * kfac);
         DFSum S[5], T0, T1, T4, V0, V4;
@@ -349,6 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
         m[3] = G3 * S04 + mr.dv12 * S3;
         m[4] = B0 + (G2233 + mr.dv2q) * S0 + mr.dv6 * (A1 + G2 * S2 + G3 * S3) + mr.c19 * S4 + 0.25 * B4 +
                0.25 * G2233 * S4;
+      }
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) red[q][t] = m[q];

@@ -44,7 +44,7 @@ EXPORTS = [
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
     "lp_autotune", "lp_set_schedule", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
     "lp_slab_create", "lp_stage_device_ptr", "lp_slab_charge", "lp_slab_fields", "lp_slab_advect_stage",
-    "lp_slab_fields_host", "lp_collision_step_host",
+    "lp_slab_fields_host", "lp_collision_step_host", "lp_set_adjoint_form",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -172,6 +172,7 @@ def lib():
         L.lp_slab_advect_stage.argtypes = [_vp, ctypes.c_int]
         L.lp_slab_fields_host.argtypes = [_vp, _dp, _dp, _dp]
         L.lp_collision_step_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+        L.lp_set_adjoint_form.argtypes = [_vp, ctypes.c_int]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
@@ -414,6 +415,10 @@ class Context:
 
     def state_restart(self, path):
         self._chk(self.L.lp_state_restart(self.h, path.encode()))
+
+    def set_adjoint_form(self, form):
+        """ComputeQ's VJP in the adjoint: 0 correlations (default), 1 pair-table gather."""
+        self._chk(self.L.lp_set_adjoint_form(self.h, int(form)))
 
     # adjoint: device pointers (e.g. torch tensors' data_ptr()) of state-sized
     # FP64 vectors

@@ -216,3 +216,23 @@ def test_autograd_composition_matches_checkpointed_gradient(gpu_lib):
     (gU,) = torch.autograd.grad(J, U)
     assert abs(J.item() - J_ref) <= 1e-12 * abs(J_ref)
     assert torch.linalg.norm(gU - g) <= 1e-10 * torch.linalg.norm(g)
+
+
+@pytest.mark.parametrize("n,nv", [(8, 8), (16, 6), (24, 4)], ids=["n8", "n16", "n24"])
+def test_collision_vjp_forms_agree(gpu_lib, n, nv):
+    """ComputeQ's VJP as correlations of the adjoint with the convolution
+    form's omega-factor arrays (3n/2-point DFTs, the default) against the
+    gather over the pair table of the weighted sum, through one collision
+    step's adjoint (40 cells: two 32-cell chunks of the correlation form)."""
+    lp = gpu_lib
+    ctx = _ctx(lp, nx1=40, n=n, nv=nv)
+    ctx.advect_step()
+    U = ctx.get_state()
+    w = np.random.default_rng(11).standard_normal(U.size)
+    out = {}
+    for form in (1, 0):
+        ctx.set_adjoint_form(form)
+        out[form] = _vjp(ctx, ctx.collision_vjp, U, w)
+    (l1, d1), (l0, d0) = out[1], out[0]
+    assert np.linalg.norm(l0 - l1) <= 1e-12 * np.linalg.norm(l1)
+    assert abs(d0 - d1) <= 1e-12 * abs(d1)
