@@ -1788,7 +1788,12 @@ cudaError_t launch_pj(const double2 *q0, const double2 *q1, const double2 *q2, c
     else
         k_pj3<N, double2><<<dim3((N * N + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(q0, q1, q2, q3, nu, rates.nu, tfac,
                                                                                 nv, Bp, Y, cf, lam4);
-    k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
+    if (tc_tab && pj2_tc_supported(N, nv, Bp)) {
+        // the axis-2 pass on the tensor cores (lp_pjtc.cu), with the axis-3 table
+        if ((e = launch_pj2_tc(Y, tc_tab, N, nv, Bp, Z, tc_err, st))) return e;
+    } else {
+        k_pj2<N><<<dim3((N * nv + 3) / 4, Bp / 32), dim3(32, 4), ts, st>>>(Y, tfac, nv, Bp, Z);
+    }
     if (tc_tab1 && pj1_tc_supported(N, nv, Bp)) {
         // the axis-1 pass as GEMMs on the tensor cores (lp_pjtc.cu)
         return launch_pj1_tc(Z, tc_tab1, N, nv, Bp, B, dt, kfac, rates.dt, dv, lv, Inc, part, tc_err, st);

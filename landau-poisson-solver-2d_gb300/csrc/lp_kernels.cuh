@@ -284,6 +284,12 @@ cudaError_t launch_pj3_tc(const QT *q0, const QT *q1, const QT *q2, const QT *q3
                           const float *btab, int n, int nv, int Bp, float2 *Y, const float *cf, const double *lam4,
                           int *err, cudaStream_t st);
 
+// The axis-2 pass (k_pj2) on the tensor cores with the axis-3 pass's table:
+// n in {8, 16, 24, 32}, nv in {8, 16, 24}, Bp a multiple of 32.
+bool pj2_tc_supported(int n, int nv, int Bp);
+size_t pj2_tc_smem(int n, int nv);
+cudaError_t launch_pj2_tc(const float2 *Y, const float *btab, int n, int nv, int Bp, float2 *Z, int *err,
+                          cudaStream_t st);
 // The axis-1 pass (k_pj1's increments and moment partials) on the tensor
 // cores: n in {8, 16, 24, 32}, even nv <= 32, Bp a multiple of 32.
 int pj1_tc_nvp(int nv);

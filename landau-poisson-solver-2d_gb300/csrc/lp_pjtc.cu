@@ -375,7 +375,135 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
     if (w == 0) tc::tmem_free(tmem, 256u);
 }
 
+// ---------------------------------------------------------------- axis 2
+// The middle pass (the CUDA-core version is k_pj2): per (pencil (k1, j3),
+// cell) the sources Y0, Y1, Y2 along k2 give Z_p(j2) = sum_k2 T_f(k2, j2)
+// Y_a(k2) for (a, f) = (0, 0), (0, 1), (0, 2), (1, 0), (2, 0), p = 0..4 --
+// complex GEMMs with the axis-3 pass's shared operand (its first 2 nv
+// columns are T0's): Y0 times all 6 nv columns into TMEM [Z0 | Z1 | Z2], Y1
+// and Y2 times T0's 2 nv columns into [Z3], [Z4] (10 nv <= 256 columns).
+// The sources pass through one A tile in turn, as in the axis-1 pass.
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_pj2_tc(const float2 *__restrict__ Y, const float *__restrict__ btab,
+                                                     int nv, int Bp, float2 *__restrict__ Z, int *__restrict__ err) {
+    constexpr int K = 2 * N, KC = K / 4, NH = N / 2;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const uint32_t bbytes = (uint32_t)6 * nv * K * 4;
+    unsigned char *Bhi = sm, *Blo = sm + bbytes, *Ahi = sm + 2 * bbytes, *Alo = Ahi + kRows * K * 4;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tslot;
+    const int t = threadIdx.x, w = t >> 5, row = t & (kRows - 1), half = t >> 7;
+    if (t == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (w == 0) tc::tmem_alloc(&tslot, 256u);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot;
+    if (t == 0) {
+        tc::mbar_expect_tx(&mbar[0], 2 * bbytes);
+        tc::bulk_g2s(Bhi, btab, 2 * bbytes, &mbar[0]);
+    }
+    int pen, c;
+    tile_row(blockIdx.x, row, Bp, pen, c);
+    const int k1 = pen / nv, j3 = pen - k1 * nv;
+    const long long ys = (long long)N * N * nv * Bp, kstride = (long long)nv * Bp;
+    const float2 *yrow = Y + (((long long)k1 * N + half * NH) * nv + j3) * Bp + c;
+    bool ok = true, have_b = true;
+    for (int a = 0; a < 3; ++a) {
+        float2 y[NH];
+#pragma unroll
+        for (int k = 0; k < NH; ++k) y[k] = yrow[a * ys + (long long)k * kstride];
+        if (a > 0 && !tc::mbar_wait(&mbar[1], (uint32_t)((a - 1) & 1))) {
+            ok = false;
+            atomicExch(err, 2);
+        }
+#pragma unroll
+        for (int k = 0; k < NH; k += 4) {
+            float4 hr, lr, hi4, li4;
+            float *phr = &hr.x, *plr = &lr.x, *phi = &hi4.x, *pli = &li4.x;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                phr[u] = tc::tf32_rna(y[k + u].x);
+                plr[u] = tc::tf32_rna(y[k + u].x - phr[u]);
+                phi[u] = tc::tf32_rna(y[k + u].y);
+                pli[u] = tc::tf32_rna(y[k + u].y - phi[u]);
+            }
+            const int kk = half * NH + k;
+            *reinterpret_cast<float4 *>(Ahi + tc::core_off(row, kk, KC)) = hr;
+            *reinterpret_cast<float4 *>(Alo + tc::core_off(row, kk, KC)) = lr;
+            *reinterpret_cast<float4 *>(Ahi + tc::core_off(row, N + kk, KC)) = hi4;
+            *reinterpret_cast<float4 *>(Alo + tc::core_off(row, N + kk, KC)) = li4;
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (t == 0) {
+            if (a == 0 && !tc::mbar_wait(&mbar[0], 0)) {
+                have_b = false;
+                atomicExch(err, 1);
+                tc::mbar_wait(&mbar[0], 0);  // another bounded wait for the bulk copy before going on
+            }
+            if (have_b) {
+                const int col = a == 0 ? 0 : (a == 1 ? 6 * nv : 8 * nv);
+                const int width = a == 0 ? 6 * nv : 2 * nv;
+                const uint32_t idesc = tc::idesc_tf32(kRows, width);
+                const uint32_t lbo = 128, sbo = KC * 128;
+                const unsigned char *As[3] = {Ahi, Ahi, Alo}, *Bs[3] = {Bhi, Blo, Bhi};
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+#pragma unroll
+                    for (int kq = 0; kq < K / 8; ++kq)
+                        tc::mma_tf32(tmem + (uint32_t)col, tc::sdesc(tc::smem_u32(As[q]) + kq * 256, lbo, sbo),
+                                     tc::sdesc(tc::smem_u32(Bs[q]) + kq * 256, lbo, sbo), idesc, q > 0 || kq > 0);
+            }
+            tc::mma_commit(&mbar[1]);  // completes phase a
+        }
+    }
+    if (!tc::mbar_wait(&mbar[1], 0u)) {  // phase 2: every product is in TMEM
+        ok = false;
+        atomicExch(err, 2);
+    }
+    ok = __all_sync(0xffffffffu, ok);  // the TMEM loads below are warp-wide
+    tc::fence_after_sync();
+    if (ok) {
+        // columns (p, j2, re/im) of this thread's row; the two warps of a lane
+        // quarter take alternate 16-column chunks
+        const long long zs = (long long)N * nv * nv * Bp;
+        const int ncol = 10 * nv;
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+        for (int c0 = 16 * half; c0 < ncol; c0 += 32) {
+            float v[16];
+            tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int u = 0; u < 16; u += 2) {
+                const int col = c0 + u;
+                if (col < ncol) {
+                    const int pj = col >> 1, p = pj / nv, j2 = pj - p * nv;
+                    Z[p * zs + (((long long)k1 * nv + j2) * nv + j3) * Bp + c] = make_float2(v[u], v[u + 1]);
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (w == 0) tc::tmem_free(tmem, 256u);
+}
+
 }  // namespace
+
+bool pj2_tc_supported(int n, int nv, int Bp) {
+    if (!(n == 8 || n == 16 || n == 24 || n == 32)) return false;
+    if (nv < 8 || nv % 8 || 10 * nv > 256) return false;  // 2 nv and 6 nv multiples of 16
+    if (Bp < 32 || Bp % 32) return false;
+    return ((long long)n * nv * Bp) % kRows == 0;
+}
+
+size_t pj2_tc_smem(int n, int nv) { return (size_t)2 * 6 * nv * 2 * n * 4 + (size_t)2 * kRows * 2 * n * 4; }
 
 int pj1_tc_nvp(int nv) { return ((nv + 15) / 16) * 16; }
 
@@ -521,6 +649,31 @@ cudaError_t launch_pj1_tc(const float2 *Z, const float *btab, int n, int nv, int
     case 16: return pj1_tc_go<16>(Z, btab, nv, Bp, B, dt, kfac, cdt, dv, lv, Inc, part, err, st);
     case 24: return pj1_tc_go<24>(Z, btab, nv, Bp, B, dt, kfac, cdt, dv, lv, Inc, part, err, st);
     default: return pj1_tc_go<32>(Z, btab, nv, Bp, B, dt, kfac, cdt, dv, lv, Inc, part, err, st);
+    }
+}
+
+
+template <int N>
+static cudaError_t pj2_tc_go(const float2 *Y, const float *btab, int nv, int Bp, float2 *Z, int *err,
+                             cudaStream_t st) {
+    const size_t smem = pj2_tc_smem(N, nv);
+    cudaError_t e = cudaFuncSetAttribute(k_pj2_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int tiles = (int)((long long)N * nv * Bp / kRows);
+    k_pj2_tc<N><<<tiles, kThreads, smem, st>>>(Y, btab, nv, Bp, Z, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pj2_tc(const float2 *Y, const float *btab, int n, int nv, int Bp, float2 *Z, int *err,
+                          cudaStream_t st) {
+    if (!pj2_tc_supported(n, nv, Bp) || !btab || !err) return cudaErrorInvalidValue;
+    if (pj3_tc_np(nv) != 6 * nv) return cudaErrorInvalidValue;  // the axis-3 table without padding columns
+    if (reinterpret_cast<uintptr_t>(btab) % 16) return cudaErrorInvalidValue;
+    switch (n) {
+    case 8: return pj2_tc_go<8>(Y, btab, nv, Bp, Z, err, st);
+    case 16: return pj2_tc_go<16>(Y, btab, nv, Bp, Z, err, st);
+    case 24: return pj2_tc_go<24>(Y, btab, nv, Bp, Z, err, st);
+    default: return pj2_tc_go<32>(Y, btab, nv, Bp, Z, err, st);
     }
 }
 
