@@ -406,6 +406,30 @@ def run_workload(args, emit=True):
             t = timed(lambda: b.step(1), args.steps, args.warmup)
         m = [b.moments(i) for i in range(len(specs))]
         extra["finite"] = bool(all(np.all(np.isfinite(x)) for x in m))
+        if prec == lp.PREC_MIXED and args.fp64_steps > 0:
+            # error against FP64 on a sample of the runs (the first 8, every N
+            # of the draw among them): the same runs as a mixed and an FP64
+            # batch, full steps from the same initial states
+            sub = specs[:8]
+            mb = lp.Batch([lp.Params(**r, fixes=lp.FIX_DEFAULT, precision=lp.PREC_MIXED) for r in sub])
+            fb = lp.Batch([lp.Params(**r, fixes=lp.FIX_DEFAULT, precision=lp.PREC_FP64) for r in sub])
+            for i in range(len(sub)):
+                mb.set_init(i, 1)
+                fb.set_init(i, 1)
+            m0 = [mb.moments(i) for i in range(len(sub))]
+            mb.step(args.fp64_steps)
+            fb.step(args.fp64_steps)
+            errs, drift = [], []
+            for i in range(len(sub)):
+                Um, Uf = mb.get_state(i), fb.get_state(i)
+                errs.append(float(np.linalg.norm(Um - Uf) / np.linalg.norm(Uf)))
+                m1 = mb.moments(i)
+                drift.append(float(abs(m1[0] - m0[i][0]) / abs(m0[i][0])))
+            extra["rel_err_vs_fp64"] = {"runs": len(sub), "steps": args.fp64_steps, "max": max(errs),
+                                        "per_run": errs, "n_of_runs": [r["n"] for r in sub]}
+            extra["mass_drift_max"] = max(drift)
+            mb.close()
+            fb.close()
         cfg = {"workload": "64 seeded uneven runs (Nx in {16,32,64,128}, N=Nv in {16,24,32}, "
                            "A, k, nu drawn), one full time step of every run per step",
                "seed": 20261203, "runs": len(specs), "cells_per_step": cells,
