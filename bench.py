@@ -73,8 +73,13 @@ def fq_kernel_model(n, cells):
     x, g, hh = 13 * n * M * M, n * M * M, n * n * M
     # valid (i, l) pairs of the direct axis-1 sum: 0 <= i + h - l < n
     pairs = sum(1 for i in range(n) for l in range(n) if 0 <= i + h - l < n)
+    x1 = 10 * n * n * M  # axis-3 spectra of the 10 source arrays
     model = {
-        # X1 and X2 fused: the X1 outputs stay in shared memory
+        # fused form: axis-3 DFTs into X1; axis-2 DFTs, axis-1 sums and
+        # inverse axis-2 DFTs with the axis-2 spectra in shared memory
+        "k_fq_x1": (n ** 3 * c8 + 7 * n ** 3 * 4 + x1 * c8, None),
+        "k_fq_yz": (x1 * c8 + hh * c8, 7 * pairs * 8.0 * M * M * cells),
+        # three-pass form: X1 and X2 fused, the X1 outputs in shared memory
         "k_fq_x12": (n ** 3 * c8 + 7 * n ** 3 * 4 + x * c8, None),
         "k_fq_y": (x * c8 + g * c8, 7 * pairs * 8.0 * M * M * cells),
         "k_fq_z1": (g * c8 + hh * c8, None),
@@ -83,8 +88,11 @@ def fq_kernel_model(n, cells):
     return model
 
 
-def fq_kernels(n):
-    """(name, lp_time_kernel code) of the convolution form's kernels."""
+def fq_kernels(form):
+    """(name, lp_time_kernel code) of the convolution form's kernels: form 1
+    (axis-2 spectra on chip) or 0 (three passes through DRAM)."""
+    if form == 1:
+        return [("k_fq_x1", 4), ("k_fq_yz", 6), ("k_fq_z2", 8)]
     return [("k_fq_x12", 4), ("k_fq_y", 6), ("k_fq_z1", 7), ("k_fq_z2", 8)]
 
 
@@ -630,7 +638,7 @@ def main():
         t_contract_ms = ctx.time_kernel(0, reps=max(5, args.steps))
         fq_ms = {}
         if schedule[1] == 0:
-            for name, code in fq_kernels(WORKLOAD["n"]):
+            for name, code in fq_kernels(ctx.convolution_form()):
                 flush.zero_()
                 fq_ms[name] = ctx.time_kernel(code, reps=max(5, args.steps))
     n = WORKLOAD["n"]
@@ -654,7 +662,8 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         extra["full_step_ms"] = e0.elapsed_time(e1) / 3
-    extra["schedule"] = {"cells_per_pass": schedule[0], "line_warps": schedule[1]}
+    extra["schedule"] = {"cells_per_pass": schedule[0], "line_warps": schedule[1],
+                         "convolution_form": ctx.convolution_form()}
     if rank == 0:
         t_fp64 = None
         if args.precision == "mixed" and args.fp64_steps > 0:

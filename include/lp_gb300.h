@@ -195,16 +195,29 @@ lp_status lp_autotune(lp_ctx *ctx, int reps, const char *cache_path, int *pass_c
  * the forms above.  LP_ERR_INVALID for a schedule the context cannot run. */
 lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
 
+/* The kernels of the convolution form (mixed path, line_warps 0): form 1
+ * (default) keeps the axis-2 spectra on chip -- the axis-3 DFTs go to
+ * device memory, then one kernel per (k3, group of cells) runs the axis-2
+ * DFTs, the direct sums along axis 1 and the inverse axis-2 DFTs, its
+ * operands brought in by bulk copies -- form 0 runs the axis-3/axis-2 DFTs,
+ * the axis-1 sums and the inverse axis-2 DFTs as three kernels through
+ * device memory.  Both forms give the same FP32 results.  The environment
+ * variable LP_FQ_FUSED=0 makes form 0 the default of new contexts. */
+lp_status lp_set_convolution_form(lp_ctx *ctx, int form);
+lp_status lp_get_convolution_form(const lp_ctx *ctx, int *form);
+
 /* ---- measurement helpers (no reference counterpart) --------------------- */
 /* Average device time in ms of one launch of a hot-path stage on the
  * context's stream, over `reps` launches after one warm-up, timed with CUDA
  * events: which = 0 the weighted contraction of ComputeQ for every collided
  * cell, 1 the forward transform, 2 the moment-conserving projection, 3 the
  * DG projection of the RK4 combination; 4, 6, 7, 8 the kernels of the
- * convolution form (axis-3 and axis-2 DFTs in one kernel, axis-1 sums,
- * inverse axis-2 and axis-3 DFTs; 5 launches nothing) for the first
- * convolution chunk of cells, each alone, when that form is the schedule.
- * Needs the resident state. */
+ * convolution form for the first convolution chunk of cells, each alone,
+ * when that form is the schedule: form 1 -- 4 the axis-3 DFTs, 6 the fused
+ * axis-2 DFTs / axis-1 sums / inverse axis-2 DFTs, 8 the inverse axis-3
+ * DFTs (5 and 7 launch nothing); form 0 -- 4 the axis-3 and axis-2 DFTs in
+ * one kernel, 6 the axis-1 sums, 7 the inverse axis-2 DFTs, 8 the inverse
+ * axis-3 DFTs (5 launches nothing).  Needs the resident state. */
 lp_status lp_time_kernel(lp_ctx *ctx, int which, int reps, double *ms);
 /* Dense FMA throughput of the current device measured with dependent-chain
  * microbenchmarks: FP32 (packed f32x2) and FP64, in TFLOP/s. */

@@ -57,7 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     cu_flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                        "-I", INCLUDE, "-I", CSRC]
-    for name in ("lp_kernels.cu", "lp_api.cu", "lp_noalloc.cu", "lp_adjoint.cu", "lp_fftq.cu", "lp_pjtc.cu", "lp_corr.cu"):
+    for name in ("lp_kernels.cu", "lp_api.cu", "lp_noalloc.cu", "lp_adjoint.cu", "lp_fftq.cu", "lp_fqf.cu",
+                 "lp_pjtc.cu", "lp_corr.cu"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OUT, name.replace(".cu", ".o"))
         objs.append(obj)

@@ -46,6 +46,7 @@ struct lp_ctx {
     float *FQC = nullptr;
     float2 *fscr = nullptr;
     int fq_bs = 0;
+    int fq_form = 1;  // 1: fused (axis-2 spectra on chip), 0: three passes through DRAM
     lp::FftTw ftw{};
     // two-species variant: linear weight table (R precision), window offsets,
     // the linear term's workspace and CCt_linear embedded in a 5x5 matrix
@@ -276,6 +277,8 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
             lp::pj1_tc_table(tf.data(), T.n, T.nv, tab);
             LP_TRY(upload(c, &c->pj1_tab, tab.data(), tab.size()));
         }
+    }
+    if (c->mixed) {  // error flag of the bounded waits (tensor-core projection, fused convolution)
         LP_TRY(dalloc(c, &c->tc_err, 1));
         LP_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
     }
@@ -313,6 +316,10 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
             c->fq_bs = std::min(c->Bcap, std::max(64, fit));
             LP_TRY(dalloc(c, &c->fscr, lp::fftq_scratch_elems(T.n, c->fq_bs)));
             c->ftw = lp::fftq_twiddles(T.n);
+            // the fused convolution (LP_FQ_FUSED=0 in the environment keeps
+            // the three passes through DRAM, for comparisons)
+            const char *fenv = std::getenv("LP_FQ_FUSED");
+            c->fq_form = (fenv && fenv[0] == '0') ? 0 : 1;
             // the convolution form is the faster one from n = 16 up
             if (T.n >= 16) c->line_warps = 0;
         }
@@ -499,7 +506,7 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *
         for (int c0 = 0; c0 < Bp; c0 += c->fq_bs)
             LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, c0,
                                             std::min(c->fq_bs, Bp - c0), c->fscr, c->fq_bs, q, c->stream, -1,
-                                            q32, lam ? &cons : nullptr));
+                                            q32, lam ? &cons : nullptr, c->fq_form, c->tc_err));
         if (lam) LP_CUDA(lp::launch_cons_lambda(c->cpart, lp::fftq_cons_blocks(T.n), c->cct, Bp, lam, c->stream));
         return LP_OK;
     }
@@ -1214,11 +1221,11 @@ lp_status lp_synchronize(lp_ctx *c) {
     LP_CUDA(cudaStreamSynchronize(c->stream));
     if (c->h2d) LP_CUDA(cudaStreamSynchronize(c->h2d));
     if (c->d2h) LP_CUDA(cudaStreamSynchronize(c->d2h));
-    if (c->tc_err) {  // a bounded wait of the tensor-core projection that ran out
+    if (c->tc_err) {  // a bounded wait of the tensor-core projection or the fused convolution that ran out
         int e = 0;
         LP_CUDA(cudaMemcpy(&e, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (e) return fail(c, LP_ERR_CUDA, "tensor-core projection: a bounded wait ran out (code " +
-                                               std::to_string(e) + ")");
+        if (e) return fail(c, LP_ERR_CUDA, std::string(e >= 3 ? "fused convolution" : "tensor-core projection") +
+                                               ": a bounded wait ran out (code " + std::to_string(e) + ")");
     }
     return LP_OK;
 }
@@ -1551,7 +1558,8 @@ lp_status lp_time_kernel(lp_ctx *c, int which, int reps, double *ms) {
         case 3: return c->mixed ? project<float>(c, 0, B, Bp) : project<double>(c, 0, B, Bp);
         default:
             LP_CUDA(lp::launch_computeq_fft((const float2 *)c->F, c->FQC, c->ftw, T.n, Bp, 0, std::min(c->fq_bs, Bp),
-                                            c->fscr, c->fq_bs, c->q[1], c->stream, which - 4));
+                                            c->fscr, c->fq_bs, c->q[1], c->stream, which - 4, nullptr, nullptr,
+                                            c->fq_form, c->tc_err));
             return LP_OK;
         }
     };
@@ -2288,6 +2296,23 @@ lp_status lp_autotune(lp_ctx *c, int reps, const char *cache_path, int *pass_cel
     if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
     if (pass_cells) *pass_cells = c->Bpass;
     if (line_warps) *line_warps = c->line_warps;
+    return LP_OK;
+}
+
+lp_status lp_set_convolution_form(lp_ctx *c, int form) {
+    if (!c) return LP_ERR_INVALID;
+    if (form != 0 && form != 1) return fail(c, LP_ERR_INVALID, "convolution form must be 0 or 1");
+    if (!c->FQC) return fail(c, LP_ERR_INVALID, "no convolution form in this context");
+    LP_CUDA(cudaStreamSynchronize(c->stream));
+    c->fq_form = form;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }  // recapture with the new kernels
+    if (c->cgexec) { cudaGraphExecDestroy(c->cgexec); c->cgexec = nullptr; }
+    return LP_OK;
+}
+
+lp_status lp_get_convolution_form(const lp_ctx *c, int *form) {
+    if (!c || !form) return LP_ERR_INVALID;
+    *form = c->FQC ? c->fq_form : -1;
     return LP_OK;
 }
 

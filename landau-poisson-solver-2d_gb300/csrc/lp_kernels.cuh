@@ -134,10 +134,15 @@ void fftq_coefficients(const double *shat, const double *ahat, const double *cw,
 size_t fftq_gh_elems(int n, int Bs);       // axis-1 sums and inverse axis-2 outputs
 size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
 // Cells [c0, c0 + Bc) of F and q (stride Bp); Bc and c0 multiples of 32,
-// Bc <= Bs, the cells of the scratch.  stage -1 runs the four kernels; 0, 2,
-// 3, 4 only one of them (the fused X1/X2, Y, Z1, Z2; 1 launches nothing), on
-// the scratch a full run left.  q32: the mode array is written as FP32
-// complex there instead of q.
+// Bc <= Bs, the cells of the scratch.  form 1 (fused, lp_fqf.cu): the axis-3
+// DFTs into X1, then the axis-2 DFTs, axis-1 sums and inverse axis-2 DFTs
+// in one kernel that keeps the axis-2 spectra on chip, then Z2; form 0
+// (three-pass): X1/X2, Y and Z1 as separate kernels through DRAM, then Z2.
+// stage -1 runs every kernel; 0, 2, 3, 4 only one of them (form 1: X1, the
+// fused kernel, nothing, Z2; form 0: X1/X2, Y, Z1, Z2; 1 launches nothing),
+// on the scratch a full run left.  q32: the mode array is written as FP32
+// complex there instead of q.  err: set by the fused kernel when one of its
+// bounded waits runs out.
 // conserveAllMoments' sums formed by the convolution form's last kernel as it
 // writes an FP32 mode array: each thread sums its outputs times the
 // constraint rows (cf, FP32 [5][n^3]) in FP32, each block adds its threads'
@@ -152,7 +157,13 @@ int fftq_cons_blocks(int n);
 
 cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw, int n, int Bp, int c0, int Bc,
                                 float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1,
-                                float2 *q32 = nullptr, const ConsFused *cons = nullptr);
+                                float2 *q32 = nullptr, const ConsFused *cons = nullptr, int form = 0,
+                                int *err = nullptr);
+// The fused form's stages 0 and 2 (lp_fqf.cu) on X1 and H of the scratch,
+// and the X1 elements it needs for Bs cells.
+cudaError_t launch_fq_fused(int n, const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc,
+                            float2 *X1, float2 *H, int Bs, cudaStream_t st, int stage, int *err);
+size_t fq_fused_x1_elems(int n, int Bs);
 
 // Moment-conserving projection of q in place (FP64).
 // apply = false: only the multipliers lam[5][Bp] (the correction is left to

@@ -70,6 +70,17 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
+// one arrival of this thread (release: its earlier shared-memory accesses
+// are ordered before the phase completes)
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// named barrier `id` (1..15) over `count` threads (a multiple of 32)
+__device__ __forceinline__ void named_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 // Wait for the completion of phase `parity`, bounded in time: the
 // non-blocking test_wait is polled until the phase completes or `limit_ns`
 // of the global timer have passed (false: the wait ran out).
@@ -86,6 +97,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint6
         if (done) return true;
         if (global_ns() - t0 > limit_ns) return false;
         __nanosleep(32);
+    }
+}
+
+// The same wait with mbarrier.try_wait: the thread is suspended until the
+// phase completes or `hint_ns` pass (then it asks again), so a waiting warp
+// neither spins on the issue slots nor oversleeps the completion.
+__device__ __forceinline__ bool mbar_wait_susp(uint64_t *mbar, uint32_t parity,
+                                               uint64_t limit_ns = 2000000000ull, uint32_t hint_ns = 1000000u) {
+    uint64_t t0 = 0;
+    for (int it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(smem_u32(mbar)), "r"(parity), "r"(hint_ns)
+            : "memory");
+        if (done) return true;
+        if (it == 0) t0 = global_ns();
+        else if (global_ns() - t0 > limit_ns) return false;
     }
 }
 

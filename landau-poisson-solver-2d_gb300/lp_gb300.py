@@ -44,7 +44,8 @@ EXPORTS = [
     "lp_diagnostics", "lp_diagnostics_append", "lp_marginal_x1v1", "lp_state_append", "lp_state_restart",
     "lp_autotune", "lp_set_schedule", "lp_compute_q_lin", "lp_conserve_lin", "lp_rk4_cell_lin",
     "lp_slab_create", "lp_stage_device_ptr", "lp_slab_charge", "lp_slab_fields", "lp_slab_advect_stage",
-    "lp_slab_fields_host", "lp_collision_step_host", "lp_set_adjoint_form",
+    "lp_slab_fields_host", "lp_collision_step_host", "lp_set_adjoint_form", "lp_set_convolution_form",
+    "lp_get_convolution_form",
 ]
 NOALLOC_MAX_CELLS = 4096
 
@@ -173,6 +174,8 @@ def lib():
         L.lp_slab_fields_host.argtypes = [_vp, _dp, _dp, _dp]
         L.lp_collision_step_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
         L.lp_set_adjoint_form.argtypes = [_vp, ctypes.c_int]
+        L.lp_set_convolution_form.argtypes = [_vp, ctypes.c_int]
+        L.lp_get_convolution_form.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
         for name in EXPORTS:
             f = getattr(L, name)
             if name not in ("lp_last_error", "lp_device_bytes", "lp_batch_last_error",
@@ -415,6 +418,16 @@ class Context:
 
     def state_restart(self, path):
         self._chk(self.L.lp_state_restart(self.h, path.encode()))
+
+    def set_convolution_form(self, form):
+        """Kernels of the convolution form: 1 axis-2 spectra on chip (default), 0 three passes."""
+        self._chk(self.L.lp_set_convolution_form(self.h, int(form)))
+
+    def convolution_form(self):
+        """1 or 0 (set_convolution_form), -1 when the context has no convolution form."""
+        f = ctypes.c_int()
+        self._chk(self.L.lp_get_convolution_form(self.h, ctypes.byref(f)))
+        return f.value
 
     def set_adjoint_form(self, form):
         """ComputeQ's VJP in the adjoint: 0 correlations (default), 1 pair-table gather."""
