@@ -9,15 +9,23 @@ FS, SetInit_LD, setInit_spectral, ComputeQ, conserveAllMoments, IntModes,
 RK4 (zero state, so the stride defect F1 does not enter), pois2d, the band
 factors, one RK3 step, the verbatim collision driver and the moments.
 
+The fixture ref_nv24 runs the reference at the strong-damping workload's
+velocity grid (Nv = N = 24, Lv = 6) on a 2 x 2 spatial grid: ComputeQ,
+conserveAllMoments, RK4 from the zero state and the verbatim collision driver
+of its two collided cells, from the SetInit_LD state (stored as a SHA-256 of
+its bytes: the oracle's and the library's initial states are compared bit for
+bit with the other fixtures' U_init, and the hash pins this one too).
+
 The two-species fixture (ref_lin_n8) comes from the reference compiled with
 its FullandLinear switch: the linear weight rows, CCt_linear, ComputeQ with
 its linear part, the two conservations and RK4 (state with equal stride-6 and
 stride-7 slots, so the slot defect F1 reads the same values either way).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]   # default: all
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import subprocess
 import sys
@@ -87,6 +95,15 @@ def make(name, case, rng):
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
 
 
+def make_rng_skip(case, rng):
+    """The draws make() takes from the seeded stream, without the reference."""
+    n, nv, n3 = case.n, case.nv, case.n ** 3
+    rng.choice(n3, 6, replace=False)
+    rng.standard_normal(n3), rng.standard_normal(n3)
+    rng.integers(0, [n, n, n, nv, nv, nv], size=(8, 6))
+    rng.standard_normal(case.size * 7)
+
+
 LIN_CASE = ("ref_lin_n8", Case(nx1=2, nx2=2, nv=4, n=8, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01,
                                 a_amp=0.2, k_wave=0.5, linear_ei=1))
 
@@ -121,13 +138,45 @@ def make_lin(name, case, rng):
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
 
 
-def main():
+NV24_CASE = ("ref_nv24", Case(nx1=2, nx2=2, nv=24, n=24, lv=6.0, lx=4 * np.pi, nu=0.05, dt=0.005,
+                              a_amp=0.5, k_wave=0.5))
+
+
+def make_nv24(name, case):
+    """About two minutes of the reference's CPU time (RK4's IntModes calls
+    and two collided cells dominate)."""
+    R = Reference(case, with_weights=True)
+    out = {"case": np.array([case.nx1, case.nx2, case.nv, case.n], np.int64),
+           "case_f": np.array([case.lv, case.lx, case.nu, case.dt, case.a_amp, case.k_wave])}
+    U = R.set_init_ld()
+    out.update(U_init_sha256=np.frombuffer(hashlib.sha256(U.tobytes()).digest(), np.uint8))
+    U2 = U.copy().reshape(-1, 7)
+    U2[:, 2] = U2[:, 3]  # node sampling without defect F2, as in the other fixtures
+    f = R.set_init_spectral(U2.ravel())[1].copy()
+    q = R.compute_q(f)
+    qc = R.conserve(q)
+    out.update(f_cell=f, qhat=q, qhat_cons=qc)
+    out.update(rk4_cell=np.int64(1), rk4_du=R.rk4(f, 1, qc, np.zeros_like(U)))
+    out.update(coll_du=R.collision_cells(U, 0, case.nx1))
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main(names=None):
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    want = lambda nm: not names or nm in names  # noqa: E731
     rng = np.random.default_rng(SEED)
     for name, case in CASES:
-        make(name, case, rng)
-    make_lin(*LIN_CASE, np.random.default_rng(SEED + 1))
+        if want(name):
+            make(name, case, rng)
+        else:  # keep the seeded stream of the later fixtures
+            make_rng_skip(case, rng)
+    if want(LIN_CASE[0]):
+        make_lin(*LIN_CASE, np.random.default_rng(SEED + 1))
+    if want(NV24_CASE[0]):
+        make_nv24(*NV24_CASE)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -97,3 +97,39 @@ def test_moments(gctx):
     ctx.set_state(g["rk3_out"])
     m = ctx.moments()
     assert np.allclose(m[:5], g["moments"][:5], rtol=1e-13, atol=1e-14 * abs(g["moments"][0]))
+
+
+# At the strong-damping workload's velocity grid (Nv = N = 24, v in [-6, 6]^3;
+# fixture ref_nv24): ComputeQ, the projection, RK4 from the zero state and
+# the verbatim collision driver of the two collided cells of a 2 x 2 grid.
+@pytest.fixture(scope="module")
+def gctx24(gpu_lib):
+    g = load_golden("ref_nv24")
+    c = golden_case(g)
+    P = gpu_lib.Params(nx1=c.nx1, nx2=c.nx2, nv=c.nv, n=c.n, lv=c.lv, lx=c.lx, nu=c.nu, dt=c.dt,
+                       a_amp=c.a_amp, k_wave=c.k_wave, fixes=0, precision=gpu_lib.PREC_FP64)
+    ctx = gpu_lib.Context(P)
+    yield g, c, ctx
+    ctx.close()
+
+
+def test_compute_q_conserve_nv24(gctx24):
+    g, _, ctx = gctx24
+    assert rel(ctx.compute_q(g["f_cell"]), g["qhat"]) < TOL
+    assert rel(ctx.conserve(g["qhat"]), g["qhat_cons"]) < TOL
+
+
+def test_rk4_zero_state_nv24(gctx24):
+    g, c, ctx = gctx24
+    ctx.set_state(np.zeros(c.size * 7))
+    du = ctx.rk4_cell(g["f_cell"], int(g["rk4_cell"]), g["qhat_cons"])
+    assert rel(du, g["rk4_du"]) < TOL
+
+
+def test_collision_verbatim_nv24(gctx24):
+    from oracle.oracle import Oracle
+    g, c, ctx = gctx24
+    ctx.set_state(Oracle(c, fixes=0).set_init(0))  # SetInit_LD, pinned by the fixture's hash
+    ctx.collision_step()
+    U = ctx.get_state().reshape(-1, 7)[: c.nx1 * c.nv ** 3]
+    assert rel(U[:, [0, 3, 4, 5, 6]].ravel(), g["coll_du"]) < TOL
