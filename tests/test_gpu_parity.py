@@ -102,6 +102,14 @@ def test_moments(gctx):
 # At the strong-damping workload's velocity grid (Nv = N = 24, v in [-6, 6]^3;
 # fixture ref_nv24): ComputeQ, the projection, RK4 from the zero state and
 # the verbatim collision driver of the two collided cells of a 2 x 2 grid.
+# Defect F11 is present at this grid (eta[n/2] != 0) and the verbatim step
+# blows the state up by ~1e10, which amplifies rounding ~2e3-fold (a 1e-16
+# relative change of the node values moves RK4's output by ~2e-13,
+# tests/test_oracle_golden_nv24.py); the GPU sums in its own order, so RK4 and
+# the collision driver are held to TOL_F11.  ComputeQ and the projection
+# precede the growth and keep TOL.  The F11-fixed step at this grid is
+# compared with the oracle at 1e-12 in tests/test_gpu_configs.py.
+TOL_F11 = 1e-10
 @pytest.fixture(scope="module")
 def gctx24(gpu_lib):
     g = load_golden("ref_nv24")
@@ -123,7 +131,7 @@ def test_rk4_zero_state_nv24(gctx24):
     g, c, ctx = gctx24
     ctx.set_state(np.zeros(c.size * 7))
     du = ctx.rk4_cell(g["f_cell"], int(g["rk4_cell"]), g["qhat_cons"])
-    assert rel(du, g["rk4_du"]) < TOL
+    assert rel(du, g["rk4_du"]) < TOL_F11
 
 
 def test_collision_verbatim_nv24(gctx24):
@@ -132,4 +140,4 @@ def test_collision_verbatim_nv24(gctx24):
     ctx.set_state(Oracle(c, fixes=0).set_init(0))  # SetInit_LD, pinned by the fixture's hash
     ctx.collision_step()
     U = ctx.get_state().reshape(-1, 7)[: c.nx1 * c.nv ** 3]
-    assert rel(U[:, [0, 3, 4, 5, 6]].ravel(), g["coll_du"]) < TOL
+    assert rel(U[:, [0, 3, 4, 5, 6]].ravel(), g["coll_du"]) < TOL_F11

@@ -6,7 +6,11 @@ the verbatim collision driver of the two collided cells at 1e-13 with the
 reference's per-(mode, v-cell) projection and 1e-12 with the separable one
 (the reference reduces in OpenMP order).  At this grid eta[n/2] is not exactly 0
 (defect F11), which the fixture keeps: the reference's collision step blows
-the state up, and the oracle reproduces that too."""
+the state up (from |f| ~ 0.07 to |dU| ~ 1e9), and the oracle reproduces that
+too.  That growth makes the step ill-conditioned: a relative perturbation of
+1e-16 in the node values moves RK4's output by ~2e-13 (checked below), so an
+implementation that only sums in another order lands ~1e3 times its own
+rounding away from the reference there."""
 from __future__ import annotations
 
 import hashlib
@@ -54,3 +58,15 @@ def test_collision_driver_verbatim_nv24(gold):
         U = O.collide(O.set_init(0), direct=direct)
         du = U.reshape(-1, 7)[: nx1 * nv3][:, [0, 3, 4, 5, 6]].ravel()
         assert rel(du, g["coll_du"]) < tol
+
+
+def test_rk4_nv24_amplifies_rounding(gold):
+    """The sensitivity that sets the GPU tolerance of the F11-amplified
+    outputs of this fixture: perturbing the node values by a relative 1e-16
+    moves RK4's output by more than 1e-14 and less than 1e-11."""
+    g, O = gold
+    ucell = np.zeros(O.nv3 * 7)
+    base = O.rk4(g["f_cell"], g["qhat_cons"], ucell, direct=True)
+    f = g["f_cell"] * (1 + 1e-16 * np.random.default_rng(1).standard_normal(g["f_cell"].shape))
+    moved = rel(O.rk4(f, g["qhat_cons"], ucell, direct=True), base)
+    assert 1e-14 < moved < 1e-11
