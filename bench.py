@@ -452,6 +452,10 @@ def run_workload(args, emit=True):
         ctx.set_stream(stream.cuda_stream)
         ctx.set_init(2, 2.0)
         cells = TWOSTREAM["nx1"]
+        # the library's autotuner picks the collision schedule (outside the timed region)
+        sched = ctx.autotune(reps=1)
+        extra["schedule"] = {"cells_per_pass": sched[0], "line_warps": sched[1],
+                             "convolution_form": ctx.convolution_form()}
         with ClockSampler(0) as clk:
             t = timed(lambda: ctx.step(1), args.steps, args.warmup)
         with torch.cuda.stream(stream):

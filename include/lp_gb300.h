@@ -183,11 +183,13 @@ lp_status lp_moments(lp_ctx *ctx, double *out6);
 /* Times one collision step of the resident state (best of `reps` after a
  * warm-up, CUDA events, the state restored before each run) for every
  * candidate schedule -- cells per pass 64, 128, ... up to the workspace's
- * capacity, times the contraction forms above -- and keeps the fastest;
- * with cache_path, a schedule recorded there for the same key (n, nv, lv,
- * cells, precision, device) is reused and new ones appended.  The chosen
- * schedule is returned in pass_cells and line_warps (optional).  Leaves the
- * state as it was. */
+ * capacity, times the contraction forms above, the convolution form in both
+ * kernel forms of lp_set_convolution_form -- and keeps the fastest; with
+ * cache_path, a schedule recorded there for the same key (n, nv, lv, cells,
+ * precision, device) is reused and new ones appended.  The chosen schedule
+ * is returned in pass_cells and line_warps (optional); the kernel form it
+ * picked is the context's convolution form afterwards
+ * (lp_get_convolution_form).  Leaves the state as it was. */
 lp_status lp_autotune(lp_ctx *ctx, int reps, const char *cache_path, int *pass_cells, int *line_warps);
 
 /* Sets the schedule directly: pass_cells a multiple of 32 up to the
@@ -202,7 +204,9 @@ lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
  * operands brought in by bulk copies -- form 0 runs the axis-3/axis-2 DFTs,
  * the axis-1 sums and the inverse axis-2 DFTs as three kernels through
  * device memory.  Both forms give the same FP32 results.  The environment
- * variable LP_FQ_FUSED=0 makes form 0 the default of new contexts. */
+ * variable LP_FQ_FUSED=0 makes form 0 the default of new contexts; the
+ * autotuners time both and keep the faster (form 1 at n <= 24, form 0 at
+ * n = 32 on GB300). */
 lp_status lp_set_convolution_form(lp_ctx *ctx, int form);
 lp_status lp_get_convolution_form(const lp_ctx *ctx, int *form);
 
@@ -316,8 +320,9 @@ lp_status lp_batch_class_info(const lp_batch *b, int cls, int *info6, double *tu
 /* Autotuner: for every class, time one collision step (best of `reps` after
  * a warm-up, CUDA events, the class state restored before each run) for
  * every candidate schedule -- cells per pass 64, 128, ... up to the
- * workspace's capacity, and 2 or 4 warps per block of the line-tiled
- * contraction -- and keep the fastest.  With cache_path, schedules already
+ * workspace's capacity; 2 or 4 warps per block of the line-tiled
+ * contraction, or the convolution form in either kernel form -- and keep
+ * the fastest.  With cache_path, schedules already
  * recorded there for the same key (n, nv, lv, cells, precision, device) are
  * reused and new ones appended.  Needs every run's state; leaves it as it
  * was. */

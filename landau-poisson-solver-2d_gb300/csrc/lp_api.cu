@@ -1786,16 +1786,20 @@ void write_tune_cache(const char *path, const std::vector<std::string> &lines) {
 }
 
 // Applies a cached schedule for `key` to e; returns whether one was found.
+// A line is "key cells_per_pass line_warps ms [convolution_form]"; lines
+// without the form leave the context's form as it is.
 bool tune_lookup(const std::vector<std::string> &lines, const std::string &key, lp_ctx *e, double *ms) {
     bool found = false;
     for (const auto &l : lines) {
         char kbuf[512];
-        int bp = 0, lw = 0;
+        int bp = 0, lw = 0, form = -1;
         double t = 0.;
-        if (sscanf(l.c_str(), "%511s %d %d %lf", kbuf, &bp, &lw, &t) == 4 && key == kbuf && bp >= 32 &&
+        const int nf = sscanf(l.c_str(), "%511s %d %d %lf %d", kbuf, &bp, &lw, &t, &form);
+        if (nf >= 4 && key == kbuf && bp >= 32 &&
             bp <= e->Bcap && bp % 32 == 0 && (lw == 2 || lw == 4 || (lw == 0 && e->FQC) || !e->LW)) {
             e->Bpass = bp;
             e->line_warps = e->LW ? lw : 2;
+            if (nf == 5 && e->FQC && (form == 0 || form == 1)) e->fq_form = form;
             *ms = t;
             found = true;
         }
@@ -1834,32 +1838,43 @@ lp_status time_engine(lp_ctx *e, int ncell, cudaStream_t st, const double *backu
 }
 
 // Picks the fastest schedule of engine e for cells [0, ncell): cells per pass
-// 64, 128, ... up to the workspace capacity, and 2 or 4 warps per line block
-// of the line-tiled contraction.  e->U1 holds the state meanwhile.
+// 64, 128, ... up to the workspace capacity; 2 or 4 warps per line block of
+// the line-tiled contraction, or the convolution form in either kernel form
+// (axis-2 spectra on chip, or three passes through device memory: the
+// first is faster at n <= 24, the second at n = 32).  e->U1 holds the state
+// meanwhile.
 lp_status tune_engine(lp_ctx *e, int ncell, cudaStream_t st, int reps, double *best_ms) {
     lp_ctx *c = e;
     const size_t bytes = sizeof(double) * (size_t)e->T.size * 7;
     std::vector<int> passes;
     for (int bp = 64; bp < e->Bcap; bp *= 2) passes.push_back(bp);
     passes.push_back(e->Bcap);
-    std::vector<int> warps = {2};
-    if (e->LW) warps.push_back(4);
-    if (e->FQC) warps.push_back(0);
+    struct Cand {
+        int lw, form;
+    };
+    std::vector<Cand> cands = {{2, e->fq_form}};
+    if (e->LW) cands.push_back({4, e->fq_form});
+    if (e->FQC) {
+        cands.push_back({0, 1});
+        cands.push_back({0, 0});
+    }
     LP_CUDA(cudaMemcpyAsync(e->U1, e->U, bytes, cudaMemcpyDeviceToDevice, st));
     double best = 1e300;
-    int bbp = e->Bcap, blw = 2;
+    int bbp = e->Bcap, blw = 2, bform = e->fq_form;
     for (int bp : passes)
-        for (int lw : warps) {
+        for (const Cand &cd : cands) {
             e->Bpass = bp;
-            e->line_warps = lw;
+            e->line_warps = cd.lw;
+            e->fq_form = cd.form;
             double ms = 0.;
             LP_TRY(time_engine(e, ncell, st, e->U1, reps, &ms));
-            if (ms < best) { best = ms; bbp = bp; blw = lw; }
+            if (ms < best) { best = ms; bbp = bp; blw = cd.lw; bform = cd.form; }
         }
     LP_CUDA(cudaMemcpyAsync(e->U, e->U1, bytes, cudaMemcpyDeviceToDevice, st));
     LP_CUDA(cudaStreamSynchronize(st));
     e->Bpass = bbp;
     e->line_warps = blw;
+    e->fq_form = bform;
     *best_ms = best;
     return LP_OK;
 }
@@ -2268,7 +2283,8 @@ lp_status lp_batch_autotune(lp_batch *b, int reps, const char *cache_path) {
         const lp_status s = tune_engine(K.eng, K.ncell, b->stream, reps, &K.tuned_ms);
         if (s != LP_OK) return bfail(b, s, "autotune: " + K.eng->err);
         char line[768];
-        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), K.eng->Bpass, K.eng->line_warps, K.tuned_ms);
+        snprintf(line, sizeof(line), "%s %d %d %.6f %d\n", key.c_str(), K.eng->Bpass, K.eng->line_warps, K.tuned_ms,
+                 K.eng->fq_form);
         lines.emplace_back(line);
         changed = true;
     }
@@ -2288,7 +2304,7 @@ lp_status lp_autotune(lp_ctx *c, int reps, const char *cache_path, int *pass_cel
     if (!tune_lookup(lines, key, c, &ms) && c->T.ncollide > 0) {
         LP_TRY(tune_engine(c, c->T.ncollide, c->stream, reps, &ms));
         char line[768];
-        snprintf(line, sizeof(line), "%s %d %d %.6f\n", key.c_str(), c->Bpass, c->line_warps, ms);
+        snprintf(line, sizeof(line), "%s %d %d %.6f %d\n", key.c_str(), c->Bpass, c->line_warps, ms, c->fq_form);
         lines.emplace_back(line);
         write_tune_cache(cache_path, lines);
     }

@@ -1004,32 +1004,30 @@ __global__ void k_cons_partial(const QT *__restrict__ q, const double *__restric
     }
 }
 
-// One block per cell: the threads sum the chunk partials in a fixed order
-// and a fixed tree, thread 0 solves (C C^T)^-1 t (solveWithCCt, K:49-55).
-__global__ void __launch_bounds__(256) k_cons_lambda(const double *__restrict__ part, int nchunk,
+// One block of five warps per cell: warp j sums the chunk partials of
+// constraint j (each lane a fixed strided subset, then a fixed butterfly of
+// shuffles), and threads 0..4 form lambda_i = sum_j (C C^T)^-1[j + 5 i] t_j
+// (solveWithCCt, K:49-55).  The FP64 dependency chains stay short: GB300's
+// FP64 unit is narrow, and a block-wide tree with one thread solving the 5x5
+// system spent most of its time waiting on FP64 results.
+__global__ void __launch_bounds__(160) k_cons_lambda(const double *__restrict__ part, int nchunk,
                                                      const double *__restrict__ cct, int Bp,
                                                      double *__restrict__ lam) {
-    __shared__ double red[5][256];
-    const int c = blockIdx.x, t = threadIdx.x;
-    double v[5] = {0, 0, 0, 0, 0};
-    for (int k = t; k < nchunk; k += 256)
+    __shared__ double t5[5];
+    const int c = blockIdx.x, lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+    double v = 0.;
+    for (int k = lane; k < nchunk; k += 32) v += part[((long long)k * 5 + j) * Bp + c];
 #pragma unroll
-        for (int j = 0; j < 5; ++j) v[j] += part[((long long)k * 5 + j) * Bp + c];
-#pragma unroll
-    for (int j = 0; j < 5; ++j) red[j][t] = v[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) t5[j] = v;
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w)
+    if (threadIdx.x < 5) {
+        const int i = threadIdx.x;
+        double s = 0.;
 #pragma unroll
-            for (int j = 0; j < 5; ++j) red[j][t] += red[j][t + w];
-        __syncthreads();
+        for (int q = 0; q < 5; ++q) s += cct[q + i * 5] * t5[q];
+        lam[(long long)i * Bp + c] = s;
     }
-    if (t == 0)
-        for (int i = 0; i < 5; ++i) {
-            double s = 0.;
-            for (int j = 0; j < 5; ++j) s += cct[j + i * 5] * red[j][0];
-            lam[(long long)i * Bp + c] = s;
-        }
 }
 
 __global__ void k_cons_apply(double2 *__restrict__ q, const double *__restrict__ c1,
@@ -2888,14 +2886,14 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
 cudaError_t launch_conserve(double2 *q, const double *c1, const double *c2, const double *cct_inv, int n3, int Bp,
                             double *part, int nchunk, double *lam, cudaStream_t st, bool apply) {
     k_cons_partial<double2><<<dim3(nchunk, Bp / 32), dim3(32, 8), 0, st>>>(q, c1, c2, n3, Bp, nchunk, part);
-    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    k_cons_lambda<<<Bp, 160, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     if (apply) k_cons_apply<<<grid1((long long)n3 * Bp, 256), 256, 0, st>>>(q, c1, c2, lam, n3, Bp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_cons_lambda(const double *part, int nchunk, const double *cct_inv, int Bp, double *lam,
                                cudaStream_t st) {
-    k_cons_lambda<<<Bp, 256, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
+    k_cons_lambda<<<Bp, 160, 0, st>>>(part, nchunk, cct_inv, Bp, lam);
     return cudaGetLastError();
 }
 

@@ -116,7 +116,21 @@ def test_context_autotune(gpu_lib, tmp_path):
     bp, lw = a.autotune(reps=2, cache_path=cache)
     assert bp % 32 == 0 and lw in (0, 2, 4)
     assert np.array_equal(a.get_state(), U0)
+    # the cache line records the kernel form of the convolution form too
+    fields = open(cache).read().split()
+    assert len(fields) == 5 and int(fields[4]) == a.convolution_form() in (0, 1)
+    b.set_convolution_form(1 - a.convolution_form())
     assert b.autotune(reps=2, cache_path=cache) == (bp, lw)  # from the cache
+    assert b.convolution_form() == a.convolution_form()
+    # a line without the form (an older cache) sets the schedule and keeps the form
+    old_cache = str(tmp_path / "old.txt")
+    with open(old_cache, "w") as f:
+        f.write(" ".join(fields[:4]) + "\n")
+    d = lp.Context(P)
+    d.set_init(1)
+    d.set_convolution_form(0)
+    assert d.autotune(reps=2, cache_path=old_cache) == (bp, lw)
+    assert d.convolution_form() == 0
     a.step(2)
     c = lp.Context(P)
     c.set_init(1)
