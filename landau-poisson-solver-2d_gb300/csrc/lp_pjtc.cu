@@ -170,17 +170,24 @@ __global__ void __launch_bounds__(kThreads) k_pj3_tc(const QT *__restrict__ q0, 
     if (done) {
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows), the two warps
         // of a lane quarter alternate 16-column chunks
+        // column pair (a, j) of the chunk: one division per chunk, then the
+        // output address advances by Bp per j and wraps to the next table
         const int ncol = 6 * nv;
         const uint32_t lane_base = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+        const long long awrap = (long long)N * N * nv * Bp - (long long)nv * Bp;
         for (int c0 = 16 * half; c0 < ncol; c0 += 32) {
             float v[16];
             tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+            const int aj0 = c0 >> 1, a0 = aj0 / nv;
+            int j = aj0 - a0 * nv;
+            long long o = (((long long)a0 * N * N + pid) * nv + j) * Bp + c;
 #pragma unroll
             for (int u = 0; u < 16; u += 2) {
-                const int col = c0 + u;
-                if (col < ncol) {
-                    const int aj = col >> 1, a = aj / nv, j = aj - a * nv;
-                    Y[(((long long)a * N * N + pid) * nv + j) * Bp + c] = make_float2(v[u], v[u + 1]);
+                if (c0 + u < ncol) Y[o] = make_float2(v[u], v[u + 1]);
+                o += Bp;
+                if (++j == nv) {
+                    j = 0;
+                    o += awrap;
                 }
             }
         }
@@ -473,18 +480,24 @@ __global__ void __launch_bounds__(kThreads) k_pj2_tc(const float2 *__restrict__ 
     if (ok) {
         // columns (p, j2, re/im) of this thread's row; the two warps of a lane
         // quarter take alternate 16-column chunks
-        const long long zs = (long long)N * nv * nv * Bp;
+        // column pair (p, j2) of the chunk: one division per chunk, then the
+        // output address advances by nv Bp per j2 and wraps to the next source
+        const long long zs = (long long)N * nv * nv * Bp, js = (long long)nv * Bp;
         const int ncol = 10 * nv;
         const uint32_t lane_base = tmem + ((uint32_t)(32 * (w & 3)) << 16);
         for (int c0 = 16 * half; c0 < ncol; c0 += 32) {
             float v[16];
             tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+            const int pj0 = c0 >> 1, p0 = pj0 / nv;
+            int j2 = pj0 - p0 * nv;
+            long long o = p0 * zs + (((long long)k1 * nv + j2) * nv + j3) * Bp + c;
 #pragma unroll
             for (int u = 0; u < 16; u += 2) {
-                const int col = c0 + u;
-                if (col < ncol) {
-                    const int pj = col >> 1, p = pj / nv, j2 = pj - p * nv;
-                    Z[p * zs + (((long long)k1 * nv + j2) * nv + j3) * Bp + c] = make_float2(v[u], v[u + 1]);
+                if (c0 + u < ncol) Z[o] = make_float2(v[u], v[u + 1]);
+                o += js;
+                if (++j2 == nv) {
+                    j2 = 0;
+                    o += zs - (long long)nv * js;
                 }
             }
         }
