@@ -203,7 +203,7 @@ lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
  * DFTs, the direct sums along axis 1 and the inverse axis-2 DFTs, its
  * operands brought in by bulk copies -- form 0 runs the axis-3/axis-2 DFTs,
  * the axis-1 sums and the inverse axis-2 DFTs as three kernels through
- * device memory.  Both forms give the same FP32 results.  The environment
+ * device memory.  Both forms agree to FP32 rounding.  The environment
  * variable LP_FQ_FUSED=0 makes form 0 the default of new contexts; the
  * autotuners time both and keep the faster (form 1 at n <= 24, form 0 at
  * n = 32 on GB300). */

@@ -28,9 +28,11 @@
 // (spectra read).  Every wait is bounded in time; a wait that runs out sets
 // *err and that thread waits no more, so the kernel ends.
 //
-// The arithmetic is that of the three-pass form operation for operation
-// (the same DFT routines on the same inputs, the axis-1 sums in the same
-// order), so both forms give the same FP32 results.
+// The arithmetic is that of the three-pass form except for where the
+// axis-1 weight (u1 - h)^e1 of the b-arrays enters: here it scales the
+// b-pencil before its axis-2 DFT (an exact integer factor combined with
+// (u2 - h)^e2), there the axis-2 outputs during the axis-1 sum.  Both forms
+// agree to FP32 rounding.
 #include "lp_kernels.cuh"
 #include "lp_dev.cuh"
 #include "lp_fft.cuh"
@@ -69,8 +71,7 @@ template <int N> struct Fqf {
 };
 
 // The pairs: a-array p (X1 array p) with the b-array formed from X1 array
-// bsrc(p) = 7 + e3 times (u2 - h)^e2 before the axis-2 DFT, weighted by
-// (u1 - h)^e1 in the axis-1 sum.  (ahat, 1), (S00, u1^2), (S11, u2^2),
+// bsrc(p) = 7 + e3 times (u2 - h)^e2 (u1 - h)^e1 before the axis-2 DFT.  (ahat, 1), (S00, u1^2), (S11, u2^2),
 // (S22, u3^2), (S01, u1 u2), (S02, u1 u3), (S12, u2 u3).
 __device__ __forceinline__ int bsrc(int p) { return p == 3 ? 9 : (p >= 5 ? 8 : 7); }
 __device__ __forceinline__ int be2(int p) { return p == 2 ? 2 : ((p == 4 || p == 6) ? 1 : 0); }
@@ -116,20 +117,27 @@ __global__ void __launch_bounds__(128) k_fq_x1(const float2 *__restrict__ F, con
 
 // One pair's direct sum along axis 1 for the outputs i = 2 j + r (j < n/2)
 // of one (k2, k3, cell): a(l) and b(u) from the spectrum rows (stride RS),
-// b weighted by (u1 - h)^e1.  b is held shifted by the parity r and padded
-// with a zero at each end, yb[v + 1] = b(v + r) for v in [-1, n), so both
-// parities run the same code.  Each output sums its terms in the order of
-// the three-pass form's y_part (l ascending), plus one product with a
-// padding zero.
+// b already weighted by (u1 - h)^e1 (the producers fold that weight into
+// the scaling of the b-pencil before its axis-2 DFT).  b is held shifted by
+// the parity r and padded with a zero at each end, yb[v + 1] = b(v + r) for
+// v in [-1, n), so both parities run the same code; the row offsets are
+// compile-time constants from a base moved by r rows.  Each output sums its
+// terms in l ascending order, plus one product with a padding zero.
 template <int N, int RS>
-__device__ __forceinline__ void ysum2(const float2 *__restrict__ as, const float2 *__restrict__ bs, int r, int e1,
+__device__ __forceinline__ void ysum2(const float2 *__restrict__ as, const float2 *__restrict__ bs, int r,
                                       unsigned long long (&A)[N / 2], unsigned long long (&B)[N / 2]) {
     constexpr int n = N, h = N / 2, NJ = N / 2;
     unsigned long long yb[N + 1];
+    const float2 *bb = bs + r * RS;  // b(v + r) = bb[v * RS] for v in [0, n - 1) and both parities
+    {
+        const float2 lo = r ? bs[0] : make_float2(0.f, 0.f);             // v = -1: b(0) when r = 1
+        const float2 hi = r ? make_float2(0.f, 0.f) : bs[(n - 1) * RS];  // v = n - 1: b(n - 1) when r = 0
+        yb[0] = pk2(lo.x, lo.y);
+        yb[n] = pk2(hi.x, hi.y);
+    }
 #pragma unroll
-    for (int v = -1; v < n; ++v) {
-        const int u = v + r;
-        const float2 val = (u >= 0 && u < n) ? cscale(bs[u * RS], poww(u, h, e1)) : make_float2(0.f, 0.f);
+    for (int v = 0; v < n - 1; ++v) {
+        const float2 val = bb[v * RS];
         yb[v + 1] = pk2(val.x, val.y);
     }
 #pragma unroll
@@ -239,9 +247,13 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
             if (which == 0) {
                 fwd_pencil_st<N, true>(x, tw.fa, st);
             } else {
-                if (e2) {
+                // (u2 - h)^e2 along the pencil times (u1 - h)^e1 of its row:
+                // small integers, so the combined weight is exact in FP32
+                const int e1 = be1(p);
+                if (e2 || e1) {
+                    const float w1 = poww(l, h, e1);
 #pragma unroll
-                    for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2));
+                    for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2) * w1);
                 }
                 fwd_pencil_st<N, false>(x, tw.fw, st);
             }
@@ -266,7 +278,7 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
                 const int g = 7 * i + p, s = g & 1;
                 fq_wait(&full2[s], (uint32_t)((g >> 1) & 1), err, bad, 5);
                 const float2 *as = s2 + (2 * s) * P::SL2 + k2 * CB + cc, *bs = as + P::SL2;
-                ysum2<N, P::RS2>(as, bs, r, be1(p), A, B);
+                ysum2<N, P::RS2>(as, bs, r, A, B);
                 if (g + 2 < G) tc::mbar_arrive(&empty2[s]);
             }
             tc::named_sync(2, P::TY);  // the previous tile's inverse DFTs are done with gs

@@ -2,11 +2,13 @@
 form 1 keeps the axis-2 spectra on chip (axis-3 DFTs into device memory,
 then one kernel per (k3, group of cells) for the axis-2 DFTs, the axis-1
 sums and the inverse axis-2 DFTs), form 0 runs them as three kernels through
-device memory.  Both evaluate the same FP32 operations in the same order:
-ComputeQ at every supported n (the reference's golden vectors at n = 8, 16,
-24, the oracle at n = 32) and whole collision steps, including passes split
-into several convolution chunks, agree to FP32 rounding between the forms
-and each stays within the FP32 tolerance of the reference values."""
+device memory.  Both evaluate the same FP32 operations except where the
+b-arrays' axis-1 weight enters (before the axis-2 DFT in form 1, after it in
+form 0).  ComputeQ at every supported n (the reference's golden vectors at
+n = 8, 16, 24, the oracle at n = 32) and whole collision steps, including
+passes split into several convolution chunks, agree to FP32 rounding between
+the forms, and each stays within the FP32 tolerance of the reference
+values."""
 from __future__ import annotations
 
 import numpy as np
@@ -18,7 +20,7 @@ from oracle.oracle import Case, FIX_DEFAULT, Oracle
 pytestmark = pytest.mark.gpu
 
 TOL_Q = 2e-5    # FP32 evaluation of Qhat against FP64 reference values
-TOL_FORMS = 1e-6  # the two forms: the same FP32 operations
+TOL_FORMS = 1e-6  # the two forms: FP32 evaluations of the same sums
 
 
 def _ctx(lp, case, precision=None, fixes=FIX_DEFAULT):
