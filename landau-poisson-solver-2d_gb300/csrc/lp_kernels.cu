@@ -1815,7 +1815,9 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ I
                                                      double dv, double lv, MomRow mr) {
     extern __shared__ double ssm[];
     double(*S)[5][33] = reinterpret_cast<double(*)[5][33]>(ssm);  // [record][coefficient][cell]
-    double(*L)[5] = reinterpret_cast<double(*)[5]>(ssm + kScatRec * 5 * 33);
+    // the cells' multipliers, converted to FP32 once here (the correction is
+    // formed in FP32; a conversion per record would load GB300's narrow FP64 pipe)
+    float(*L)[5] = reinterpret_cast<float(*)[5]>(ssm + kScatRec * 5 * 33);
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     double *ut = ssm + kScatRec * 5 * 33 + 32 * 5 + w * 7 * kScatRec;  // this warp's records of U
     const int nv3 = nv * nv * nv;
@@ -1837,7 +1839,7 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ I
     }
     if (t < 160) {
         const int cc = t / 5, q = t - cc * 5;
-        L[cc][q] = (lam && cb + cc < B) ? lam[5 * (cb + cc) + q] : 0.;
+        L[cc][q] = (lam && cb + cc < B) ? (float)lam[5 * (cb + cc) + q] : 0.f;
     }
     __syncthreads();
     const int kt = kt0 + lane, j3 = kt % nv, j2 = (kt / nv) % nv, j1 = kt / (nv * nv);
@@ -1863,8 +1865,7 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ I
         if (lane < nrec) {
             double a[5] = {S[lane][0][cc], S[lane][1][cc], S[lane][2][cc], S[lane][3][cc], S[lane][4][cc]};
             if (lam) {  // Phi^T lambda (mom_correct with the cell centre of this lane's record)
-                const float l0 = (float)L[cc][0], l1 = (float)L[cc][1], l2 = (float)L[cc][2], l3 = (float)L[cc][3],
-                            l4 = (float)L[cc][4];
+                const float l0 = L[cc][0], l1 = L[cc][1], l2 = L[cc][2], l3 = L[cc][3], l4 = L[cc][4];
                 const float gl = G[0] * l1 + G[1] * l2 + G[2] * l3;
                 a[0] += f32_to_f64_bits(l0 + gl + (g2 + dv2q) * l4);
                 a[1] += f32_to_f64_bits(dv12 * l1 + dv6 * G[0] * l4);
@@ -1888,43 +1889,39 @@ __global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ I
 
 // The multipliers of one cell per block from the partials part[c][5][nk]
 // (coalesced) and, when given, the target partials tpart[nchunk][5][Bp].
-__global__ void __launch_bounds__(256) k_lambda_inc(const double *__restrict__ tpart, int nchunk,
+__global__ void __launch_bounds__(160) k_lambda_inc(const double *__restrict__ tpart, int nchunk,
                                                     const double *__restrict__ part, int nk,
                                                     const double *__restrict__ gm_inv, double scale, double kfac,
                                                     const double *__restrict__ cdt, int Bp,
                                                     double *__restrict__ lam) {
-    __shared__ double red[2][5][256];
-    const int c = blockIdx.x, t = threadIdx.x;
-    double tg[5] = {0, 0, 0, 0, 0}, ac[5] = {0, 0, 0, 0, 0};
-    const double *pc = part + (long long)c * 5 * nk;
-#pragma unroll
-    for (int m = 0; m < 5; ++m)
-        for (int k = t; k < nk; k += 256) ac[m] += pc[m * nk + k];
+    // one block of five warps per cell: warp m sums moment m of the
+    // increments' partials (and of the target's, two-species operator) over
+    // a fixed strided subset per lane and a fixed butterfly of shuffles;
+    // threads 0..4 then solve with the inverse Gram matrix.  The FP64
+    // dependency chains stay short on GB300's narrow FP64 unit.
+    __shared__ double r5[5];
+    const int c = blockIdx.x, lane = threadIdx.x & 31, m = threadIdx.x >> 5;
+    const double *pc = part + ((long long)c * 5 + m) * nk;
+    double ac = 0., tg = 0.;
+    for (int k = lane; k < nk; k += 32) ac += pc[k];
     if (tpart)
-        for (int k = t; k < nchunk; k += 256)
-            for (int m = 0; m < 5; ++m) tg[m] += tpart[((long long)k * 5 + m) * Bp + c];
-    for (int m = 0; m < 5; ++m) {
-        red[0][m][t] = tg[m];
-        red[1][m][t] = ac[m];
+        for (int k = lane; k < nchunk; k += 32) tg += tpart[((long long)k * 5 + m) * Bp + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ac += __shfl_xor_sync(0xffffffffu, ac, o);
+        tg += __shfl_xor_sync(0xffffffffu, tg, o);
+    }
+    if (lane == 0) {
+        const double sc = cdt ? cdt[c] * kfac : scale;
+        r5[m] = sc * tg - ac;
     }
     __syncthreads();
-    for (int wd = 128; wd > 0; wd >>= 1) {
-        if (t < wd)
-            for (int m = 0; m < 5; ++m) {
-                red[0][m][t] += red[0][m][t + wd];
-                red[1][m][t] += red[1][m][t + wd];
-            }
-        __syncthreads();
-    }
-    if (t == 0) {
-        if (cdt) scale = cdt[c] * kfac;
-        double r[5];
-        for (int m = 0; m < 5; ++m) r[m] = scale * red[0][m][0] - red[1][m][0];
-        for (int i = 0; i < 5; ++i) {
-            double sum = 0;
-            for (int j = 0; j < 5; ++j) sum += gm_inv[i * 5 + j] * r[j];
-            lam[5 * c + i] = sum;
-        }
+    if (threadIdx.x < 5) {
+        const int i = threadIdx.x;
+        double sum = 0.;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) sum += gm_inv[i * 5 + j] * r5[j];
+        lam[5 * c + i] = sum;
     }
 }
 
@@ -2970,7 +2967,7 @@ cudaError_t launch_project_inc(const double2 *q0, const double2 *q1, const doubl
 cudaError_t launch_lambda_inc(const double *tpart, int nchunk, const double *part, int n, int nv, int B, int Bp,
                               const double *gm_inv, double scale, double kfac, double *lam, cudaStream_t st,
                               Rates rates) {
-    k_lambda_inc<<<B, 256, 0, st>>>(tpart, nchunk, part, project_inc_blocks(n, nv), gm_inv, scale, kfac, rates.dt, Bp,
+    k_lambda_inc<<<B, 160, 0, st>>>(tpart, nchunk, part, project_inc_blocks(n, nv), gm_inv, scale, kfac, rates.dt, Bp,
                                     lam);
     return cudaGetLastError();
 }
