@@ -190,8 +190,17 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
     float2 *s2 = fsm + 4 * P::SL1;   // [slot][a, b][SL2] spectra
     float2 *gs = s2 + 4 * P::SL2;    // [i1][k2][cc] a tile's axis-1 sums
     __shared__ __align__(8) uint64_t bar[8];  // fa[2], fb[2], full2[2], empty2[2]
+    // the axis-2 twiddles of the a-side (with the output phase) and of the
+    // b-side: one DFT routine serves both through a table pointer (the
+    // b-side's q2 = 0 row is exactly 1, so applying it changes nothing),
+    // which halves the producers' unrolled code
+    __shared__ float2 tws[2][48];
     uint64_t *fa = bar, *fb = bar + 2, *full2 = bar + 4, *empty2 = bar + 6;
     const int tid = threadIdx.x;
+    if (tid < 48) {
+        tws[0][tid] = tw.fa[tid];
+        tws[1][tid] = tw.fw[tid];
+    }
     const int my_tiles = (ntile - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     const int G = 7 * my_tiles;
     const bool issuer = tid == P::TY;
@@ -244,9 +253,7 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
             if (g >= 2) fq_wait(&empty2[s], (uint32_t)(((g - 2) >> 1) & 1), err, bad, 4);
             float2 *dst = s2 + (2 * s + which) * P::SL2 + l * P::RS2 + cc;
             auto st = [&](int k, float2 v) { dst[k * CB] = v; };
-            if (which == 0) {
-                fwd_pencil_st<N, true>(x, tw.fa, st);
-            } else {
+            if (which) {
                 // (u2 - h)^e2 along the pencil times (u1 - h)^e1 of its row:
                 // small integers, so the combined weight is exact in FP32
                 const int e1 = be1(p);
@@ -255,8 +262,8 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
 #pragma unroll
                     for (int m = 0; m < n; ++m) x[m] = cscale(x[m], poww(m, h, e2) * w1);
                 }
-                fwd_pencil_st<N, false>(x, tw.fw, st);
             }
+            fwd_pencil_st<N, true>(x, tws[which], st);
             tc::mbar_arrive(&full2[s]);
             // refills two steps ahead once every producer has read step g's slices
             tc::fence_async_smem();    // this thread's slice reads before the bulk copies' writes
