@@ -76,7 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout, r.stderr)
     if force or _stale(LIB, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs)
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-ldl"])
     # C++ drop-in driver (reference routine signatures over the C ABI)
     dsrc = [os.path.join(HOST, "lp_dropin.cpp"), os.path.join(HOST, "dropin_driver.cpp")]
     if all(os.path.exists(s) for s in dsrc) and (force or _stale(DROPIN_TEST, dsrc + [LIB] + hdrs)):

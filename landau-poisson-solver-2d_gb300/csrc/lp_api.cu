@@ -10,12 +10,25 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "lp_gb300.h"
 #include "lp_adjoint.cuh"
 #include "lp_kernels.cuh"
 #include "lp_tables.h"
 
 using lp::V2;
+
+// An NVTX range over a host scope: the stages of a step appear as named
+// ranges in Nsight timelines and ncu's NVTX filters (no cost without a tool
+// attached).  Work that a CUDA graph replays is marked where it is captured
+// and where the graph is launched.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 constexpr int kHostChunksMax = 16;  // chunks of lp_collision_step_host
 
@@ -448,6 +461,7 @@ lp_status poisson_mixed(lp_ctx *c, const double *Us) {
 // Mixed path: fluxes in FP32 from FP32 stage copies, the stage combinations,
 // charge sums and Poisson solves in FP64.
 lp_status advect(lp_ctx *c) {
+    NvtxRange r("RK3 advection + LDG Poisson");
     const lp::AdvectDev ad = advect_dev(c);
     if (!c->mixed) {
         LP_TRY(poisson_on(c, c->U));
@@ -672,15 +686,25 @@ template <typename R> lp_status collide_batch(lp_ctx *c, int c0, int B) {
     const lp::Tables &T = c->T;
     const int Bp = round32(B);
     const int slot1 = (T.prm.fixes & LP_FIX_F2) ? 3 : 2;
-    LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
-                                c->stream));
-    LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream,
-                              c->dff));
+    {
+        NvtxRange rn("setInit_spectral + fft3D");
+        LP_CUDA(lp::launch_nodes<R>(c->U, T.nv, T.n, c0, B, Bp, slot1, c->nodecell, c->nodeoff, T.dv, (R *)c->f,
+                                    c->stream));
+        LP_CUDA(lp::launch_fwd<R>((const R *)c->f, (C *)c->t1, (C *)c->F, (const R *)c->mfwd, T.n, Bp, c->stream,
+                                  c->dff));
+    }
     const bool lazy = lazy_cons(c);
     // FP32 mode arrays: the convolution form's output is FP32-accurate
     const bool f32 = lazy && c->FQC && c->line_warps == 0 && c->qf[0];
-    LP_TRY(stage_q<R>(c, Bp, c->q[0], lazy ? 0 : -1, f32 ? c->qf[0] : nullptr));
-    LP_TRY(rk4_stages<R>(c, c0, Bp, lazy, f32));
+    {
+        NvtxRange r("ComputeQ + conserveAllMoments, stage 0");
+        LP_TRY(stage_q<R>(c, Bp, c->q[0], lazy ? 0 : -1, f32 ? c->qf[0] : nullptr));
+    }
+    {
+        NvtxRange r("RK4 stages 1-3 (FS, fft3D, ComputeQ, conserveAllMoments)");
+        LP_TRY(rk4_stages<R>(c, c0, Bp, lazy, f32));
+    }
+    NvtxRange r("DG projection (IntModes) and moment correction");
     if (fused_tail(c)) return project_fused(c, c0, B, Bp, lazy, f32);
     LP_TRY(project<R>(c, c0, B, Bp, true));
     return LP_OK;
@@ -703,6 +727,7 @@ template <typename R> lp_status collide_batch_prefix(lp_ctx *c, int c0, int B) {
 }
 
 lp_status collide(lp_ctx *c, int c0, int c1) {
+    NvtxRange r("collision step");
     // All batches read the pre-collision state (the reference scatters after
     // the loop), so dU of every batch is kept and scattered at the end when
     // the whole range fits one batch; larger ranges are processed batch by
@@ -1387,6 +1412,7 @@ lp_status lp_advect_step(lp_ctx *c) {
 }
 
 lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
+    NvtxRange r("lp_collision_step");
     if (!c) return LP_ERR_INVALID;
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
     if (cell_begin == -1 && cell_end == -1) { cell_begin = 0; cell_end = c->T.ncollide; }
@@ -1423,6 +1449,7 @@ lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
 }
 
 lp_status lp_collision_step_host(lp_ctx *c, const double *U_in, double *U_out, int chunks, int flags) {
+    NvtxRange r("lp_collision_step_host");
     if (!c || !U_in || !U_out || chunks < 1 || chunks > kHostChunksMax || (flags & ~LP_HOST_ASYNC))
         return LP_ERR_INVALID;
     if (!c->collide_on || !c->owns_state) return fail(c, LP_ERR_INVALID, "no collision tables or state in this context");
@@ -1514,6 +1541,7 @@ lp_status lp_collision_graph_kernels(lp_ctx *c, int *kernels) {
 }
 
 lp_status lp_step(lp_ctx *c, int nsteps) {
+    NvtxRange r("lp_step");
     if (!c || nsteps < 0) return LP_ERR_INVALID;
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
     if (nsteps == 0) return LP_OK;
@@ -2038,6 +2066,7 @@ lp_status lp_batch_collision_step(lp_batch *b) {
 }
 
 lp_status lp_batch_step(lp_batch *b, int nsteps) {
+    NvtxRange r("lp_batch_step");
     if (!b || nsteps < 0) return LP_ERR_INVALID;
     if (!batch_ready(b)) return bfail(b, LP_ERR_STATE, "a run has no state");
     if (nsteps == 0) return LP_OK;
@@ -2215,6 +2244,7 @@ lp_status lp_step_vjp(lp_ctx *c, const double *lout, double *lin, double *dnu) {
 }
 
 lp_status lp_field_energy_gradient(lp_ctx *c, int nsteps, int checkpoint, double *J, double *dU0, double *dnu) {
+    NvtxRange r("lp_field_energy_gradient (checkpointed adjoint)");
     if (!c || nsteps < 0 || checkpoint < 1 || !J || !dU0) return LP_ERR_INVALID;
     if (!c->has_state) return fail(c, LP_ERR_STATE, "no state uploaded");
     LP_TRY(adj_setup(c));
