@@ -64,6 +64,25 @@ def profiled_traffic(kernel):
     return None, None
 
 
+def profiled_fma_pipe(kernel):
+    """Fraction of cycles the FP32 FMA pipe was busy in one launch of
+    `kernel` (sm__pipe_fma_cycles_active), from the committed ncu summaries
+    under profiles/: a line `fma_pipe <kernel>: <percent> %`.  Returns
+    (fraction, summary file) or (None, None)."""
+    import re
+    if not os.path.isdir(PROFILES):
+        return None, None
+    pat = re.compile(r"^fma_pipe\s+" + re.escape(kernel) + r":\s*([0-9.]+)\s*%", re.M)
+    for name in sorted(os.listdir(PROFILES)):
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(PROFILES, name)) as f:
+            m = pat.search(f.read())
+        if m:
+            return float(m.group(1)) / 100.0, "profiles/" + name
+    return None, None
+
+
 def fq_kernel_model(n, cells):
     """Algorithmic DRAM bytes and FP32 flops per launch of the four kernels of
     the convolution form (complex FP32 intermediates of 8 bytes, q in FP64):
@@ -705,9 +724,12 @@ def main():
                     "algorithmic_bytes": dom["algorithmic_bytes"], "peak_kind": peak_kind,
                     "kernel": dom["kernel"] + " (the largest kernel of the convolution form)",
                     "ms_per_launch": dom["ms_per_launch"]}
+            fma_busy, fma_src = profiled_fma_pipe(dom["kernel"])
             comp = {"pipe": "fp32 FMA (packed f32x2, CUDA cores)", "kernel": dom["kernel"],
                     "achieved_tflops": dom["tflops"], "peak_tflops": fp32_peak,
                     "frac": (dom["tflops"] / fp32_peak) if (dom["tflops"] and fp32_peak) else None,
+                    "flops_counted": "the direct axis-1 sums only (7 pairs x 432 (i, l) pairs x 8 x M^2 per cell)",
+                    "fma_pipe_busy_ncu": fma_busy, "fma_pipe_source": fma_src,
                     "peak_kind": "measured (FMA-chain microbenchmark)", "fp64_peak_tflops": fp64_peak}
         else:
             achieved = contract_bytes / (t_contract_ms * 1e-3) / 1e9
