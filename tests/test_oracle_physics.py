@@ -45,3 +45,28 @@ def test_reference_field_scaling_shifts_frequency():
     omega, _, peaks = rate(ts, ee, t_max=6.0)
     assert len(peaks) >= 3
     assert 1.6 < omega < 1.8, omega
+
+
+def test_dg_mass_matrix_of_the_collision_basis():
+    """The collided DG coefficients of a velocity cell (slots 0, 3-6: 1,
+    the three centred linears and |xi|^2 in cell units xi in [-1/2, 1/2]^3)
+    have the mass matrix whose inverse the RK4 update applies
+    (source/collisionRoutines_1.cpp:894-901: the moments tp0..tp5 enter as
+    tp0 + U5/4 and U0/4 + 19 U5/240, and the new coefficients are
+    19 tp0/4 - 15 tp5, 12 tp_i and 60 tp5 - 15 tp0).  Gauss-Legendre
+    quadrature over the unit cell gives the matrix and its inverse."""
+    x, w = np.polynomial.legendre.leggauss(4)
+    x, w = x / 2, w / 2  # nodes and weights on [-1/2, 1/2]
+    X1, X2, X3 = np.meshgrid(x, x, x, indexing="ij")
+    W = np.einsum("i,j,k->ijk", w, w, w)
+    basis = [np.ones_like(X1), X1, X2, X3, X1 ** 2 + X2 ** 2 + X3 ** 2]
+    M = np.array([[np.sum(W * a * b) for b in basis] for a in basis])
+    # the forward map the reference applies: moments from coefficients
+    assert np.allclose(M[0], [1, 0, 0, 0, 1 / 4], atol=1e-15)
+    assert np.allclose(M[4], [1 / 4, 0, 0, 0, 19 / 240], atol=1e-15)
+    assert np.allclose(np.diag(M)[1:4], 1 / 12, atol=1e-15)
+    Minv = np.linalg.inv(M)
+    assert np.allclose(Minv[0, [0, 4]], [19 / 4, -15], atol=1e-12)
+    assert np.allclose(Minv[4, [0, 4]], [-15, 60], atol=1e-12)
+    assert np.allclose(np.diag(Minv)[1:4], 12, atol=1e-12)
+    assert np.allclose(Minv[1:4, [0, 4]], 0, atol=1e-12)
