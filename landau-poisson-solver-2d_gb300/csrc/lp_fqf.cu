@@ -24,8 +24,8 @@
 // cell, output parity)) sum the slot along axis 1 while the producers fill
 // the other slot, and after a tile's seventh pair run its inverse axis-2
 // DFTs while the producers start on the next tile.  The hand-offs are
-// mbarriers: full1 (bulk copy landed), full2 (spectra written), empty2
-// (spectra read).  Every wait is bounded in time; a wait that runs out sets
+// mbarriers: fa and fb (the a- and b-slice bulk copies landed), full2
+// (spectra written), empty2 (spectra read).  Every wait is bounded in time; a wait that runs out sets
 // *err and that thread waits no more, so the kernel ends.
 //
 // The arithmetic is that of the three-pass form except for where the
