@@ -206,7 +206,10 @@ lp_status lp_set_schedule(lp_ctx *ctx, int pass_cells, int line_warps);
  * device memory.  Both forms agree to FP32 rounding.  The environment
  * variable LP_FQ_FUSED=0 makes form 0 the default of new contexts; the
  * autotuners time both and keep the faster (form 1 at n <= 24, form 0 at
- * n = 32 on GB300). */
+ * n = 32 on GB300).  A pass runs the convolution in chunks of cells, 64 or
+ * more while their scratch stays within 512 MB; LP_FQ_CHUNK=<cells> (a
+ * multiple of 32) in the environment at context creation sets a smaller
+ * chunk.  The chunk changes no result: each cell's sums are the same. */
 lp_status lp_set_convolution_form(lp_ctx *ctx, int form);
 lp_status lp_get_convolution_form(const lp_ctx *ctx, int *form);
 

@@ -327,6 +327,13 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
             const size_t per_cell = lp::fftq_scratch_elems(T.n, 1) * sizeof(float2);
             const int fit = (int)std::min<size_t>((size_t)c->Bcap, (512ull << 20) / per_cell) / 32 * 32;
             c->fq_bs = std::min(c->Bcap, std::max(64, fit));
+            // LP_FQ_CHUNK=<cells> (a multiple of 32) in the environment sets a
+            // smaller chunk: the intermediates of a smaller chunk stay in L2
+            // between the convolution's kernels
+            if (const char *cenv = std::getenv("LP_FQ_CHUNK")) {
+                const int v = std::atoi(cenv) / 32 * 32;
+                if (v >= 32 && v < c->fq_bs) c->fq_bs = v;
+            }
             LP_TRY(dalloc(c, &c->fscr, lp::fftq_scratch_elems(T.n, c->fq_bs)));
             c->ftw = lp::fftq_twiddles(T.n);
             // the fused convolution (LP_FQ_FUSED=0 in the environment keeps

@@ -59,7 +59,8 @@ template <int N> struct Fqf {
     static constexpr int SL1 = N * RS1;  // one X1 slice (float2)
     static constexpr int RS2 = CB < 16 ? (M + 1) * CB : M * CB;
     static constexpr int SL2 = N * RS2;  // one array's spectrum in shared memory
-    // consumer threads: two (the output parities) per (k2, cell) of a tile;
+    // consumer threads: two (the real and imaginary parts of the a-arrays)
+    // per (k2, cell) of a tile;
     // producer threads after them
     static constexpr int UY = M * CB, TY = 2 * UY, TP = 32 * PW, T = TY + TP;
     // two a-slice slots, two b-slice slots, two spectrum slots of a pair's
@@ -115,42 +116,33 @@ __global__ void __launch_bounds__(128) k_fq_x1(const float2 *__restrict__ F, con
     }
 }
 
-// One pair's direct sum along axis 1 for the outputs i = 2 j + r (j < n/2)
-// of one (k2, k3, cell): a(l) and b(u) from the spectrum rows (stride RS),
-// b already weighted by (u1 - h)^e1 (the producers fold that weight into
-// the scaling of the b-pencil before its axis-2 DFT).  b is held shifted by
-// the parity r and padded with a zero at each end, yb[v + 1] = b(v + r) for
-// v in [-1, n), so both parities run the same code; the row offsets are
-// compile-time constants from a base moved by r rows.  Each output sums its
-// terms in l ascending order, plus one product with a padding zero.
+// One pair's direct sum along axis 1 for every output i of one (k2, k3,
+// cell), one component of a per thread: P[i] += a_s(l) (b.x, b.y)(u) with
+// u = i + h - l, a_s = Re a (s = 0) or Im a (s = 1), a(l) and b(u) from the
+// spectrum rows (stride RS), b already weighted by (u1 - h)^e1 (the
+// producers fold that weight into the scaling of the b-pencil before its
+// axis-2 DFT).  The two threads of a lane pair hold the two components; a
+// b-row is held in registers, only the (i, l) with u on the grid are
+// summed, and each output sums its terms in l ascending order.
 template <int N, int RS>
-__device__ __forceinline__ void ysum2(const float2 *__restrict__ as, const float2 *__restrict__ bs, int r,
-                                      unsigned long long (&A)[N / 2], unsigned long long (&B)[N / 2]) {
-    constexpr int n = N, h = N / 2, NJ = N / 2;
-    unsigned long long yb[N + 1];
-    const float2 *bb = bs + r * RS;  // b(v + r) = bb[v * RS] for v in [0, n - 1) and both parities
-    {
-        const float2 lo = r ? bs[0] : make_float2(0.f, 0.f);             // v = -1: b(0) when r = 1
-        const float2 hi = r ? make_float2(0.f, 0.f) : bs[(n - 1) * RS];  // v = n - 1: b(n - 1) when r = 0
-        yb[0] = pk2(lo.x, lo.y);
-        yb[n] = pk2(hi.x, hi.y);
-    }
+__device__ __forceinline__ void ysum_c(const float2 *__restrict__ as, const float2 *__restrict__ bs, int s,
+                                       unsigned long long (&P)[N]) {
+    constexpr int n = N, h = N / 2;
+    unsigned long long yb[N];
 #pragma unroll
-    for (int v = 0; v < n - 1; ++v) {
-        const float2 val = bb[v * RS];
-        yb[v + 1] = pk2(val.x, val.y);
+    for (int u = 0; u < n; ++u) {
+        const float2 val = bs[u * RS];
+        yb[u] = pk2(val.x, val.y);
     }
+    const float *ac = reinterpret_cast<const float *>(as) + s;
 #pragma unroll
     for (int l = 0; l < n; ++l) {
-        const float2 a = as[l * RS];
-        const unsigned long long ar = pk2(a.x, a.x), ai = pk2(a.y, a.y);
+        const float a = ac[2 * l * RS];
+        const unsigned long long a2 = pk2(a, a);
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int v = 2 * j + h - l;  // u - r
-            if (v >= -1 && v < n) {
-                A[j] = fma2(ar, yb[v + 1], A[j]);
-                B[j] = fma2(ai, yb[v + 1], B[j]);
-            }
+        for (int i = 0; i < n; ++i) {
+            const int u = i + h - l;
+            if (u >= 0 && u < n) P[i] = fma2(a2, yb[u], P[i]);
         }
     }
 }
@@ -274,27 +266,33 @@ __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict
             }
         }
     } else {
-        // consumers: thread (k2, cc, parity r) sums the outputs i = 2 j + r
-        // of every pair of its tile, then the tile's inverse axis-2 DFTs
+        // consumers: the lane pair (k2, cc) sums every output of every pair
+        // of its tile, lane s with component s of a (P0 = Re a b, P1 = Im a b,
+        // G = (P0.x - P1.y, P0.y + P1.x)), then the tile's inverse axis-2 DFTs
         const int r = tid & 1, uid = tid >> 1, k2 = uid / CB, cc = uid % CB;
         for (int i = 0; i < my_tiles; ++i) {
-            unsigned long long A[NJ], B[NJ];
+            unsigned long long Pc[N];
 #pragma unroll
-            for (int j = 0; j < NJ; ++j) A[j] = B[j] = 0ull;
+            for (int j = 0; j < N; ++j) Pc[j] = 0ull;
             for (int p = 0; p < 7; ++p) {
                 const int g = 7 * i + p, s = g & 1;
                 fq_wait(&full2[s], (uint32_t)((g >> 1) & 1), err, bad, 5);
                 const float2 *as = s2 + (2 * s) * P::SL2 + k2 * CB + cc, *bs = as + P::SL2;
-                ysum2<N, P::RS2>(as, bs, r, A, B);
+                ysum_c<N, P::RS2>(as, bs, r, Pc);
                 if (g + 2 < G) tc::mbar_arrive(&empty2[s]);
             }
             tc::named_sync(2, P::TY);  // the previous tile's inverse DFTs are done with gs
             {
+                // lane r writes the outputs i = 2 j + r, taking the partner's
+                // component of them in exchange for its own of the others
                 float2 *gp = gs + r * P::RS2 + k2 * CB + cc;
 #pragma unroll
                 for (int j = 0; j < NJ; ++j) {
-                    const float2 a = up2(A[j]), b = up2(B[j]);
-                    gp[2 * j * P::RS2] = make_float2(a.x - b.y, a.y + b.x);
+                    const float2 send = up2(r ? Pc[2 * j] : Pc[2 * j + 1]), own = up2(r ? Pc[2 * j + 1] : Pc[2 * j]);
+                    const float2 got = make_float2(__shfl_xor_sync(0xffffffffu, send.x, 1),
+                                                   __shfl_xor_sync(0xffffffffu, send.y, 1));
+                    const float2 p0 = r ? got : own, p1 = r ? own : got;
+                    gp[2 * j * P::RS2] = make_float2(p0.x - p1.y, p0.y + p1.x);
                 }
             }
             tc::named_sync(2, P::TY);

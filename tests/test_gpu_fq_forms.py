@@ -64,15 +64,20 @@ def test_compute_q_forms_n32(gpu_lib):
     assert rel(q1, O.compute_q(f)) < TOL_Q
 
 
-# every supported n; nx1 = 160 with passes of 160 cells splits each pass
-# into convolution chunks of 64, 64 and 32 cells; the 2-D case runs 12 x 8
-@pytest.mark.parametrize("nx1,nx2,n,nv,lv", [(40, 1, 8, 8, 5.25), (160, 1, 16, 4, 5.25), (64, 1, 24, 8, 5.0),
-                                              (12, 8, 24, 8, 5.0), (36, 1, 32, 4, 5.25)],
+# every supported n; nx1 = 160 with passes of 160 cells and convolution
+# chunks of at most 64 cells (LP_FQ_CHUNK=64) splits each pass into chunks of
+# 64, 64 and 32 cells; the 2-D case runs 12 x 8
+@pytest.mark.parametrize("nx1,nx2,n,nv,lv,chunk", [(40, 1, 8, 8, 5.25, 0), (160, 1, 16, 4, 5.25, 64),
+                                                    (64, 1, 24, 8, 5.0, 0), (12, 8, 24, 8, 5.0, 0),
+                                                    (36, 1, 32, 4, 5.25, 0)],
                          ids=["n8", "n16-chunks", "n24", "n24-2d", "n32"])
-def test_collision_step_forms(gpu_lib, nx1, nx2, n, nv, lv):
+def test_collision_step_forms(gpu_lib, monkeypatch, nx1, nx2, n, nv, lv, chunk):
     lp = gpu_lib
     case = Case(nx1=nx1, nx2=nx2, nv=nv, n=n, lv=lv, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.5, k_wave=0.5)
+    if chunk:
+        monkeypatch.setenv("LP_FQ_CHUNK", str(chunk))
     ctx = _ctx(lp, case)
+    monkeypatch.delenv("LP_FQ_CHUNK", raising=False)
     ctx.set_schedule(min(160, ((nx1 * nx2 + 31) // 32) * 32), 0)
     ctx.set_init(1)
     U0 = ctx.get_state()
@@ -116,3 +121,37 @@ def test_graph_replay_after_form_change(gpu_lib):
     assert rel(s1, s0) < TOL_FORMS
     with pytest.raises(lp.LPError):
         ctx.set_convolution_form(2)
+
+
+@pytest.mark.parametrize("n,nv", [(24, 8), (16, 4)])
+def test_chunked_convolution_passes(gpu_lib, monkeypatch, n, nv):
+    """LP_FQ_CHUNK=32 at context creation splits each 96-cell pass into three
+    convolution chunks of 32 cells.  Every cell's sums, and its conservation
+    partials, are the same operations in the same order as in one chunk of
+    96, so a whole time step matches the unsplit context bit for bit, in
+    both kernel forms."""
+    lp = gpu_lib
+    case = Case(nx1=96, nx2=1, nv=nv, n=n, lv=5.0, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.5, k_wave=0.5)
+
+    def run(chunk):
+        if chunk:
+            monkeypatch.setenv("LP_FQ_CHUNK", str(chunk))
+        else:
+            monkeypatch.delenv("LP_FQ_CHUNK", raising=False)
+        ctx = _ctx(lp, case)
+        ctx.set_schedule(96, 0)
+        ctx.set_init(1)
+        U0 = ctx.get_state()
+        out = []
+        for form in (0, 1):
+            ctx.set_convolution_form(form)
+            ctx.set_state(U0)
+            ctx.step(1)
+            ctx.synchronize()
+            out.append(ctx.get_state())
+        return out
+
+    whole, split = run(0), run(32)
+    monkeypatch.delenv("LP_FQ_CHUNK", raising=False)
+    for form in (0, 1):
+        assert np.array_equal(split[form], whole[form])
