@@ -774,7 +774,9 @@ def main():
                         "ms_per_step_by_chunks": {str(k): 1e3 * v for k, v in e2e_try.items()}},
                 "roofline": roof, "compute_roofline": comp,
                 "cpu_baseline": cb, "clocks": clk.summary(),
-                "gpu_launches": ctx.collision_graph_kernels() * args.steps}
+                "gpu_launches": ctx.collision_graph_kernels() * args.steps,
+                "graph": {"kernels": ctx.collision_graph_kernels(),
+                          "programmatic_edges": ctx.collision_graph_edges()}}
         line.update(extra)
         if ws == 1 and not args.no_secondary and args.precision == "mixed":
             line["secondary"] = secondary_lines(args)

@@ -165,6 +165,15 @@ lp_status lp_collision_step_host(lp_ctx *ctx, const double *U_in, double *U_out,
 /* Kernel launches in one replay of the captured collision step over every
  * collided cell (its graph's kernel nodes); 0 before the first such step. */
 lp_status lp_collision_graph_kernels(lp_ctx *ctx, int *kernels);
+/* Programmatic kernel-to-kernel edges of that graph; 0 before the first
+ * such step and by default.  With LP_PDL=1 (or 2) in the environment at
+ * capture, the step graphs (collision step, time step, host-buffer collision
+ * chunks, batch step) are instantiated with every edge from one kernel to the
+ * next made a programmatic dependency: the next grid may be launched once
+ * every block of the previous one has exited (or, with 2, started).  Each
+ * kernel waits on the device for its predecessors' completion before it
+ * reads anything, so results are unchanged either way. */
+lp_status lp_collision_graph_edges(lp_ctx *ctx, int *programmatic);
 /* nsteps passes of the time loop (advection, then collisions when nu > 0),
  * replayed from one captured CUDA graph per step. */
 lp_status lp_step(lp_ctx *ctx, int nsteps);

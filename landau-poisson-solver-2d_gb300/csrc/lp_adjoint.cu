@@ -23,6 +23,7 @@ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // a * conj(b)
 // xi loop over the box where xi + n/2 - a lies in the grid (a correlation).
 __global__ void k_qvjp(const double2 *__restrict__ F, const double2 *__restrict__ lq, const double *__restrict__ P,
                        const int *__restrict__ pair_off, int n, int Bp, double2 *__restrict__ lF) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const int n3 = n * n * n, h = n / 2;
     if (tid >= (long long)n3 * Bp) return;
@@ -60,6 +61,7 @@ __global__ void k_qvjp(const double2 *__restrict__ F, const double2 *__restrict_
 // (tp0, tp2, tp3, tp4, tp5).
 __global__ void k_projT1(const double *__restrict__ ltp, const double *__restrict__ tf, int n, int nv, int Bp,
                          double2 *__restrict__ lZ) {
+    lp_grid_wait();
     // lZ[p][k1][j2][j3]: p0 = T0 tp0 + T1 tp2 + T2 tp5, p1 = T0 tp3, p2 = T0 tp5, p3 = T0 tp4, p4 = T0 tp5
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nv2 = (long long)nv * nv, nv3 = nv2 * nv;
@@ -88,6 +90,7 @@ __global__ void k_projT1(const double *__restrict__ ltp, const double *__restric
 
 __global__ void k_projT2(const double2 *__restrict__ lZ, const double *__restrict__ tf, int n, int nv, int Bp,
                          double2 *__restrict__ lY) {
+    lp_grid_wait();
     // lY[a][k1][k2][j3]: a0 = T0 Z0 + T1 Z1 + T2 Z2, a1 = T0 Z3, a2 = T0 Z4 (conjugated factors)
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= (long long)n * n * nv * Bp) return;
@@ -115,6 +118,7 @@ __global__ void k_projT2(const double2 *__restrict__ lZ, const double *__restric
 
 __global__ void k_projT3(const double2 *__restrict__ lY, const double *__restrict__ tf, int n, int nv, int Bp,
                          double2 *__restrict__ lQ) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= (long long)n * n * n * Bp) return;
     const int c = (int)(tid % Bp);
@@ -138,6 +142,7 @@ __global__ void k_projT3(const double2 *__restrict__ lY, const double *__restric
 // lam_in (slots 1, 2 pass through).
 __global__ void k_collide_out_vjp(const double *__restrict__ lout, int nv, int c0, int B, int Bp, double dt,
                                   double kfac, double *__restrict__ ltp, double *__restrict__ lin) {
+    lp_grid_wait();
     const long long nv3 = (long long)nv * nv * nv;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= nv3 * Bp) return;
@@ -172,6 +177,7 @@ __global__ void k_collide_out_vjp(const double *__restrict__ lout, int nv, int c
 __global__ void k_nodes_vjp(const double *__restrict__ lf, int nv, int n, int c0, int B, int Bp, int slot1,
                             const int *__restrict__ nfirst, const int *__restrict__ ncount,
                             const double *__restrict__ nodeoff, double *__restrict__ lin) {
+    lp_grid_wait();
     const long long nv3 = (long long)nv * nv * nv;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= nv3 * B) return;
@@ -193,11 +199,13 @@ __global__ void k_nodes_vjp(const double *__restrict__ lf, int nv, int n, int c0
 // ---------------------------------------------------------------- elementwise helpers (cell-minor)
 // y = a*y + b*x for real arrays (a == 0: y is not read)
 __global__ void k_axpby(double *__restrict__ y, double a, const double *__restrict__ x, double b, long long n) {
+    lp_grid_wait();
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) y[i] = a == 0. ? b * x[i] : a * y[i] + b * x[i];
 }
 // y = a*y + b*x for complex arrays (a == 0: y is not read)
 __global__ void k_caxpby(double2 *__restrict__ y, double a, const double2 *__restrict__ x, double b, long long n) {
+    lp_grid_wait();
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double2 v = x[i];
@@ -206,12 +214,14 @@ __global__ void k_caxpby(double2 *__restrict__ y, double a, const double2 *__res
 }
 // y (real) = a*y + b*Re x (a == 0: y is not read)
 __global__ void k_add_re(double *__restrict__ y, double a, const double2 *__restrict__ x, double b, long long n) {
+    lp_grid_wait();
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) y[i] = a == 0. ? b * x[i].x : a * y[i] + b * x[i].x;
 }
 // out[c] += scale * sum_pt x[pt][c] y[pt][c] (real) over cells c < B; one warp per cell
 __global__ void k_dot_cell(const double *__restrict__ x, const double *__restrict__ y, long long npt, int Bp, int B,
                            double scale, double *__restrict__ out) {
+    lp_grid_wait();
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
     double s = 0.;
@@ -222,6 +232,7 @@ __global__ void k_dot_cell(const double *__restrict__ x, const double *__restric
 // out[c] += scale * Re sum_pt conj(x) y (complex)
 __global__ void k_cdot_cell(const double2 *__restrict__ x, const double2 *__restrict__ y, long long npt, int Bp,
                             int B, double scale, double *__restrict__ out) {
+    lp_grid_wait();
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
     double s = 0.;
@@ -235,6 +246,7 @@ __global__ void k_cdot_cell(const double2 *__restrict__ x, const double2 *__rest
 // Qc / nu = q0/2 + (q1 + q2 + q3)/6
 __global__ void k_qsum(const double2 *__restrict__ q0, const double2 *__restrict__ q1, const double2 *__restrict__ q2,
                        const double2 *__restrict__ q3, long long n, double2 *__restrict__ out) {
+    lp_grid_wait();
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double2 a = q0[i], b = q1[i], d = q2[i], e = q3[i];
@@ -248,6 +260,7 @@ __global__ void k_qsum(const double2 *__restrict__ q0, const double2 *__restrict
 // the per-cell field adjoints lam_f = (ie, ixe, ixxe) per cell.
 __global__ void k_flux_vjp(AdvectDev ad, const double *__restrict__ V, const double *__restrict__ fields,
                            const double *__restrict__ lamH, double *__restrict__ lamV, double *__restrict__ lamF) {
+    lp_grid_wait();
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= ad.size) return;
     const int nv = ad.nv;
@@ -344,6 +357,7 @@ __global__ void k_flux_vjp(AdvectDev ad, const double *__restrict__ V, const dou
 
 // lam_H = c * lam_out for every record (stage adjoint source)
 __global__ void k_scale(double *__restrict__ y, const double *__restrict__ x, double c, long long n) {
+    lp_grid_wait();
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) y[i] = c * x[i];
 }
@@ -355,6 +369,7 @@ __global__ void k_scale(double *__restrict__ y, const double *__restrict__ x, do
 __global__ void k_poisson_vjp(PoissonDev pd, const double *__restrict__ lamF, const double *__restrict__ lphix,
                               const double *__restrict__ lphiy, const double *__restrict__ Ainv,
                               double *__restrict__ lrt) {
+    lp_grid_wait();
     extern __shared__ double sm[];
     const int nc = pd.nx * pd.ny, nd = pd.ndim, t = threadIdx.x;
     double *lpx = sm, *lpy = sm + 3 * nc, *lb = sm + 6 * nc;
@@ -416,6 +431,7 @@ __global__ void k_poisson_vjp(PoissonDev pd, const double *__restrict__ lamF, co
 // lam_U[rec] += scalev * (lam_rt0, lam_rt1, lam_rt2) on slots (0 and 6/4, 1, 2)
 __global__ void k_charge_vjp(const double *__restrict__ lrt, long long size, int nv3, double scalev,
                              double *__restrict__ lamU) {
+    lp_grid_wait();
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= size) return;
     const long long s = k / nv3;
@@ -428,6 +444,7 @@ __global__ void k_charge_vjp(const double *__restrict__ lrt, long long size, int
 // gradient with respect to phix, phiy (one block).
 __global__ void k_field_energy(const double *__restrict__ phix, const double *__restrict__ phiy, int nc, double dxdy,
                                double *__restrict__ J, double *__restrict__ lphix, double *__restrict__ lphiy) {
+    lp_grid_wait();
     __shared__ double red[256];
     const int t = threadIdx.x;
     double s = 0.;

@@ -160,12 +160,92 @@ struct lp_ctx {
     // captured step, and captured collision step of all collided cells
     cudaGraphExec_t gexec = nullptr, cgexec = nullptr;
     int cg_kernels = 0;  // kernel nodes of the captured collision step
+    int cg_pdl = 0;      // its programmatic kernel-to-kernel edges
     cudaStream_t gstream = nullptr, cgstream = nullptr;
 };
 
 namespace {
 
 constexpr int kMomBlocks = 240;
+
+// Programmatic kernel-to-kernel edges in a captured step graph.  Each edge
+// from one kernel node to another becomes a programmatic dependency on the
+// upstream kernel's `port`: the downstream grid may be launched before the
+// upstream kernel has completed (once its blocks have all exited, or all
+// started).  Every kernel of the library starts with lp_grid_wait, which holds its
+// blocks until the upstream grids have completed and their writes are
+// visible, so the graph keeps stream order.  Edges to or from other nodes
+// (copies, memsets) stay as captured.
+cudaError_t make_edges_programmatic(cudaGraph_t g, int port, int *nconv) {
+    *nconv = 0;
+    size_t ne = 0;
+    cudaError_t e = cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &ne);
+    if (e != cudaSuccess || ne == 0) return e;
+    std::vector<cudaGraphNode_t> from(ne), to(ne);
+    std::vector<cudaGraphEdgeData> ed(ne);
+    e = cudaGraphGetEdges(g, from.data(), to.data(), ed.data(), &ne);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> kf, kt;
+    std::vector<cudaGraphEdgeData> kold;
+    for (size_t i = 0; i < ne; ++i) {
+        cudaGraphNodeType tf, tt;
+        if (cudaGraphNodeGetType(from[i], &tf) != cudaSuccess || cudaGraphNodeGetType(to[i], &tt) != cudaSuccess)
+            return cudaErrorInvalidValue;
+        if (tf != cudaGraphNodeTypeKernel || tt != cudaGraphNodeTypeKernel) continue;
+        if (ed[i].type != cudaGraphDependencyTypeDefault || ed[i].from_port != cudaGraphKernelNodePortDefault)
+            continue;
+        kf.push_back(from[i]);
+        kt.push_back(to[i]);
+        kold.push_back(ed[i]);
+    }
+    if (kf.empty()) return cudaSuccess;
+    cudaGraphEdgeData pd{};
+    pd.from_port = (unsigned char)port;
+    pd.type = cudaGraphDependencyTypeProgrammatic;
+    const std::vector<cudaGraphEdgeData> knew(kf.size(), pd);
+    e = cudaGraphRemoveDependencies(g, kf.data(), kt.data(), kold.data(), kf.size());
+    if (e != cudaSuccess) return e;
+    e = cudaGraphAddDependencies(g, kf.data(), kt.data(), knew.data(), kf.size());
+    if (e != cudaSuccess) {
+        cudaGraphAddDependencies(g, kf.data(), kt.data(), kold.data(), kf.size());
+        return e;
+    }
+    *nconv = (int)kf.size();
+    return cudaSuccess;
+}
+
+// Instantiates a captured step graph.  LP_PDL in the environment at capture
+// selects programmatic kernel-to-kernel edges: 1 from the upstream kernel's
+// programmatic port (the next grid is launched as the last upstream block
+// exits), 2 from its launch-completion port (as the last upstream block
+// starts); unset or 0 keeps the edges as captured.  On GB300 at 64 cells,
+// n = 24, the collision step takes the same time with port 1 and 5% longer
+// with port 2 (the next grids' waiting blocks are placed while the current
+// kernel runs), so ordinary edges are the default.  A refused edge update or
+// instantiation falls back to the graph as captured.  *pdl_edges: the
+// programmatic edges of the instantiated graph.
+cudaError_t instantiate_step_graph(cudaGraphExec_t *exec, cudaGraph_t g, int *pdl_edges = nullptr) {
+    if (pdl_edges) *pdl_edges = 0;
+    const char *env = std::getenv("LP_PDL");
+    if (env && (env[0] == '1' || env[0] == '2')) {
+        const int port = env[0] == '2' ? cudaGraphKernelNodePortLaunchCompletion
+                                       : cudaGraphKernelNodePortProgrammatic;
+        cudaGraph_t pg = nullptr;
+        if (cudaGraphClone(&pg, g) == cudaSuccess) {
+            int nconv = 0;
+            cudaError_t e = make_edges_programmatic(pg, port, &nconv);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(exec, pg, 0);
+            cudaGraphDestroy(pg);
+            if (e == cudaSuccess) {
+                if (pdl_edges) *pdl_edges = nconv;
+                return e;
+            }
+            *exec = nullptr;
+        }
+        cudaGetLastError();  // a refused update or instantiation leaves no sticky error
+    }
+    return cudaGraphInstantiate(exec, g, 0);
+}
 
 lp_status fail(lp_ctx *c, lp_status s, const std::string &msg) {
     if (c) c->err = msg;
@@ -1446,7 +1526,7 @@ lp_status lp_collision_step(lp_ctx *c, int cell_begin, int cell_end) {
                         ++c->cg_kernels;
                 }
         }
-        e = cudaGraphInstantiate(&c->cgexec, g, 0);
+        e = instantiate_step_graph(&c->cgexec, g, &c->cg_pdl);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
         c->cgstream = c->stream;
@@ -1518,7 +1598,7 @@ lp_status lp_collision_step_host(lp_ctx *c, const double *U_in, double *U_out, i
             c->U = keep;
             if (st != LP_OK) { if (gr) cudaGraphDestroy(gr); return st; }
             if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&g, gr, 0);
+            e = instantiate_step_graph(&g, gr);
             cudaGraphDestroy(gr);
             if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
             c->hgraphs.push_back({b, c0, c1, g});
@@ -1547,6 +1627,12 @@ lp_status lp_collision_graph_kernels(lp_ctx *c, int *kernels) {
     return LP_OK;
 }
 
+lp_status lp_collision_graph_edges(lp_ctx *c, int *programmatic) {
+    if (!c || !programmatic) return LP_ERR_INVALID;
+    *programmatic = c->cgexec ? c->cg_pdl : 0;
+    return LP_OK;
+}
+
 lp_status lp_step(lp_ctx *c, int nsteps) {
     NvtxRange r("lp_step");
     if (!c || nsteps < 0) return LP_ERR_INVALID;
@@ -1560,7 +1646,7 @@ lp_status lp_step(lp_ctx *c, int nsteps) {
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
         if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        e = instantiate_step_graph(&c->gexec, g);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
         c->gstream = c->stream;
@@ -2085,7 +2171,7 @@ lp_status lp_batch_step(lp_batch *b, int nsteps) {
         const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (s != LP_OK) { if (g) cudaGraphDestroy(g); return s; }
         if (e != cudaSuccess) return bfail(b, LP_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
-        const cudaError_t e2 = cudaGraphInstantiate(&b->gexec, g, 0);
+        const cudaError_t e2 = instantiate_step_graph(&b->gexec, g);
         cudaGraphDestroy(g);
         if (e2 != cudaSuccess) return bfail(b, LP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e2));
         b->gstream = b->stream;
@@ -2408,6 +2494,7 @@ namespace {
 // x1) from those of the whole grid; layout [14][cells] on both sides.
 __global__ void k_slab_fields(const double *__restrict__ gf, int gnc, double *__restrict__ f, int nc, int nx2,
                               int i1_off, int gnx1) {
+    lp::lp_grid_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nc) return;
     const int i1 = s / nx2, i2 = s % nx2;

@@ -35,6 +35,7 @@ __device__ __forceinline__ double2 cmulc2(double2 a, double2 b) {  // a * conj(b
 // cell-minor with kCorrCells cells); one thread per (output point, cell)
 __global__ void k_sep_pass(const double2 *__restrict__ in, int d0, int d1, int d2, int ax,
                            const double2 *__restrict__ Mat, int dout, double2 *__restrict__ out) {
+    lp_grid_wait();
     int e[3] = {d0, d1, d2};
     const int din = e[ax];
     e[ax] = dout;
@@ -67,6 +68,7 @@ __global__ void k_sep_pass(const double2 *__restrict__ in, int d0, int d1, int d
 // (stride Bp); lam (kind 2): g = lam_q of those cells
 __global__ void k_corr_make(const double2 *__restrict__ src, int Bp, int c0, int B, const double *__restrict__ Cp,
                             int p, int n, int kind, double2 *__restrict__ g) {
+    lp_grid_wait();
     const long long n3 = (long long)n * n * n;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= n3 * kCorrCells) return;
@@ -89,6 +91,7 @@ __global__ void k_corr_make(const double2 *__restrict__ src, int Bp, int c0, int
 
 // G = L conj(G), elementwise
 __global__ void k_corr_prod(const double2 *__restrict__ L, double2 *__restrict__ G, long long nel) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid < nel) G[tid] = cmulc2(L[tid], G[tid]);
 }
@@ -97,6 +100,7 @@ __global__ void k_corr_prod(const double2 *__restrict__ L, double2 *__restrict__
 // w_p(x) for one with a_p (kind 1)
 __global__ void k_corr_acc(const double2 *__restrict__ R, const double *__restrict__ Cp, int p, int n, int kind,
                            bool first, double2 *__restrict__ acc) {
+    lp_grid_wait();
     const long long n3 = (long long)n * n * n;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= n3 * kCorrCells) return;
@@ -116,6 +120,7 @@ __global__ void k_corr_acc(const double2 *__restrict__ R, const double *__restri
 }
 
 __global__ void k_corr_store(const double2 *__restrict__ acc, int n, int Bp, int c0, int B, double2 *__restrict__ lF) {
+    lp_grid_wait();
     const long long n3 = (long long)n * n * n;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= n3 * kCorrCells) return;

@@ -57,6 +57,7 @@ constexpr int kPY = 4;  // pencils per block (blockDim.y); blockDim.x = 32 cells
 template <int N, int PY, int CB>
 __global__ void __launch_bounds__(CB * PY) k_fq_x12(const float2 *__restrict__ F, const float *__restrict__ C,
                                                     int Bp, int c0, float2 *__restrict__ X, int Bs, FftTw tw) {
+    lp_grid_wait();
     constexpr int n = N, h = N / 2, M = 3 * N / 2;
     extern __shared__ float2 t3[];  // [m][k3][CB]
     const int tx = threadIdx.x, ty = threadIdx.y, l = blockIdx.x, t = blockIdx.z;
@@ -180,6 +181,7 @@ __device__ __forceinline__ void y_part(const float2 *__restrict__ base, size_t p
 // Dynamic shared memory: 2 stages x 2N values x blockDim threads.
 template <int N, int NI, int PY>
 __global__ void __launch_bounds__(32 * PY) k_fq_y(const float2 *__restrict__ X, int Bs, float2 *__restrict__ G) {
+    lp_grid_wait();
     constexpr int M = 3 * N / 2;
     extern __shared__ float2 ysm[];
     const int pen = blockIdx.x * PY + threadIdx.y;
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(32 * PY) k_fq_y(const float2 *__restrict__ X, 
 template <int N>
 __global__ void __launch_bounds__(32 * kPY) k_fq_z1(const float2 *__restrict__ G, int Bs, float2 *__restrict__ H,
                                                     FftTw tw) {
+    lp_grid_wait();
     constexpr int n = N, M = 3 * N / 2;
     const int pen = blockIdx.x * kPY + threadIdx.y;
     if (pen >= n * M) return;
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(32 * kPY) k_fq_z1(const float2 *__restrict__ G
 template <int N, typename QT, bool CONS>
 __global__ void __launch_bounds__(32 * kPY) k_fq_z2(const float2 *__restrict__ H, int Bs, QT *__restrict__ q,
                                                     int Bp, int c0, FftTw tw, ConsFused cons) {
+    lp_grid_wait();
     constexpr int n = N, M = 3 * N / 2;
     const int pen = blockIdx.x * kPY + threadIdx.y;
     const int cell = blockIdx.y * 32 + threadIdx.x;

@@ -89,6 +89,7 @@ __device__ __forceinline__ bool bstart(int p) { return p == 0 || p == 3 || p == 
 template <int N>
 __global__ void __launch_bounds__(128) k_fq_x1(const float2 *__restrict__ F, const float *__restrict__ C, int Bp,
                                                int c0, int Bc, float2 *__restrict__ X1, FftTw tw) {
+    lp_grid_wait();
     using P = Fqf<N>;
     constexpr int n = N, h = N / 2, CB = P::CB;
     const long long g = (long long)blockIdx.x * 128 + threadIdx.x;
@@ -174,6 +175,7 @@ __device__ __forceinline__ void fq_wait(uint64_t *mb, uint32_t parity, int *err,
 template <int N>
 __global__ void __launch_bounds__(Fqf<N>::T, 1) k_fq_yz(const float2 *__restrict__ X1, int ntile, int Bs,
                                                          float2 *__restrict__ H, FftTw tw, int *__restrict__ err) {
+    lp_grid_wait();
     using P = Fqf<N>;
     constexpr int n = N, h = N / 2, M = P::M, CB = P::CB, NJ = N / 2;
     extern __shared__ __align__(128) float2 fsm[];

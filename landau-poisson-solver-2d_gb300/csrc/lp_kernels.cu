@@ -53,6 +53,7 @@ __global__ void k_pairs(const double *__restrict__ eta, const double *__restrict
                         const double *__restrict__ ahat, const unsigned char *__restrict__ rzero,
                         const double *__restrict__ cw, const int *__restrict__ pair_off, int n,
                         double *__restrict__ P64, float *__restrict__ P32, unsigned *__restrict__ PI) {
+    lp_grid_wait();
     const int xi = blockIdx.x, h = n / 2;
     const int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
     // window of omega where u = xi + n/2 - omega lies in the grid (C:764-789)
@@ -93,6 +94,7 @@ __device__ double weight_lin_dev(const double *eta, const double *shat, int n, i
 __global__ void k_lin_weights(const double *__restrict__ eta, const double *__restrict__ shat,
                               const double *__restrict__ cw, const long long *__restrict__ win_off, int n,
                               double scale3, double *__restrict__ W64, float *__restrict__ W32) {
+    lp_grid_wait();
     const int xi = blockIdx.x, h = n / 2;
     const int i = xi / (n * n), j = (xi / n) % n, k = xi % n;
     const int si = i < h ? 0 : i - h + 1, sj = j < h ? 0 : j - h + 1, sk = k < h ? 0 : k - h + 1;
@@ -114,6 +116,7 @@ __global__ void k_lin_weights(const double *__restrict__ eta, const double *__re
 template <typename R>
 __global__ void k_qlin(const typename V2<R>::t *__restrict__ F, const R *__restrict__ Wl,
                        const long long *__restrict__ win_off, int n, int Bp, double2 *__restrict__ ql) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const int n3 = n * n * n, h = n / 2;
     if (tid >= (long long)n3 * Bp) return;
@@ -161,6 +164,7 @@ __global__ void k_qlin(const typename V2<R>::t *__restrict__ F, const R *__restr
 
 // q += ql (the two-species stage's mode array, C:656-698)
 __global__ void k_qadd(double2 *__restrict__ q, const double2 *__restrict__ ql, long long total) {
+    lp_grid_wait();
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t < total) { const double2 a = q[t], b = ql[t]; q[t] = make_double2(a.x + b.x, a.y + b.y); }
 }
@@ -174,6 +178,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_nodes_t(const double *__restrict__ U, int nv, int n, int c0, int B, int Bp,
                                                  int slot1, const int *__restrict__ nodecell,
                                                  const double *__restrict__ nodeoff, R *__restrict__ f) {
+    lp_grid_wait();
     __shared__ R tile[32][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int lm = blockIdx.x, l = lm / n, m = lm - l * n, cb = blockIdx.y * 32;
@@ -214,6 +219,7 @@ __global__ void k_dft(const TIn *__restrict__ in, typename V2<R>::t *__restrict_
                       const R *__restrict__ M, int n, int ax, int Bp, int stage, R dt, R nu,
                       const R *__restrict__ f, R *__restrict__ qn, R *__restrict__ f1,
                       const double *__restrict__ cnu, const double *__restrict__ cdt) {
+    lp_grid_wait();
     using C = typename V2<R>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *Ms = reinterpret_cast<C *>(smem_raw);
@@ -279,6 +285,7 @@ __global__ void __launch_bounds__(32 * PY * OG) k_dftp(const TIn *__restrict__ i
                                                        R *__restrict__ f1, const double *__restrict__ cnu,
                                                        const double *__restrict__ cdt, const float *__restrict__ cf,
                                                        const double *__restrict__ lamc) {
+    lp_grid_wait();
     using C = typename V2<R>::t;
     constexpr int NO = N / OG;  // outputs per thread
     __shared__ C Ms[N * N];
@@ -451,6 +458,7 @@ __global__ void __launch_bounds__(32 * PY) k_fftf(const TIn *__restrict__ in, fl
                                                   float *__restrict__ qn, float *__restrict__ f1,
                                                   const double *__restrict__ cnu, const double *__restrict__ cdt,
                                                   const float *__restrict__ cf, const double *__restrict__ lamc) {
+    lp_grid_wait();
     __shared__ float cfs[PY][5][N];
     if (cf) {
         constexpr int n3 = N * N * N;
@@ -521,6 +529,7 @@ __global__ void __launch_bounds__(32 * PY) k_fftf_fs(const float2 *__restrict__ 
                                                      const __grid_constant__ DftFac ff, int Bp, int stage, float dt,
                                                      float nu, const float *__restrict__ f, float *__restrict__ qn,
                                                      const double *__restrict__ cnu, const double *__restrict__ cdt) {
+    lp_grid_wait();
     const int pid = blockIdx.x * PY + threadIdx.y;
     if (pid >= N * N) return;
     const int c = blockIdx.y * 32 + threadIdx.x;
@@ -564,6 +573,7 @@ __global__ void __launch_bounds__(CB * N) k_fftf_plane(const float2 *__restrict_
                                                        float dt, float nu, const float *__restrict__ f,
                                                        float *__restrict__ qn, const double *__restrict__ cnu,
                                                        const double *__restrict__ cdt) {
+    lp_grid_wait();
     constexpr int RS = N * CB + 8;  // row stride (float2) of the plane
     __shared__ float2 pl[N * RS];
     const int c = threadIdx.x, p = threadIdx.y, i2 = blockIdx.x, cb = blockIdx.y * CB;
@@ -718,6 +728,7 @@ __global__ void __launch_bounds__(128) k_computeq(const typename V2<R>::t *__res
                                                   const R *__restrict__ P, const unsigned *__restrict__ PI,
                                                   const int *__restrict__ pair_off, int n3, int Bp,
                                                   double2 *__restrict__ q) {
+    lp_grid_wait();
     using C = typename V2<R>::t;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int xi = blockIdx.x * 4 + warp;
@@ -810,6 +821,7 @@ template <int N, int TILE, int LW>
 __global__ void __launch_bounds__(32 * LW, 12 / LW) k_cq_lines(const float2 *__restrict__ F, const float *__restrict__ W,
                                                             const long long *__restrict__ line_off, int Bp,
                                                             double2 *__restrict__ q) {
+    lp_grid_wait();
     constexpr int KT = LinesCfg<N>::KT, h = N / 2, K0 = TILE * KT;
     constexpr int TP = pp_floats<N, KT>(), TOFF = tile_off<N, KT>(TILE);
     constexpr int TT = tile_floats<N>(K0, K0 + KT);  // weight floats of this tile per plane pair
@@ -937,6 +949,7 @@ __global__ void k_lines_table(const double *__restrict__ eta, const double *__re
                               const double *__restrict__ ahat, const unsigned char *__restrict__ rzero,
                               const double *__restrict__ cw, const long long *__restrict__ line_off,
                               float *__restrict__ W) {
+    lp_grid_wait();
     constexpr int KT = LinesCfg<N>::KT, NT = N / KT, h = N / 2, TP = pp_floats<N, KT>();
     const int ij = blockIdx.x, i = ij / N, j = ij % N;
     const int si = i < h ? 0 : i - h + 1, ni = i < h ? i + h + 1 : 3 * h - 1 - i;
@@ -977,6 +990,7 @@ template <typename QT>
 __global__ void k_cons_partial(const QT *__restrict__ q, const double *__restrict__ c1,
                                const double *__restrict__ c2, int n3, int Bp, int nchunk,
                                double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[8][5][32];
     const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
     const int cs = (n3 + nchunk - 1) / nchunk, p0 = k * cs, p1 = min(n3, p0 + cs);
@@ -1013,6 +1027,7 @@ __global__ void k_cons_partial(const QT *__restrict__ q, const double *__restric
 __global__ void __launch_bounds__(160) k_cons_lambda(const double *__restrict__ part, int nchunk,
                                                      const double *__restrict__ cct, int Bp,
                                                      double *__restrict__ lam) {
+    lp_grid_wait();
     __shared__ double t5[5];
     const int c = blockIdx.x, lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     double v = 0.;
@@ -1032,6 +1047,7 @@ __global__ void __launch_bounds__(160) k_cons_lambda(const double *__restrict__ 
 
 __global__ void k_cons_apply(double2 *__restrict__ q, const double *__restrict__ c1,
                              const double *__restrict__ c2, const double *__restrict__ lam, int n3, int Bp) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= (long long)n3 * Bp) return;
     const int c = (int)(tid % Bp), pt = (int)(tid / Bp);
@@ -1050,6 +1066,7 @@ __global__ void k_qcomb(const double2 *__restrict__ q0, const double2 *__restric
                         const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
                         long long total, int Bp, const double *__restrict__ cnu,
                         typename V2<R>::t *__restrict__ Qc) {
+    lp_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= total) return;
     if (cnu) nu = cnu[tid % Bp];
@@ -1069,6 +1086,7 @@ constexpr int JB = 8;
 template <typename R>
 __global__ void k_proj3(const typename V2<R>::t *__restrict__ Qc, const R *__restrict__ tf, int n, int nv,
                         int Bp, typename V2<R>::t *__restrict__ Y) {
+    lp_grid_wait();
     const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long total = (long long)n * n * nch * Bp;
@@ -1108,6 +1126,7 @@ __global__ void k_proj3(const typename V2<R>::t *__restrict__ Qc, const R *__res
 template <typename R>
 __global__ void k_proj2(const typename V2<R>::t *__restrict__ Y, const R *__restrict__ tf, int n, int nv,
                         int Bp, typename V2<R>::t *__restrict__ Z) {
+    lp_grid_wait();
     const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long total = (long long)n * nv * nch * Bp;
@@ -1156,6 +1175,7 @@ template <typename R>
 __global__ void k_proj1(const typename V2<R>::t *__restrict__ Z, const R *__restrict__ tf, int n, int nv,
                         int Bp, int B, int c0, const double *__restrict__ U, int ustride, int4 us, int us4,
                         double dt, double kfac, const double *__restrict__ cdt, double *__restrict__ dU) {
+    lp_grid_wait();
     const int nch = (nv + JB - 1) / JB;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nv3 = (long long)nv * nv * nv;
@@ -1223,6 +1243,7 @@ __global__ void k_mom_target(const double2 *__restrict__ q0, const double2 *__re
                              const double2 *__restrict__ q2, const double2 *__restrict__ q3, double nu,
                              const double *__restrict__ cnu, const double *__restrict__ gmom, int n3, int Bp,
                              int nchunk, double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[8][5][32];
     const int cl = threadIdx.x, y = threadIdx.y, c = blockIdx.y * 32 + cl, k = blockIdx.x;
     if (cnu) nu = cnu[c];
@@ -1265,6 +1286,7 @@ inline MomRow mom_row(double dv) { return MomRow{dv / 12., dv / 6., dv * dv / 4.
 
 __global__ void k_mom_actual(const double *__restrict__ dU, const double *__restrict__ U, int nv, double dv,
                              double lv, MomRow mr, int c0, int nrc, double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[5][256];
     const int cc = blockIdx.y, t = threadIdx.x;
     const long long nv3 = (long long)nv * nv * nv;
@@ -1298,6 +1320,7 @@ __global__ void k_mom_lambda(const double *__restrict__ tpart, int nchunk, const
                              int nk, long long sc, long long sk, long long sm, const double *__restrict__ gm_inv,
                              double scale, double kfac, const double *__restrict__ cdt, int B, int Bp,
                              double *__restrict__ lam) {
+    lp_grid_wait();
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= B) return;
     if (cdt) scale = cdt[c] * kfac;
@@ -1338,6 +1361,7 @@ __device__ __forceinline__ void mom_correct(double a[5], const double *l, double
 
 __global__ void k_mom_apply(double *__restrict__ dU, const double *__restrict__ lam, int nv, double dv, double lv,
                             MomRow mr, long long nrec) {
+    lp_grid_wait();
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     const long long nv3 = (long long)nv * nv * nv;
@@ -1351,6 +1375,7 @@ __global__ void k_mom_apply(double *__restrict__ dU, const double *__restrict__ 
 // moment correction Phi^T lambda applied on the way when lam is given.
 __global__ void k_scatter(const double *__restrict__ dU, long long nrec, long long r0, double *__restrict__ U,
                           const double *__restrict__ lam, int nv, double dv, double lv, MomRow mr) {
+    lp_grid_wait();
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     const double *dd = dU + 5 * r;
@@ -1378,6 +1403,7 @@ __global__ void __launch_bounds__(32 * kIncWarps)
     k_proj1_inc(const float2 *__restrict__ Z, const float *__restrict__ tf, int n, int nv, int Bp, int B, double dt,
                 double kfac, const double *__restrict__ cdt, double dv, double lv, MomRow mr,
                 float *__restrict__ Inc, double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[kIncWarps][5][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c = blockIdx.y * 32 + lane;
@@ -1486,6 +1512,7 @@ __global__ void __launch_bounds__(128) k_pj3(const QT *__restrict__ q0, const QT
                                              double nu, const double *__restrict__ cnu, const float *__restrict__ tf,
                                              int nv, int Bp, float2 *__restrict__ Y, const float *__restrict__ cf,
                                              const double *__restrict__ lam4) {
+    lp_grid_wait();
     extern __shared__ float2 Ts[];
     for (int t = threadIdx.y * 32 + threadIdx.x; t < 3 * N * nv; t += 128) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
     __syncthreads();
@@ -1553,6 +1580,7 @@ __global__ void __launch_bounds__(128) k_pj3(const QT *__restrict__ q0, const QT
 template <int N>
 __global__ void __launch_bounds__(128) k_pj2(const float2 *__restrict__ Y, const float *__restrict__ tf, int nv,
                                              int Bp, float2 *__restrict__ Z) {
+    lp_grid_wait();
     extern __shared__ float2 Ts[];
     for (int t = threadIdx.y * 32 + threadIdx.x; t < 3 * N * nv; t += 128) Ts[t] = make_float2(tf[2 * t], tf[2 * t + 1]);
     __syncthreads();
@@ -1619,6 +1647,7 @@ __global__ void __launch_bounds__(32 * kPj1Warps, MINB) k_pj1(const float2 *__re
                                                         int nv, int Bp, int B, double dt, double kfac,
                                                         const double *__restrict__ cdt, double dv, double lv,
                                                         MomRow mr, float *__restrict__ Inc, double *__restrict__ part) {
+    lp_grid_wait();
     extern __shared__ __align__(16) float2 Ts[];  // [3][N][nv], then the pencils [kPj1Pen][5][N][32]
     float2 *Zs = Ts + 3 * N * nv;
     __shared__ double red[kPj1Warps][5][32];
@@ -1813,6 +1842,7 @@ constexpr size_t kScatSmem = sizeof(double) * (kScatRec * 5 * 33 + 32 * 5 + 8 * 
 __global__ void __launch_bounds__(256) k_scatter_inc(const float *__restrict__ Inc, int Bp, int B, int nv, int c0,
                                                      double *__restrict__ U, const double *__restrict__ lam,
                                                      double dv, double lv, MomRow mr) {
+    lp_grid_wait();
     extern __shared__ double ssm[];
     double(*S)[5][33] = reinterpret_cast<double(*)[5][33]>(ssm);  // [record][coefficient][cell]
     // the cells' multipliers, converted to FP32 once here (the correction is
@@ -1894,6 +1924,7 @@ __global__ void __launch_bounds__(160) k_lambda_inc(const double *__restrict__ t
                                                     const double *__restrict__ gm_inv, double scale, double kfac,
                                                     const double *__restrict__ cdt, int Bp,
                                                     double *__restrict__ lam) {
+    lp_grid_wait();
     // one block of five warps per cell: warp m sums moment m of the
     // increments' partials (and of the target's, two-species operator) over
     // a fixed strided subset per lane and a fixed butterfly of shuffles;
@@ -1936,6 +1967,7 @@ __global__ void __launch_bounds__(160) k_lambda_inc(const double *__restrict__ t
 constexpr int kChargeChunk = 1024;
 __global__ void __launch_bounds__(256) k_charge_seq(const double *__restrict__ U, int nv3, double scalev,
                                                    double *__restrict__ rt) {
+    lp_grid_wait();
     __shared__ double term[2][3][kChargeChunk];
     const int s = blockIdx.x, t = threadIdx.x;
     const double *base = U + 7 * (long long)s * nv3;
@@ -1989,6 +2021,7 @@ __device__ __forceinline__ void charge_block_sum(double a0, double a1, double a2
 // the same records (one record per thread, 128 records per block).
 __global__ void __launch_bounds__(128) k_state_f32(const double *__restrict__ U, long long size,
                                                   float *__restrict__ Uf, double *__restrict__ part) {
+    lp_grid_wait();
     const long long k = blockIdx.x * 128ll + threadIdx.x;
     double a0 = 0., a1 = 0., a2 = 0.;
     if (k < size) {
@@ -2011,6 +2044,7 @@ __global__ void __launch_bounds__(128) k_state_f32(const double *__restrict__ U,
 __global__ void k_poisson(PoissonDev pd, const double *__restrict__ rt, int npart, double *__restrict__ bg,
                           double *__restrict__ potc, double *__restrict__ phix, double *__restrict__ phiy,
                           double *__restrict__ fields) {
+    lp_grid_wait();
     extern __shared__ double b[];
     const int t = threadIdx.x, nc = pd.nx * pd.ny, nd = pd.ndim;
     const bool fast = pd.rdiag != nullptr;
@@ -2284,6 +2318,7 @@ __global__ void __launch_bounds__(128) k_flux(AdvectDev ad, const double *__rest
                                              const S *__restrict__ Uin, const double *__restrict__ fields, int stage,
                                              double *__restrict__ Uout, float *__restrict__ Uoutf,
                                              double *__restrict__ part) {
+    lp_grid_wait();
     const long long k = blockIdx.x * 128ll + threadIdx.x;
     double a0 = 0., a1 = 0., a2 = 0.;
     if (k < ad.size) {
@@ -2317,6 +2352,7 @@ __global__ void __launch_bounds__(128) k_flux(AdvectDev ad, const double *__rest
 // part[3 * group] = (sum U0 + U6/4, sum U1, sum U2).
 __global__ void __launch_bounds__(128) k_state_f32_grp(const double *__restrict__ U, long long size,
                                                       float *__restrict__ Uf, double *__restrict__ part) {
+    lp_grid_wait();
     const int lane = threadIdx.x & 31;
     const long long g = blockIdx.x * 4ll + (threadIdx.x >> 5);
     double a0 = 0., a1 = 0., a2 = 0.;
@@ -2353,6 +2389,7 @@ __global__ void __launch_bounds__(128) k_flux_inc(AdvectDev ad, const float *__r
                                                  const float *__restrict__ Uf0, const double *__restrict__ fields,
                                                  float *__restrict__ S, float *__restrict__ Uoutf,
                                                  double *__restrict__ U, float *__restrict__ ipart) {
+    lp_grid_wait();
     const long long k = blockIdx.x * 128ll + threadIdx.x;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
     if (k < ad.size) {
@@ -2395,6 +2432,7 @@ __global__ void __launch_bounds__(128) k_flux_inc(AdvectDev ad, const float *__r
 // integrals (one thread per cell; pois2d P:1292-1467).
 __global__ void k_prhs(PoissonDev pd, const double *__restrict__ base, const float *__restrict__ inc,
                        double iscale, int npart, double *__restrict__ b) {
+    lp_grid_wait();
     const int lane = threadIdx.x & 31;
     const int ii = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (ii >= pd.nx * pd.ny) return;
@@ -2422,6 +2460,7 @@ __global__ void k_prhs(PoissonDev pd, const double *__restrict__ base, const flo
 
 __global__ void k_psolve_dense(const double *__restrict__ Ainv, const double *__restrict__ b, int nd,
                                double *__restrict__ x) {
+    lp_grid_wait();
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= nd) return;
@@ -2435,6 +2474,7 @@ __global__ void k_psolve_dense(const double *__restrict__ Ainv, const double *__
 
 __global__ void k_pfields(PoissonDev pd, const double *__restrict__ b, double *__restrict__ phix,
                           double *__restrict__ phiy, double *__restrict__ fields) {
+    lp_grid_wait();
     const int nc = pd.nx * pd.ny;
     const int ii = blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= nc) return;
@@ -2493,6 +2533,7 @@ __constant__ float c_gl_w[5] = {0.5688888888888889f, 0.4786286704993665f, 0.4786
                                 0.2369268850561891f, 0.2369268850561891f};
 __global__ void __launch_bounds__(256) k_entropy(const double *__restrict__ U, long long kend,
                                                 double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[256];
     double acc = 0.;
     for (long long k = blockIdx.x * 256ll + threadIdx.x; k < kend; k += 256ll * gridDim.x) {
@@ -2535,6 +2576,7 @@ __global__ void __launch_bounds__(256) k_entropy(const double *__restrict__ U, l
 // out[(i1*4 + a) * (nv*4) + j1*4 + b].
 __global__ void k_marginal_x1v1(const double *__restrict__ U, int nx1, int nx2, int nv, double dx, double dv,
                                 double lv, double *__restrict__ out) {
+    lp_grid_wait();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int npv = nv * 4;
     if (t >= nx1 * 4 * npv) return;
@@ -2564,6 +2606,7 @@ __global__ void k_marginal_x1v1(const double *__restrict__ U, int nx1, int nx2, 
 // Eight independent dependent chains per thread of packed FP32x2 FMAs (two
 // FMAs each) or of FP64 FMAs; the result is written so nothing is elided.
 __global__ void k_fma_f32(int iters, double *sink) {
+    lp_grid_wait();
     unsigned long long a[8], b = pk2(1.0000001f, 0.9999999f), c = pk2(1e-7f, -1e-7f);
 #pragma unroll
     for (int q = 0; q < 8; ++q) a[q] = pk2((float)threadIdx.x + q, (float)blockIdx.x);
@@ -2576,6 +2619,7 @@ __global__ void k_fma_f32(int iters, double *sink) {
     if (sum == 1234.5f) sink[0] = sum;
 }
 __global__ void k_fma_f64(int iters, double *sink) {
+    lp_grid_wait();
     double a[8];
     const double b = 1.0000000001, c = 1e-12;
 #pragma unroll
@@ -2592,6 +2636,7 @@ __global__ void k_fma_f64(int iters, double *sink) {
 // ---------------------------------------------------------------- moments
 __global__ void k_moments(const double *__restrict__ U, long long size, long long kend, int nv, double lv,
                           double dv, double *__restrict__ part) {
+    lp_grid_wait();
     __shared__ double red[5][256];
     const int t = threadIdx.x;
     double m = 0, a1 = 0, a2 = 0, a3 = 0, ke = 0;

@@ -12,6 +12,16 @@
 
 namespace lp {
 
+#ifdef __CUDACC__
+// Every kernel of the library starts with this: under a programmatic
+// dependency (the step graphs' kernel-to-kernel edges, which let a grid be
+// launched while the previous one still runs) it returns once the grids this
+// one depends on have completed and their writes are visible, so no kernel
+// reads anything before its predecessors are done.  Under an ordinary launch
+// it returns at once.
+__device__ __forceinline__ void lp_grid_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
+
 template <typename R> struct V2;
 template <> struct V2<double> { using t = double2; };
 template <> struct V2<float> { using t = float2; };

@@ -38,11 +38,17 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 double *g_scratch_addr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;
 
+// A kernel launched as a programmatic dependent (inside a caller's graph
+// whose edges allow early launch) reads nothing before its predecessors have
+// completed; under an ordinary launch this returns at once.
+__device__ __forceinline__ void na_grid_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // t_m = sum over the chunk of Re/Im(q) times the constraint rows
 // (conserveAllMoments, source/conservationRoutines.cpp:109-117), one block per
 // (chunk, cell), reference layout q[cell][n3].
 __global__ void k_na_partial(const double2 *__restrict__ q, const double *__restrict__ c1,
                              const double *__restrict__ c2, int n3, double *__restrict__ part) {
+    na_grid_wait();
     __shared__ double red[5][256];
     const int cell = blockIdx.y, k = blockIdx.x, t = threadIdx.x;
     const int cs = (n3 + kChunks - 1) / kChunks, p0 = k * cs, p1 = min(n3, p0 + cs);
@@ -69,6 +75,7 @@ __global__ void k_na_partial(const double2 *__restrict__ q, const double *__rest
 // lambda = (C C^T)^-1 t per cell (solveWithCCt, conservationRoutines.cpp:49-55).
 __global__ void k_na_lambda(const double *__restrict__ part, const double *__restrict__ cct, int ncell,
                             double *__restrict__ lam) {
+    na_grid_wait();
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= ncell) return;
     double t[5] = {0, 0, 0, 0, 0};
@@ -84,6 +91,7 @@ __global__ void k_na_lambda(const double *__restrict__ part, const double *__res
 // q -= C^T lambda (conservationRoutines.cpp:121-126).
 __global__ void k_na_apply(double2 *__restrict__ q, const double *__restrict__ c1, const double *__restrict__ c2,
                            const double *__restrict__ lam, int n3, long long total) {
+    na_grid_wait();
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid >= total) return;
     const int cell = (int)(tid / n3), pt = (int)(tid % n3);

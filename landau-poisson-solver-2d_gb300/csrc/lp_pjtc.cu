@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(kThreads) k_pj3_tc(const QT *__restrict__ q0, 
                                                      int nv, int NP, int tcols, int Bp, float2 *__restrict__ Y,
                                                      const float *__restrict__ cf, const double *__restrict__ lam4,
                                                      int *__restrict__ err) {
+    lp_grid_wait();
     constexpr int K = 2 * N, KC = K / 4;  // K of the real GEMM, its 16-byte core columns
     constexpr int NH = N / 2;             // k3 values per thread (a multiple of 4)
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -224,6 +225,7 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
                                                      const double *__restrict__ cdt, double dv, double lv, PjMom mr,
                                                      float *__restrict__ Inc, double *__restrict__ part,
                                                      int *__restrict__ err) {
+    lp_grid_wait();
     constexpr int K = 2 * N, KC = K / 4, NH = N / 2;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t bbytes = (uint32_t)3 * nvp * K * 4;
@@ -393,6 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_pj1_tc(const float2 *__restrict__ 
 template <int N>
 __global__ void __launch_bounds__(kThreads) k_pj2_tc(const float2 *__restrict__ Y, const float *__restrict__ btab,
                                                      int nv, int Bp, float2 *__restrict__ Z, int *__restrict__ err) {
+    lp_grid_wait();
     constexpr int K = 2 * N, KC = K / 4, NH = N / 2;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t bbytes = (uint32_t)6 * nv * K * 4;

@@ -34,7 +34,7 @@ EXPORTS = [
     "lp_device_bytes", "lp_set_state", "lp_get_state", "lp_state_device_ptr", "lp_set_init",
     "lp_fft3d", "lp_fs", "lp_compute_q", "lp_conserve", "lp_rk4_cell", "lp_nodes",
     "lp_weights_rows", "lp_conservation_rows", "lp_poisson", "lp_last_fields", "lp_advect_step",
-    "lp_collision_step", "lp_collision_graph_kernels", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
+    "lp_collision_step", "lp_collision_graph_kernels", "lp_collision_graph_edges", "lp_step", "lp_moments", "lp_time_kernel", "lp_measure_fp_peaks",
     "lp_conserve_noalloc",
     "lp_batch_create", "lp_batch_destroy", "lp_batch_set_stream", "lp_batch_synchronize",
     "lp_batch_last_error", "lp_batch_device_bytes", "lp_batch_set_state", "lp_batch_get_state",
@@ -128,6 +128,7 @@ def lib():
         L.lp_advect_step.argtypes = [_vp]
         L.lp_collision_step.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
         L.lp_collision_graph_kernels.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+        L.lp_collision_graph_edges.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
         L.lp_step.argtypes = [_vp, ctypes.c_int]
         L.lp_moments.argtypes = [_vp, _dp]
         L.lp_time_kernel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _dp]
@@ -367,6 +368,14 @@ class Context:
         every collided cell (0 before the first such step)."""
         k = ctypes.c_int()
         self._chk(self.L.lp_collision_graph_kernels(self.h, ctypes.byref(k)))
+        return k.value
+
+    def collision_graph_edges(self):
+        """Programmatic kernel-to-kernel edges of that graph (0 before the
+        first such step, and unless LP_PDL=1 or 2 was in the environment at
+        capture)."""
+        k = ctypes.c_int()
+        self._chk(self.L.lp_collision_graph_edges(self.h, ctypes.byref(k)))
         return k.value
 
     def step(self, nsteps=1):
