@@ -106,9 +106,17 @@ __global__ void __launch_bounds__(128) k_fq_x1(const float2 *__restrict__ F, con
     auto st = [&](int k, float2 v) { dst[k * ks] = v; };
     float2 x[N];
     if (arr < 7) {
-        const float *cp = C + (size_t)arr * n * n * n + (size_t)lm * n;
+        // the pencil's n weights are contiguous and 16-byte aligned (n a
+        // multiple of 4, C from cudaMalloc): n / 4 vector loads
+        const float4 *cp = reinterpret_cast<const float4 *>(C + (size_t)arr * n * n * n + (size_t)lm * n);
 #pragma unroll
-        for (int q = 0; q < n; ++q) x[q] = cscale(src[(size_t)q * Bp], __ldg(cp + q));
+        for (int q4 = 0; q4 < n / 4; ++q4) {
+            const float4 w = __ldg(cp + q4);
+            x[4 * q4] = cscale(src[(size_t)(4 * q4) * Bp], w.x);
+            x[4 * q4 + 1] = cscale(src[(size_t)(4 * q4 + 1) * Bp], w.y);
+            x[4 * q4 + 2] = cscale(src[(size_t)(4 * q4 + 2) * Bp], w.z);
+            x[4 * q4 + 3] = cscale(src[(size_t)(4 * q4 + 3) * Bp], w.w);
+        }
         fwd_pencil_st<N, true>(x, tw.fa, st);
     } else {
 #pragma unroll
