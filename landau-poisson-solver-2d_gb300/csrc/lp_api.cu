@@ -61,6 +61,12 @@ struct lp_ctx {
     int fq_bs = 0;
     int fq_form = 1;  // 1: fused (axis-2 spectra on chip), 0: three passes through DRAM
     lp::FftTw ftw{};
+    // the same form in FP64 for the FP64 path: omega factors, twiddles and
+    // the scratch of fq64_bs cells (nullptr: the pair form)
+    double *FQC64 = nullptr;
+    double2 *fscr64 = nullptr;
+    int fq64_bs = 0;
+    lp::FftTw64 ftw64{};
     // two-species variant: linear weight table (R precision), window offsets,
     // the linear term's workspace and CCt_linear embedded in a 5x5 matrix
     void *WLin = nullptr;
@@ -432,6 +438,25 @@ template <typename R> lp_status upload_tables(lp_ctx *c) {
         LP_CUDA(lp::launch_pairs(c->eta, c->shat, c->ahat, c->rzero, c->cw, c->pair_off, T.n,
                                  std::is_same<R, double>::value ? (double *)P : nullptr,
                                  std::is_same<R, float>::value ? (float *)P : nullptr, c->PI, c->stream));
+        // FP64 path: the convolution form in FP64 where the node grid is
+        // uniform.  The form needs eta(xi) - eta(omega) = (xi - omega) h_eta;
+        // with defect F11 left in (n = 24) the middle node is 8.9e-16 instead
+        // of 0, the weight there is that of a node off zero, and the pair form
+        // (the reference's own evaluation) is kept.  Elsewhere the two forms
+        // agree to 1e-14 (relative L2) at every n.  LP_FQ64=0 in the
+        // environment keeps the pair form, for comparisons.
+        const char *fenv = std::getenv("LP_FQ64");
+        if (!c->mixed && lp::fftq_supported(T.n) && T.eta[T.n / 2] == 0.0 && !(fenv && fenv[0] == '0')) {
+            std::vector<double> C;
+            lp::fftq_coefficients64(T.shat.data(), T.ahat.data(), T.cw.data(), T.h_eta, T.n, C);
+            LP_TRY(upload(c, &c->FQC64, C.data(), C.size()));
+            // chunks of 32 cells or more while the scratch stays within 512 MB
+            const size_t per_cell = lp::fftq_scratch_elems64(T.n, 1) * sizeof(double2);
+            const int fit = (int)std::min<size_t>((size_t)c->Bcap, (512ull << 20) / per_cell) / 32 * 32;
+            c->fq64_bs = std::min(c->Bcap, std::max(32, fit));
+            LP_TRY(dalloc(c, &c->fscr64, lp::fftq_scratch_elems64(T.n, c->fq64_bs)));
+            c->ftw64 = lp::fftq_twiddles64(T.n);
+        }
     }
     if (T.prm.linear_ei) {
         LP_TRY(upload(c, &c->win_off, T.win_off.data(), T.win_off.size()));
@@ -596,6 +621,15 @@ template <typename R> lp_status contract(lp_ctx *c, int Bp, double2 *q, float2 *
                                          double *lam = nullptr) {
     using C = typename V2<R>::t;
     const lp::Tables &T = c->T;
+    if constexpr (std::is_same<R, double>::value) {
+        if (c->FQC64 && !q32) {
+            for (int c0 = 0; c0 < Bp; c0 += c->fq64_bs)
+                LP_CUDA(lp::launch_computeq_fft64((const double2 *)c->F, c->FQC64, c->ftw64, T.n, Bp, c0,
+                                                  std::min(c->fq64_bs, Bp - c0), c->fscr64, c->fq64_bs, q,
+                                                  c->stream));
+            return LP_OK;
+        }
+    }
     if (c->FQC && c->line_warps == 0) {
         lp::ConsFused cons;
         if (lam) {

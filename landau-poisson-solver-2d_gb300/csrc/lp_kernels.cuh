@@ -132,15 +132,20 @@ cudaError_t launch_computeq_lines(const float2 *F, const float *W, const long lo
 // weight splits into seven omega-factors C[7][n^3] times polynomials in u,
 // so q is a sum of seven windowed convolutions, evaluated with M = 3n/2
 // point DFTs along axes 2 and 3 and summed directly along axis 1.
-struct FftTw {
-    float2 fw[48];  // exp(-2 pi i q2 k1 / M) at q2 * 6 + k1
-    float2 fa[48];  // fw exp(2 pi i k1 / 3): the a-side, output shift n/2
-    float2 iv[48];  // conj(fw) / M
+template <typename C> struct FftTwT {
+    C fw[48];  // exp(-2 pi i q2 k1 / M) at q2 * 6 + k1
+    C fa[48];  // fw exp(2 pi i k1 / 3): the a-side, output shift n/2
+    C iv[48];  // conj(fw) / M
 };
+using FftTw = FftTwT<float2>;
+using FftTw64 = FftTwT<double2>;
 bool fftq_supported(int n);
 FftTw fftq_twiddles(int n);
+FftTw64 fftq_twiddles64(int n);
 void fftq_coefficients(const double *shat, const double *ahat, const double *cw, double h_eta, int n,
                        std::vector<float> &C);
+void fftq_coefficients64(const double *shat, const double *ahat, const double *cw, double h_eta, int n,
+                         std::vector<double> &C);
 size_t fftq_gh_elems(int n, int Bs);       // axis-1 sums and inverse axis-2 outputs
 size_t fftq_scratch_elems(int n, int Bs);  // float2 elements for Bs cells
 // Cells [c0, c0 + Bc) of F and q (stride Bp); Bc and c0 multiples of 32,
@@ -169,6 +174,14 @@ cudaError_t launch_computeq_fft(const float2 *F, const float *C, const FftTw &tw
                                 float2 *scratch, int Bs, double2 *q, cudaStream_t st, int stage = -1,
                                 float2 *q32 = nullptr, const ConsFused *cons = nullptr, int form = 0,
                                 int *err = nullptr);
+// FP64 path, the same contraction in FP64 (the three-pass kernels at
+// double precision): F and q FP64 complex, C the seven omega-factors in FP64,
+// scratch of fftq_scratch_elems64(n, Bs) double2 elements.  Where the node
+// grid is uniform (eta[n/2] exactly 0) its sums agree with the direct
+// weighted sum of the pair form to 1e-14 (relative L2).
+size_t fftq_scratch_elems64(int n, int Bs);
+cudaError_t launch_computeq_fft64(const double2 *F, const double *C, const FftTw64 &tw, int n, int Bp, int c0,
+                                  int Bc, double2 *scratch, int Bs, double2 *q, cudaStream_t st);
 // The fused form's stages 0 and 2 (lp_fqf.cu) on X1 and H of the scratch,
 // and the X1 elements it needs for Bs cells.
 cudaError_t launch_fq_fused(int n, const float2 *F, const float *C, const FftTw &tw, int Bp, int c0, int Bc,
