@@ -3,8 +3,9 @@ n in {8, 16, 24, 32} on a uniform node grid.
 
 - Against the reference's golden ComputeQ at n = 8 and 16 (its own grids,
   no fixes) to 1e-12.
-- Against the pair form (LP_FQ64=0 at context creation), ComputeQ and whole
-  collision steps at every n, to 1e-13 (measured: 1.5e-15 to 6.6e-15).
+- Against the pair form (LP_FQ64=0 at context creation) at every n:
+  ComputeQ to 1e-13 (measured 1.5e-15 to 6.6e-15), a whole collision
+  step's increment to 1e-11 (measured 3.1e-13 at n = 16).
 - Against the oracle to 1e-12, and to 1e-11 at n = 32.  The oracle sums the
   same weighted terms in another order, and the terms cancel more as n
   grows; both GPU forms differ from it by the same amount (measured
@@ -24,7 +25,10 @@ from oracle.oracle import Case, FIX_DEFAULT, Oracle
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12       # FP64 against the reference's golden values
-TOL_FORMS = 1e-13  # the two FP64 forms on the GPU
+TOL_FORMS = 1e-13  # ComputeQ of the two FP64 forms on the GPU
+# a collision step's increment (a small difference after four stages, the
+# conservation and the projection) of the two forms: 3.1e-13 at n = 16
+TOL_STEP = 1e-11
 TOL_ORACLE = {8: 1e-12, 16: 1e-12, 24: 1e-12, 32: 1e-11}
 
 
@@ -100,4 +104,4 @@ def test_collision_step(gpu_lib, monkeypatch, nx1, nx2, n, nv):
         assert np.all(np.abs(m1[1:4] - m0[1:4]) / abs(m0[0]) < 1e-12)
         assert abs(m1[4] - m0[4]) / abs(m0[4]) < 1e-12
         out.append(ctx.get_state() - U0)
-    assert rel(out[0], out[1]) < TOL_FORMS
+    assert rel(out[0], out[1]) < TOL_STEP
