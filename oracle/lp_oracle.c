@@ -127,6 +127,15 @@ static inline double weight_of(const lpo_ctx *c, int xi, int om)
 
 double lpo_weight(const lpo_ctx *c, int xi, int om) { return weight_of(c, xi, om); }
 
+/* The omega tables weight_of reads (C:30-69): ahat (n3), Shat (n3 x 6: 00, 01,
+ * 02, 11, 12, 22) and the nodes |omega| == 0, whose weight omits ahat. */
+void lpo_omega_tables(const lpo_ctx *c, double *ah, double *sh, unsigned char *rz)
+{
+    memcpy(ah, c->ah, sizeof(double) * (size_t)c->n3);
+    memcpy(sh, c->sh, sizeof(double) * 6 * (size_t)c->n3);
+    memcpy(rz, c->rzero, (size_t)c->n3);
+}
+
 /* ---------------------------------------------------------- conservation */
 static double sinc_(double x) { return x == 0.0 ? 1.0 : sin(x) / x; }
 

@@ -44,6 +44,7 @@ void lpo_destroy(lpo_ctx *c);
 void lpo_grids(const lpo_ctx *c, double *v, double *eta, double *wt, double *sc);
 void lpo_cons(const lpo_ctx *c, double *c1, double *c2, double *cct);
 double lpo_weight(const lpo_ctx *c, int xi, int om);
+void lpo_omega_tables(const lpo_ctx *c, double *ah, double *sh, unsigned char *rz);
 void lpo_fft3d(const lpo_ctx *c, const double *in, double *out);
 void lpo_fs(const lpo_ctx *c, const double *in, double *out);
 void lpo_compute_q(const lpo_ctx *c, const double *f, double *qhat);

@@ -95,6 +95,7 @@ def _oracle_lib():
         L.lpo_destroy.argtypes = [ctypes.c_void_p]
         L.lpo_weight.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.lpo_weight.restype = ctypes.c_double
+        L.lpo_omega_tables.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         for name in ["lpo_grids", "lpo_cons", "lpo_fft3d", "lpo_fs", "lpo_compute_q",
                      "lpo_conserve", "lpo_intmodes", "lpo_rk4", "lpo_nodes", "lpo_set_init",
                      "lpo_poisson", "lpo_rk3", "lpo_collide", "lpo_step", "lpo_moments",
@@ -165,6 +166,13 @@ class Oracle:
 
     def weight(self, xi, om):
         return self.L.lpo_weight(self.h, int(xi), int(om))
+
+    def omega_tables(self):
+        """ahat (n3), Shat (n3 x 6: 00, 01, 02, 11, 12, 22) and the |omega| == 0
+        flags that weight() reads: W = (0 if flag else ahat) - d^T Shat d."""
+        ah = np.zeros(self.n3); sh = np.zeros(6 * self.n3); rz = np.zeros(self.n3, np.uint8)
+        self.L.lpo_omega_tables(self.h, _p(ah), _p(sh), rz.ctypes.data_as(ctypes.c_void_p))
+        return ah, sh.reshape(-1, 6), rz.astype(bool)
 
     def fft3d(self, x):
         x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)

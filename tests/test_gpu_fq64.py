@@ -6,11 +6,14 @@ n in {8, 16, 24, 32} on a uniform node grid.
 - Against the pair form (LP_FQ64=0 at context creation) at every n:
   ComputeQ to 1e-13 (measured 1.5e-15 to 6.6e-15), a whole collision
   step's increment to 1e-11 (measured 3.1e-13 at n = 16).
-- Against the oracle to 1e-12, and to 1e-11 at n = 32.  The oracle sums the
-  same weighted terms in another order, and the terms cancel more as n
-  grows; both GPU forms differ from it by the same amount (measured
-  2.0e-14, 2.2e-13 and 9.0e-13 at n = 8, 16, 24; 5.0e-12 at n = 32 with
-  v in [-5.25, 5.25]^3).
+- Against the oracle to 1e-12, and to 1e-11 at n = 32.  Both GPU forms
+  differ from it by the same amount (measured 2.0e-14, 2.2e-13 and 9.0e-13
+  at n = 8, 16, 24; 5.0e-12 at n = 32 with v in [-5.25, 5.25]^3): they
+  start from the GPU's FP64 transform of f, which rounds differently from
+  the oracle's, and ComputeQ carries that absolute error into its small
+  outputs (tests/test_oracle_convolution_form.py measures the effect on the
+  oracle's own transform; there the convolution form's FP64 sums match the
+  oracle's direct sum to 1.2e-14).
 - The fallback where defect F11 leaves the middle node off zero (n = 24
   without the fix): the context keeps the pair form, so its results are the
   pair form's bit for bit."""
