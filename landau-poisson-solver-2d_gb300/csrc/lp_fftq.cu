@@ -1,4 +1,5 @@
-// ComputeQ of the mixed path as a sum of seven windowed convolutions.
+// ComputeQ as a sum of seven windowed convolutions (the mixed path in FP32,
+// the FP64 path in FP64).
 //
 // The reference's weight (source/collisionRoutines_1.cpp:30-69, used at
 // C:739-822) is gHat3(xi, omega) = ahat(omega) - d^T Shat(omega) d with
@@ -27,7 +28,8 @@
 //       (X1 and X2 in one kernel, the X1 outputs held in shared memory);
 //   Y   per (k2, k3): sum_p sum_l a_p(l) (u1-h)^e1 b_p(u1), u1 = i + h - l;
 //   Z1  inverse axis-2 DFT, only the n outputs xi2 + h;
-//   Z2  inverse axis-3 DFT, only the n outputs xi3 + h, written as FP64.
+//   Z2  inverse axis-3 DFT, only the n outputs xi3 + h, written as FP64
+//       (or FP32 for the mixed path's lazily conserved stages).
 //
 // The shift by h of the output window is the factor exp(2 pi i k h / M) =
 // exp(2 pi i k / 3) on the a-side spectra.  The M-point DFTs factor as
@@ -35,7 +37,9 @@
 // six S-point DFTs; the inverse is the conjugate transpose with only 4 of
 // the 6 outputs of its last stage kept.  A thread transforms one pencil of
 // one cell; the 32 lanes of a warp are 32 cells, so every load and store is
-// coalesced on the cell-minor arrays.  Arithmetic is FP32.
+// coalesced on the cell-minor arrays.  The kernels are templates on the real
+// type: FP32 for the mixed path (packed f32x2 FMAs in Y), FP64 for the FP64
+// path (Y in four output parts, its accumulators in registers).
 #include "lp_kernels.cuh"
 #include "lp_dev.cuh"
 #include "lp_fft.cuh"
