@@ -11,7 +11,10 @@ omega-factors with polynomials in u.  This model takes A and Shat from the
 oracle's own tables, forms the seven pairs as the GPU kernels do, convolves
 them with zero-padded FFTs in FP64 and compares with the oracle's sum.  It
 checks the algebra and the index window that the mixed path's and the FP64
-path's convolution kernels evaluate."""
+path's convolution kernels evaluate.  The two-species variant's linear term
+factorises the same way (nine convolutions of F-independent omega-factors
+with F times a polynomial in u, weighted by the output's node coordinate);
+its model is checked against the oracle's linear term here too."""
 from __future__ import annotations
 
 import numpy as np
@@ -114,3 +117,45 @@ def test_sensitivity_to_the_transform(n, bound):
     err = np.linalg.norm(q1 - q0) / np.linalg.norm(q0)
     assert bound / 30 < err < bound, err
 
+
+
+def linear_term_model(O, case, f):
+    """The two-species variant's linear term (lpo_compute_q_lin, after
+    source/collisionRoutines_1.cpp:551-635 with the weight of :71-96):
+    sum over omega of h_eta^3 wt wt wt scale3 Wlin(xi, omega) F(u) with
+    Wlin = -sum_ij Shat_ij(omega) eta(xi)_i (eta(xi)_j - eta(omega)_j).
+    With eta(xi)_j - eta(omega)_j = (u_j - h) h_eta it is
+    -scale3 sum_i eta(xi)_i sum_j (A_ij * B_j)(xi + h): nine convolutions of
+    the F-independent A_ij = cw Shat_ij with B_j = (u_j - h) h_eta F."""
+    n, h = case.n, case.n // 2
+    _, eta, wt, sc = O.grids()
+    h_eta, s3 = sc[1], sc[6]
+    _, sh, _ = O.omega_tables()
+    F = O.fft3d(f.astype(np.complex128)).reshape(n, n, n)
+    cw = (h_eta ** 3) * wt[:, None, None] * wt[None, :, None] * wt[None, None, :]
+    S = sh.reshape(n, n, n, 6)
+    sidx = [[0, 1, 2], [1, 3, 4], [2, 4, 5]]
+    d = (np.arange(n) - h) * h_eta
+    du = [d[:, None, None], d[None, :, None], d[None, None, :]]
+    ez = [eta[:, None, None], eta[None, :, None], eta[None, None, :]]
+    shape, ax = (2 * n,) * 3, (0, 1, 2)
+    Bh = [np.fft.fftn(du[j] * F, shape, axes=ax) for j in range(3)]
+    out = np.zeros((n, n, n), np.complex128)
+    for i in range(3):
+        acc = sum(np.fft.fftn(cw * S[..., sidx[i][j]], shape, axes=ax) * Bh[j] for j in range(3))
+        out += ez[i] * np.fft.ifftn(acc, axes=ax)[h:h + n, h:h + n, h:h + n]
+    return (-s3 * out).reshape(-1)
+
+
+@pytest.mark.parametrize("n", [8, 16, 24])
+def test_linear_term_as_convolutions(n):
+    case = Case(nx1=2, nx2=1, nv=4, n=n, lv=5.25, lx=4 * np.pi, nu=0.05, dt=0.01, a_amp=0.5, k_wave=0.5)
+    O = Oracle(case, fixes=FIX_DEFAULT)
+    v, _, _, _ = O.grids()
+    V1, V2, V3 = np.meshgrid(v, v, v, indexing="ij")
+    f = (np.exp(-((V1 - 0.7) ** 2 + V2 ** 2 + V3 ** 2) / 2)
+         + 0.4 * np.exp(-((V1 + 1.2) ** 2 + (V2 - 0.3) ** 2 + 1.5 * V3 ** 2) / 2)).reshape(-1)
+    _, ql = O.compute_q_lin(f)
+    qm = linear_term_model(O, case, f)
+    err = np.linalg.norm(qm - ql) / np.linalg.norm(ql)
+    assert err < 1e-13, err
